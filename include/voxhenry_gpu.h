@@ -1,0 +1,92 @@
+/*
+ * voxhenry_gpu.h -- C ABI of the GB300 (sm_103a) VoxHenry solve-path library (libvhgpu.so).
+ *
+ * The library replaces the MATLAB/Octave hot path of VoxHenry:
+ *   lse_matvect_mult            src_lse_formation/lse_matvect_mult.m:1
+ *   lse_sparse_precon_prepare   src_lse_formation/lse_sparse_precon_prepare.m:1
+ *   lse_sparse_precon_multiply  src_lse_formation/lse_sparse_precon_multiply.m:1
+ *   pgmres / fpgmres            src_iterative_solver/pgmres.m:70, fpgmres.m:58
+ * Conventions (as in the reference):
+ *   - complex values are interleaved (re, im) doubles;
+ *   - 3-D grids are column-major (x fastest), voxel indices 1-based (idxS);
+ *   - the incidence matrix Ae (num_node x 5*nv, port rows already removed, the
+ *     "Ar" of the executer) is passed in CSC form with 0-based row indices.
+ * Every call returns a vh_status; vh_last_error() gives the text of the last failure
+ * on a context.  Host pointers are borrowed for the duration of the call.
+ * A context owns one CUDA stream; calls on one context must not overlap.
+ */
+#ifndef VOXHENRY_GPU_H
+#define VOXHENRY_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum vh_status {
+  VH_OK = 0,
+  VH_ERR_BAD_ARG = 1,
+  VH_ERR_OOM = 2,
+  VH_ERR_UNSUPPORTED = 3,
+  VH_ERR_TIMEOUT = 4,
+  VH_ERR_NOT_CONVERGED = 5,
+  VH_ERR_CUDA = 6,
+  VH_ERR_NO_DEVICE = 7
+} vh_status;
+
+/* arithmetic of the FFT convolution: complex128, or complex64 with fp32 accumulation */
+typedef enum vh_prec { VH_PREC_FP64 = 0, VH_PREC_FP32 = 1 } vh_prec;
+
+/* preconditioner kinds of lse_sparse_precon_prepare.m:5,71,83,90 */
+typedef enum vh_precon_kind {
+  VH_PRECON_NONE = 0,        /* 'no_precond' */
+  VH_PRECON_SCHUR_INVERT = 1 /* 'schur_invert' : exact Schur complement, sparse LDL^T */
+} vh_precon_kind;
+
+typedef struct vh_ctx vh_ctx;
+typedef struct vh_geom vh_geom;
+typedef struct vh_precon vh_precon;
+
+/* ---- context ----------------------------------------------------------------------------- */
+int vh_version(void);
+const char* vh_status_string(vh_status s);
+vh_status vh_ctx_create(int device, vh_ctx** out);
+void vh_ctx_destroy(vh_ctx* ctx);
+const char* vh_last_error(const vh_ctx* ctx);
+vh_status vh_ctx_synchronize(vh_ctx* ctx);
+
+/* ---- geometry: the fixed arguments of lse_matvect_mult (lse_matvect_mult.m:1) ------------------
+ * fN_all      : circulant tensor spectrum, complex (2L, 2M, 2N, 7) column-major.  The drop-in passes
+ *               the per-frequency fN_all = (j w mu) fN_all2 (VoxHenry_executer.m:266); the batched
+ *               solver passes fN_all2 and a per-RHS scale j w mu.
+ * idxS        : nv sorted 1-based linear indices of non-empty voxels (pre_define_structure_params.m:6-14);
+ *               idxS5 of the reference is [idxS; idxS+LMN; ... ; idxS+4LMN].
+ * Ae          : num_node x 5nv CSC (jc: 5nv+1 offsets, ir: 0-based rows, pr: values).
+ * z_real      : (L,M,N) real; z_imag : (L,M,N) complex or NULL (VoxHenry_executer.m:231-259).
+ * want_fp32   : also keep a complex64 copy of the tensor for VH_PREC_FP32 products.            */
+vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const double* fN_all, int64_t nv,
+                         const int64_t* idxS, int64_t num_node, const int64_t* Ae_jc, const int64_t* Ae_ir,
+                         const double* Ae_pr, const double* z_real, const double* z_imag, int want_fp32,
+                         vh_geom** out);
+void vh_geom_destroy(vh_geom* g);
+/* sizes: n_curr = 5 nv, n_node = rows of Ae, n = n_curr + n_node */
+vh_status vh_geom_sizes(const vh_geom* g, int64_t* n_curr, int64_t* n_node, int64_t* n);
+/* replaces z (per-voxel) in slot `slot` (0 = the z given at creation).  Superconductors have an
+ * omega-dependent z; one slot per frequency.  z_imag may be NULL. */
+vh_status vh_geom_set_z(vh_geom* g, int slot, const double* z_real, const double* z_imag);
+
+/* ---- matvec: JOut_full = lse_matvect_mult(JIn0, ...) for B right-hand sides ---------------------
+ * x, y   : HOST arrays, B x n complex (RHS b at offset b*n).
+ * scale  : B complex factors multiplying the tensor (NULL: all 1, the drop-in form).
+ * zslot  : B slot numbers (NULL: slot 0 for all).                                                */
+vh_status vh_matvec(vh_geom* g, int B, const double* x, double* y, const double* scale, const int* zslot,
+                    vh_prec prec);
+/* same with DEVICE pointers, enqueued on the context stream (no synchronisation) */
+vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, const void* scale_dev,
+                           const int* zslot, vh_prec prec);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VOXHENRY_GPU_H */

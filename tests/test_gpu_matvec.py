@@ -1,0 +1,136 @@
+"""FFT matvec parity: GPU (through the C ABI) vs the CPU oracle's lse_matvect_mult."""
+import numpy as np
+import pytest
+
+from conftest import golden_vhr_text
+from oracle import circulant, solver, structure, vhr
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12     # single FP64 matvec, relative 2-norm
+FP32_TOL = 2e-6      # complex64 FFT convolution, relative 2-norm
+
+
+@pytest.fixture(scope="module")
+def vie():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from voxhenry_gb300 import vie as v
+
+    return v
+
+
+def system_of(w):
+    S = structure.build_system(w.sigma_e, w.lambdaL, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, st = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
+    return S, fN, st
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def rand_c(rng, n):
+    return rng.standard_normal(n) + 1j * rng.standard_normal(n)
+
+
+GRIDS = [(2, 4, 4), (6, 5, 4), (5, 7, 3), (12, 10, 9), (16, 8, 8), (20, 6, 5)]
+
+
+@pytest.mark.parametrize("shape", GRIDS)
+def test_matvec_fp64_random_grids(vie, shape):
+    from voxhenry_gb300 import geometry
+
+    w = geometry.random_blob(shape, fill=0.65, seed=sum(shape))
+    S, fN, st = system_of(w)
+    f = 2.5e9
+    jwmu = 1j * 2 * np.pi * f * solver.MU0
+    fNf = jwmu * fN
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 2 * np.pi * f)
+    rng = np.random.default_rng(3)
+    x = rand_c(rng, S.n)
+    ref = solver.lse_matvect_mult(x, fNf, S.Ar, z_real, None, S.dx, S.idxS5)
+    got = vie.lse_matvect_mult(x, fNf, S.Ar, z_real, None, S.dx, S.idxS5)
+    assert rel(got, ref) < FP64_TOL
+
+
+def test_matvec_numex1_reference_input(vie):
+    """The reference's own numex1 input (60 x 20 x 20, padded 120 x 40 x 40: radices 2, 3, 5)."""
+    inp = vhr.read_vhr_text(golden_vhr_text("straight_cond1_len30.0u_wid10.0u_dist20.0u.vhr"))
+    S = structure.build_system(inp.sigma_e, None, inp.dx, inp.pnt_lft, inp.pnt_rght)
+    fN, st = circulant.generate_circulant_tensor(inp.dx, 1.0, S.L, S.M, S.N)
+    f = 1e10
+    fNf = (1j * 2 * np.pi * f * solver.MU0) * fN
+    z_real, _ = solver.z_arrays(inp.sigma_e, None, 2 * np.pi * f)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        x = rand_c(rng, S.n)
+        ref = solver.lse_matvect_mult(x, fNf, S.Ar, z_real, None, S.dx, S.idxS5)
+        got = vie.lse_matvect_mult(x, fNf, S.Ar, z_real, None, S.dx, S.idxS5)
+        assert rel(got, ref) < FP64_TOL
+
+
+def test_matvec_superconductor(vie):
+    """z_imag present (two-fluid superconductor, VoxHenry_executer.m:236-259)."""
+    from voxhenry_gb300 import geometry
+
+    w = geometry.random_blob((8, 6, 5), fill=0.7, seed=11)
+    lam = np.where(w.sigma_e > 0, 5e-8, 0.0)
+    w.lambdaL = np.asfortranarray(lam)
+    S, fN, st = system_of(w)
+    f = 5e9
+    om = 2 * np.pi * f
+    z_real, z_imag = solver.z_arrays(w.sigma_e, w.lambdaL, om)
+    fNf = (1j * om * solver.MU0) * fN
+    x = rand_c(np.random.default_rng(9), S.n)
+    ref = solver.lse_matvect_mult(x, fNf, S.Ar, z_real, z_imag, S.dx, S.idxS5)
+    got = vie.lse_matvect_mult(x, fNf, S.Ar, z_real, z_imag, S.dx, S.idxS5)
+    assert rel(got, ref) < FP64_TOL
+
+
+def test_matvec_batched_scales_and_slots(vie):
+    """B right-hand sides with per-RHS j*omega*mu and per-RHS z: each equals its single-RHS product."""
+    from voxhenry_gb300 import geometry
+
+    w = geometry.random_blob((10, 8, 6), fill=0.6, seed=21)
+    S, fN, st = system_of(w)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)
+    z2 = z_real * 1.7
+    g.set_z(1, z2)
+    freqs = np.array([1e3, 1e6, 1e9, 2e10])
+    scales = 1j * 2 * np.pi * freqs * solver.MU0
+    slots = np.array([0, 1, 0, 1], dtype=np.int32)
+    rng = np.random.default_rng(2)
+    X = np.stack([rand_c(rng, S.n) for _ in freqs])
+    Yb = g.matvec(X, scale=scales, zslot=slots)
+    for b in range(len(freqs)):
+        zr = z_real if slots[b] == 0 else z2
+        ref = solver.lse_matvect_mult(X[b], scales[b] * fN, S.Ar, zr, None, S.dx, S.idxS5)
+        assert rel(Yb[b], ref) < FP64_TOL
+        single = g.matvec(X[b], scale=scales[b], zslot=int(slots[b]))
+        assert np.array_equal(single, Yb[b])      # batching invariance: bitwise
+    Y32 = g.matvec(X, scale=scales, zslot=slots, prec="fp32")
+    for b in range(len(freqs)):
+        assert rel(Y32[b], Yb[b]) < FP32_TOL
+
+
+def test_matvec_linearity_large(vie):
+    """Size-independent property at a BASELINE-sized grid (64 x 16 x 16 bar): A(ax + by) = aAx + bAy."""
+    from voxhenry_gb300 import geometry
+
+    w = geometry.bar()
+    S = structure.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, st = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS)
+    rng = np.random.default_rng(4)
+    x, y = rand_c(rng, S.n), rand_c(rng, S.n)
+    a, b = 0.3 - 1.1j, 2.0 + 0.5j
+    s = 1j * 2 * np.pi * 1e9 * solver.MU0
+    lhs = g.matvec(a * x + b * y, scale=s)
+    rhs = a * g.matvec(x, scale=s) + b * g.matvec(y, scale=s)
+    assert rel(lhs, rhs) < 1e-13
+    ref = solver.lse_matvect_mult(x, s * fN, S.Ar, z_real, None, S.dx, S.idxS5)
+    assert rel(g.matvec(x, scale=s), ref) < FP64_TOL

@@ -1,0 +1,93 @@
+"""ctypes binding of libvhgpu.so (declarations mirror include/voxhenry_gpu.h).
+
+The library is required: there is no CPU fallback.  Loading fails loudly when
+libvhgpu.so is missing (build it with ``voxhenry_gb300._build.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libvhgpu.so")
+
+VH_OK = 0
+STATUS = {0: "VH_OK", 1: "VH_ERR_BAD_ARG", 2: "VH_ERR_OOM", 3: "VH_ERR_UNSUPPORTED", 4: "VH_ERR_TIMEOUT",
+          5: "VH_ERR_NOT_CONVERGED", 6: "VH_ERR_CUDA", 7: "VH_ERR_NO_DEVICE"}
+PREC = {"fp64": 0, "fp32": 1}
+
+_p = C.c_void_p
+_i64p = C.POINTER(C.c_int64)
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "vh_version": (C.c_int, []),
+    "vh_status_string": (C.c_char_p, [C.c_int]),
+    "vh_ctx_create": (C.c_int, [C.c_int, C.POINTER(_p)]),
+    "vh_ctx_destroy": (None, [_p]),
+    "vh_last_error": (C.c_char_p, [_p]),
+    "vh_ctx_synchronize": (C.c_int, [_p]),
+    "vh_geom_create": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int64, _i64p, C.c_int64,
+                                 _i64p, _i64p, _dp, _dp, _dp, C.c_int, C.POINTER(_p)]),
+    "vh_geom_destroy": (None, [_p]),
+    "vh_geom_sizes": (C.c_int, [_p, _i64p, _i64p, _i64p]),
+    "vh_geom_set_z": (C.c_int, [_p, C.c_int, _dp, _dp]),
+    "vh_matvec": (C.c_int, [_p, C.c_int, _dp, _dp, _dp, _ip, C.c_int]),
+    "vh_matvec_device": (C.c_int, [_p, C.c_int, _p, _p, _p, _ip, C.c_int]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libvhgpu.so and declare every exported entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with voxhenry_gb300._build.build() (requires nvcc)")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class VHError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def check(status: int, ctx=None):
+    if status != VH_OK:
+        lib = load()
+        msg = lib.vh_last_error(ctx).decode() if ctx else lib.vh_status_string(status).decode()
+        raise VHError(status, msg)
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def i64ptr(a: np.ndarray):
+    return a.ctypes.data_as(_i64p) if a is not None else None
+
+
+def as_c128(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def as_f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def cview(a: np.ndarray):
+    """complex128 array -> pointer to interleaved doubles."""
+    return a.ctypes.data_as(_dp)

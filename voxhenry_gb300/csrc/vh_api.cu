@@ -1,0 +1,294 @@
+// C ABI entry points (include/voxhenry_gpu.h): context, geometry and matvec.
+#include <cstring>
+#include <vector>
+
+#include "../../include/voxhenry_gpu.h"
+#include "vh_internal.cuh"
+
+using namespace vh;
+
+namespace {
+
+template <typename F>
+vh_status guarded(vh_ctx* ctx, F&& f) {
+  try {
+    f();
+    return VH_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->last_error = e.msg;
+    return (vh_status)e.st;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->last_error = "host allocation failed";
+    return VH_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->last_error = e.what();
+    return VH_ERR_CUDA;
+  }
+}
+
+__global__ void k_fill_c(double2* p, int64_t n, double2 v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// z per non-empty voxel: z_real(idxS) + z_imag(idxS)
+__global__ void k_gather_z(const double* __restrict__ zr, const double2* __restrict__ zi, const int64_t* __restrict__ idx,
+                           int64_t nv, double2* __restrict__ out) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t li = idx[v] - 1;
+    double2 z = make_double2(zr[li], 0.0);
+    if (zi) { z.x += zi[li].x; z.y += zi[li].y; }
+    out[v] = z;
+  }
+}
+
+void set_z_slot(vh_geom* g, int slot, const double* z_real, const double* z_imag) {
+  VH_REQUIRE(slot >= 0 && slot < 4096, ERR_BAD_ARG, "z slot out of range");
+  VH_REQUIRE(z_real != nullptr, ERR_BAD_ARG, "z_real is required");
+  cudaStream_t st = g->ctx->stream;
+  const int64_t lmn = (int64_t)g->L * g->M * g->N;
+  if ((int)g->zslots.size() <= slot) g->zslots.resize(slot + 1, nullptr);
+  if (!g->zslots[slot]) VH_CUDA_TRY(cudaMalloc(&g->zslots[slot], std::max<int64_t>(1, g->nv) * sizeof(double2)));
+  double* d_zr = nullptr;
+  double2* d_zi = nullptr;
+  int64_t* d_idx = nullptr;
+  VH_CUDA_TRY(cudaMalloc(&d_zr, lmn * sizeof(double)));
+  VH_CUDA_TRY(cudaMalloc(&d_idx, std::max<int64_t>(1, g->nv) * sizeof(int64_t)));
+  if (z_imag) VH_CUDA_TRY(cudaMalloc(&d_zi, lmn * sizeof(double2)));
+  VH_CUDA_TRY(cudaMemcpyAsync(d_zr, z_real, lmn * sizeof(double), cudaMemcpyHostToDevice, st));
+  VH_CUDA_TRY(cudaMemcpyAsync(d_idx, g->idxS.data(), g->nv * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  if (z_imag) VH_CUDA_TRY(cudaMemcpyAsync(d_zi, z_imag, lmn * sizeof(double2), cudaMemcpyHostToDevice, st));
+  if (g->nv) k_gather_z<<<256, 256, 0, st>>>(d_zr, d_zi, d_idx, g->nv, g->zslots[slot]);
+  VH_CUDA_TRY(cudaGetLastError());
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(d_zr);
+  cudaFree(d_zi);
+  cudaFree(d_idx);
+}
+
+void ensure_ones(vh_geom* g, int B) {
+  if (B <= g->ones_cap) return;
+  cudaFree(g->ones);
+  g->ones = nullptr;
+  g->ones_cap = 0;
+  VH_CUDA_TRY(cudaMalloc(&g->ones, B * sizeof(double2)));
+  k_fill_c<<<1, 256, 0, g->ctx->stream>>>(g->ones, B, make_double2(1.0, 0.0));
+  VH_CUDA_TRY(cudaGetLastError());
+  g->ones_cap = B;
+}
+
+// Resolves per-RHS z slots to a (pointer, stride) pair.
+const double2* resolve_z(vh_geom* g, int B, const int* zslot, int64_t& zstride) {
+  int s0 = zslot ? zslot[0] : 0;
+  bool same = true;
+  for (int b = 0; zslot && b < B; ++b) same = same && zslot[b] == s0;
+  auto slot_ptr = [&](int s) {
+    VH_REQUIRE(s >= 0 && s < (int)g->zslots.size() && g->zslots[s], ERR_BAD_ARG, "z slot not set");
+    return g->zslots[s];
+  };
+  if (same) {
+    zstride = 0;
+    return slot_ptr(s0);
+  }
+  const size_t need = (size_t)B * g->nv;
+  if (need > g->zgather_cap) {
+    cudaFree(g->zgather);
+    g->zgather = nullptr;
+    g->zgather_cap = 0;
+    VH_CUDA_TRY(cudaMalloc(&g->zgather, need * sizeof(double2)));
+    g->zgather_cap = need;
+  }
+  for (int b = 0; b < B; ++b)
+    VH_CUDA_TRY(cudaMemcpyAsync(g->zgather + (size_t)b * g->nv, slot_ptr(zslot[b]), g->nv * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, g->ctx->stream));
+  zstride = g->nv;
+  return g->zgather;
+}
+
+}  // namespace
+
+namespace vh {
+// Full operator of lse_matvect_mult.m for B right-hand sides (device pointers, leading dimension n).
+void matvec_device(vh_geom* g, int B, const double2* x, double2* y, const double2* scale, const int* zslot, Prec prec) {
+  cudaStream_t st = g->ctx->stream;
+  if (!scale) {
+    ensure_ones(g, B);
+    scale = g->ones;
+  }
+  int64_t zstride = 0;
+  const double2* z = resolve_z(g, B, zslot, zstride);
+  if (g->nv > 0) conv_apply(g->conv, prec, B, x, g->n, y, g->n, scale, z, zstride, st);
+  // y_J -= Ae^T phi ; y_phi = Ae J   (lse_matvect_mult.m:138-140)
+  spmv_batched(g->AeT, B, x, g->n, g->nc, y, g->n, 0, -1, st);
+  spmv_batched(g->Ae, B, x, g->n, 0, y, g->n, g->nc, 0, st);
+}
+}  // namespace vh
+
+extern "C" {
+
+int vh_version(void) { return 100; }
+
+const char* vh_status_string(vh_status s) {
+  switch (s) {
+    case VH_OK: return "ok";
+    case VH_ERR_BAD_ARG: return "bad argument";
+    case VH_ERR_OOM: return "out of device memory";
+    case VH_ERR_UNSUPPORTED: return "unsupported";
+    case VH_ERR_TIMEOUT: return "timeout";
+    case VH_ERR_NOT_CONVERGED: return "not converged";
+    case VH_ERR_CUDA: return "CUDA error";
+    case VH_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+vh_status vh_ctx_create(int device, vh_ctx** out) {
+  if (!out) return VH_ERR_BAD_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return VH_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return VH_ERR_BAD_ARG;
+  auto* c = new vh_ctx();
+  c->device = device;
+  vh_status s = guarded(c, [&] {
+    VH_CUDA_TRY(cudaSetDevice(device));
+    VH_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  });
+  if (s != VH_OK) {
+    delete c;
+    return s;
+  }
+  *out = c;
+  return VH_OK;
+}
+
+void vh_ctx_destroy(vh_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* vh_last_error(const vh_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+vh_status vh_ctx_synchronize(vh_ctx* ctx) {
+  if (!ctx) return VH_ERR_BAD_ARG;
+  return guarded(ctx, [&] { VH_CUDA_TRY(cudaStreamSynchronize(ctx->stream)); });
+}
+
+vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const double* fN_all, int64_t nv,
+                         const int64_t* idxS, int64_t num_node, const int64_t* Ae_jc, const int64_t* Ae_ir,
+                         const double* Ae_pr, const double* z_real, const double* z_imag, int want_fp32,
+                         vh_geom** out) {
+  if (!ctx || !out) return VH_ERR_BAD_ARG;
+  *out = nullptr;
+  auto* g = new vh_geom();
+  vh_status s = guarded(ctx, [&] {
+    VH_REQUIRE(L >= 2 && M >= 2 && N >= 2, ERR_UNSUPPORTED, "grids thinner than 2 voxels are not supported");
+    VH_REQUIRE(dx > 0 && nv >= 0 && num_node >= 0, ERR_BAD_ARG, "bad sizes");
+    VH_REQUIRE(nv <= (int64_t)L * M * N, ERR_BAD_ARG, "nv exceeds the grid");
+    VH_REQUIRE(fN_all && (nv == 0 || idxS) && Ae_jc && z_real, ERR_BAD_ARG, "null input");
+    VH_REQUIRE(5 * nv < (1LL << 31), ERR_UNSUPPORTED, "too many current unknowns");
+    VH_CUDA_TRY(cudaSetDevice(ctx->device));
+    g->ctx = ctx;
+    g->L = L; g->M = M; g->N = N; g->dx = dx;
+    g->nv = nv; g->nc = 5 * nv; g->nphi = num_node; g->n = g->nc + g->nphi;
+    g->idxS.assign(idxS, idxS + nv);
+    cudaStream_t st = ctx->stream;
+    const int64_t P = 8LL * L * M * N;
+    double2* raw = nullptr;
+    VH_CUDA_TRY(cudaMalloc(&raw, 7 * P * sizeof(double2)));
+    cudaError_t e = cudaMemcpyAsync(raw, fN_all, 7 * P * sizeof(double2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+      try {
+        conv_plan_create(g->conv, L, M, N, dx, raw, nv, g->idxS.data(), want_fp32 != 0, st);
+      } catch (...) {
+        cudaFree(raw);
+        throw;
+      }
+    }
+    cudaFree(raw);
+    VH_CUDA_TRY(e);
+    csc_upload(num_node, g->nc, Ae_jc, Ae_ir, Ae_pr, g->Ae, g->AeT, st);
+    set_z_slot(g, 0, z_real, z_imag);
+  });
+  if (s != VH_OK) {
+    vh_geom_destroy(g);
+    return s;
+  }
+  *out = g;
+  return VH_OK;
+}
+
+void vh_geom_destroy(vh_geom* g) {
+  if (!g) return;
+  if (g->ctx) cudaSetDevice(g->ctx->device);
+  conv_plan_destroy(g->conv);
+  g->Ae.free_all();
+  g->AeT.free_all();
+  for (auto* z : g->zslots) cudaFree(z);
+  cudaFree(g->ones);
+  cudaFree(g->io_x);
+  cudaFree(g->io_y);
+  cudaFree(g->io_s);
+  cudaFree(g->zgather);
+  delete g;
+}
+
+vh_status vh_geom_sizes(const vh_geom* g, int64_t* n_curr, int64_t* n_node, int64_t* n) {
+  if (!g) return VH_ERR_BAD_ARG;
+  if (n_curr) *n_curr = g->nc;
+  if (n_node) *n_node = g->nphi;
+  if (n) *n = g->n;
+  return VH_OK;
+}
+
+vh_status vh_geom_set_z(vh_geom* g, int slot, const double* z_real, const double* z_imag) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded(g->ctx, [&] {
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    set_z_slot(g, slot, z_real, z_imag);
+  });
+}
+
+vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, const void* scale_dev,
+                           const int* zslot, vh_prec prec) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded(g->ctx, [&] {
+    VH_REQUIRE(B >= 1 && x_dev && y_dev && x_dev != y_dev, ERR_BAD_ARG, "bad matvec arguments");
+    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32, ERR_BAD_ARG, "bad precision");
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    matvec_device(g, B, (const double2*)x_dev, (double2*)y_dev, (const double2*)scale_dev, zslot, (Prec)prec);
+  });
+}
+
+vh_status vh_matvec(vh_geom* g, int B, const double* x, double* y, const double* scale, const int* zslot,
+                    vh_prec prec) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded(g->ctx, [&] {
+    VH_REQUIRE(B >= 1 && x && y, ERR_BAD_ARG, "bad matvec arguments");
+    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32, ERR_BAD_ARG, "bad precision");
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    cudaStream_t st = g->ctx->stream;
+    if ((size_t)B > g->io_cap) {
+      cudaFree(g->io_x); cudaFree(g->io_y); cudaFree(g->io_s);
+      g->io_x = g->io_y = g->io_s = nullptr;
+      g->io_cap = 0;
+      VH_CUDA_TRY(cudaMalloc(&g->io_x, (size_t)B * g->n * sizeof(double2)));
+      VH_CUDA_TRY(cudaMalloc(&g->io_y, (size_t)B * g->n * sizeof(double2)));
+      VH_CUDA_TRY(cudaMalloc(&g->io_s, (size_t)B * sizeof(double2)));
+      g->io_cap = B;
+    }
+    const size_t bytes = (size_t)B * g->n * sizeof(double2);
+    VH_CUDA_TRY(cudaMemcpyAsync(g->io_x, x, bytes, cudaMemcpyHostToDevice, st));
+    const double2* sd = nullptr;
+    if (scale) {
+      VH_CUDA_TRY(cudaMemcpyAsync(g->io_s, scale, B * sizeof(double2), cudaMemcpyHostToDevice, st));
+      sd = g->io_s;
+    }
+    matvec_device(g, B, g->io_x, g->io_y, sd, zslot, (Prec)prec);
+    VH_CUDA_TRY(cudaMemcpyAsync(y, g->io_y, bytes, cudaMemcpyDeviceToHost, st));
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,412 @@
+// FFT convolution with the 7-component circulant Green tensor, batched over RHS.
+//
+// Restates the FFT part of lse_matvect_mult.m:34-128 (scatter to the L x M x N x 5
+// grid, five zero-padded 3-D FFTs to 2L x 2M 2N, 13 distinct tensor products,
+// five inverse FFTs, crop, diagonal z/dx {1,1,1,1/6,1/2} term, gather) as five
+// passes over HBM:
+//   1. fwd-x : gather x_J through the voxel map, FFT along x (input half zero)
+//              -> A[b][c][z<N][y<M][kx<2L]
+//   2. fwd-y : FFT along y (input half zero)          -> B[b][c][z<N][ky<2M][kx]
+//   3. z     : FFT along z, multiply by the tensor spectrum, inverse FFT along z,
+//              keep z<N (in place in B).  The 7 tensor values of a point stay in
+//              registers while the CTA walks the RHS batch.
+//   4. inv-y : inverse FFT along y, keep y<M          -> A
+//   5. inv-x : inverse FFT along x, keep x<L, add the diagonal term, scatter to y_J.
+// The 1/(8LMN) normalisation of ifftn is folded into the stored tensor; the
+// frequency factor j*omega*mu is a per-RHS scalar applied in pass 5.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "vh_conv.cuh"
+
+namespace vh {
+
+bool fft_factor(int n, FftDesc& d) {
+  memset(&d, 0, sizeof(d));
+  d.n = n;
+  if (n < 2) return false;
+  int m = n;
+  std::vector<int> r;
+  while (m % 8 == 0) { r.push_back(8); m /= 8; }
+  while (m % 4 == 0) { r.push_back(4); m /= 4; }
+  while (m % 2 == 0) { r.push_back(2); m /= 2; }
+  while (m % 3 == 0) { r.push_back(3); m /= 3; }
+  while (m % 5 == 0) { r.push_back(5); m /= 5; }
+  while (m % 7 == 0) { r.push_back(7); m /= 7; }
+  if (m != 1 || (int)r.size() > kMaxStages) return false;
+  d.nstages = (int)r.size();
+  for (size_t i = 0; i < r.size(); ++i) d.radix[i] = (signed char)r[i];
+  return true;
+}
+
+// tw[m] = exp(-2 pi i m / n), evaluated in long double and rounded once.
+static std::vector<double2> twiddles(int n) {
+  std::vector<double2> t(n);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int m = 0; m < n; ++m) {
+    // reduce the angle to [0, pi/4] by symmetry for accuracy
+    long double a = 2.0L * pi * (long double)m / (long double)n;
+    t[m] = make_double2((double)cosl(a), (double)-sinl(a));
+  }
+  return t;
+}
+
+// ------------------------------------------------------------------------------------------
+template <typename T> struct TileCfg;
+template <> struct TileCfg<double> { static constexpr int target = 2048; };
+template <> struct TileCfg<float> { static constexpr int target = 4096; };
+
+static int x_lines_per_cta(int X, int target) { return std::max(1, std::min(64, target / X)); }
+static int y_lines_per_cta(int Y, int X, bool dbl) {
+  int tx = dbl ? (Y <= 512 ? 8 : 4) : (Y <= 512 ? 16 : 8);
+  while (tx > 1 && (int64_t)2 * Y * tx * (dbl ? 16 : 8) > 160 * 1024) tx /= 2;
+  return std::max(1, std::min(tx, X));
+}
+static int z_lines_per_cta(int Z, int X) {
+  int tx = 16;
+  while (tx > 1 && Z * tx > 512) tx /= 2;
+  return std::max(1, std::min(tx, X));
+}
+
+// ------------------------------------------------------------------------------------------
+// pass 1: fwd-x.  CTA handles `nl` consecutive lines (y fastest, then z, c, b), line-major smem.
+template <typename T>
+__global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int32_t* __restrict__ vmap, int L, int M,
+                        int N, int64_t nv, int64_t nlines_total, cplx<T>* __restrict__ A, FftDesc fd,
+                        const cplx<T>* __restrict__ twg, int nl) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int X = fd.n;
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* b0 = tw + X;
+  C* b1 = b0 + X * nl;
+  for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
+  const int64_t l0 = (int64_t)blockIdx.x * nl;
+  for (int t = threadIdx.x; t < X * nl; t += blockDim.x) {
+    const int line = t / X, i = t % X;
+    const int64_t gl = l0 + line;
+    C v = czero<C>();
+    if (gl < nlines_total && i < L) {
+      const int64_t y = gl % M;
+      const int64_t z = (gl / M) % N;
+      const int64_t c = (gl / ((int64_t)M * N)) % 5;
+      const int64_t b = gl / ((int64_t)M * N * 5);
+      const int32_t vid = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
+      if (vid >= 0) v = to_c(xin[b * ldx + c * nv + vid], C());
+    }
+    b0[line * X + i] = v;
+  }
+  __syncthreads();
+  C* r = fft_lines<-1>(b0, b1, tw, fd, 1, X, nl, true);
+  for (int t = threadIdx.x; t < X * nl; t += blockDim.x) {
+    const int line = t / X, i = t % X;
+    const int64_t gl = l0 + line;
+    if (gl < nlines_total) A[gl * X + i] = r[line * X + i];
+  }
+}
+
+// pass 2 / 4: FFT along y.  Rows of `nin` input (index < nin), `nout` output rows written.
+// src: [plane][nin_rows_stride][X], dst: [plane][nout_stride][X]; CTA: `tx` consecutive kx of one plane.
+template <typename T, int DIR>
+__global__ void k_pass_y(const cplx<T>* __restrict__ src, int src_rows, int nin, cplx<T>* __restrict__ dst,
+                         int dst_rows, int nout, int X, FftDesc fd, const cplx<T>* __restrict__ twg, int tx) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Y = fd.n;
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* b0 = tw + Y;
+  C* b1 = b0 + Y * tx;
+  for (int i = threadIdx.x; i < Y; i += blockDim.x) tw[i] = twg[i];
+  const int kx0 = blockIdx.x * tx;
+  const int64_t plane = blockIdx.y;
+  const C* s = src + plane * src_rows * (int64_t)X;
+  C* d = dst + plane * dst_rows * (int64_t)X;
+  for (int t = threadIdx.x; t < Y * tx; t += blockDim.x) {
+    const int line = t % tx, i = t / tx;
+    const int kx = kx0 + line;
+    C v = czero<C>();
+    if (i < nin && kx < X) v = s[(int64_t)i * X + kx];
+    b0[i * tx + line] = v;
+  }
+  __syncthreads();
+  C* r = fft_lines<DIR>(b0, b1, tw, fd, tx, 1, tx, false);
+  for (int t = threadIdx.x; t < nout * tx; t += blockDim.x) {
+    const int line = t % tx, i = t / tx;
+    const int kx = kx0 + line;
+    if (kx < X) d[(int64_t)i * X + kx] = r[i * tx + line];
+  }
+}
+
+// pass 3: z-FFT, tensor product, inverse z-FFT.  B[b][c][z<N][ky][kx] in place.
+// blockDim = Z * tx; thread (kz, tx) keeps the 7 tensor values of its point in registers.
+template <typename T>
+__global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ tens, int N, int Y, int X, int nrhs,
+                        FftDesc fd, const cplx<T>* __restrict__ twg, int tx) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Z = fd.n;
+  const int nl = 5 * tx;  // lines: c * tx + t
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* b0 = tw + Z;
+  C* b1 = b0 + Z * nl;
+  for (int i = threadIdx.x; i < Z; i += blockDim.x) tw[i] = twg[i];
+  const int kx0 = blockIdx.x * tx;
+  const int ky = blockIdx.y;
+  const int my_t = threadIdx.x % tx;
+  const int my_kz = threadIdx.x / tx;
+  const int my_kx = kx0 + my_t;
+  C g[7];
+  if (my_kz < Z && my_kx < X) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) g[k] = tens[(((int64_t)ky * Z + my_kz) * 7 + k) * X + my_kx];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) g[k] = czero<C>();
+  }
+  const int64_t plane = (int64_t)Y * X;      // one z row of one component
+  const int64_t comp = (int64_t)N * plane;   // one component of one RHS
+  for (int b = 0; b < nrhs; ++b) {
+    C* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X;
+    for (int t = threadIdx.x; t < Z * nl; t += blockDim.x) {
+      const int line = t % nl, i = t / nl;
+      const int c = line / tx, tt = line % tx;
+      const int kx = kx0 + tt;
+      C v = czero<C>();
+      if (i < N && kx < X) v = base[c * comp + i * plane + kx];
+      b0[i * nl + line] = v;
+    }
+    __syncthreads();
+    C* f = fft_lines<-1>(b0, b1, tw, fd, nl, 1, nl, false);
+    if (my_kz < Z) {
+      C* p = f + my_kz * nl + my_t;
+      const C jx = p[0], jy = p[tx], jz = p[2 * tx], j2 = p[3 * tx], j3 = p[4 * tx];
+      // lse_matvect_mult.m:57-86
+      const C a = cmul(g[1], jx);             // G2 Jx
+      const C bb = cmul(g[2], jy);            // G3 Jy
+      const C o1 = cadd(cmul(g[0], jx), cmul(g[1], cadd(j2, j3)));
+      const C o2 = cadd(cmul(g[0], jy), cmul(g[2], csub(j2, j3)));
+      const C o3 = cadd(cmul(g[0], jz), cmul(g[4], j3));
+      const C o4 = cadd(csub(cneg(a), bb), cadd(cmul(g[3], j2), cmul(g[5], j3)));
+      const C o5 = cadd(cadd(csub(bb, a), cneg(cmul(g[4], jz))), cadd(cmul(g[5], j2), cmul(g[6], j3)));
+      p[0] = o1;
+      p[tx] = o2;
+      p[2 * tx] = o3;
+      p[3 * tx] = o4;
+      p[4 * tx] = o5;
+    }
+    __syncthreads();
+    C* other = (f == b0) ? b1 : b0;
+    C* r = fft_lines<+1>(f, other, tw, fd, nl, 1, nl, false);
+    for (int t = threadIdx.x; t < N * nl; t += blockDim.x) {
+      const int line = t % nl, i = t / nl;
+      const int c = line / tx, tt = line % tx;
+      const int kx = kx0 + tt;
+      if (kx < X) base[c * comp + i * plane + kx] = r[i * nl + line];
+    }
+    __syncthreads();
+  }
+}
+
+// pass 5: inverse x-FFT, crop, diagonal term, scatter.
+template <typename T>
+__global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict__ vmap, int L, int M, int N,
+                        int64_t nv, int64_t nlines_total, const double2* __restrict__ xin, int64_t ldx,
+                        double2* __restrict__ yout, int64_t ldy, const double2* __restrict__ scale,
+                        const double2* __restrict__ zdiag, int64_t zstride, double inv_dx, FftDesc fd,
+                        const cplx<T>* __restrict__ twg, int nl) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int X = fd.n;
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* b0 = tw + X;
+  C* b1 = b0 + X * nl;
+  for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
+  const int64_t l0 = (int64_t)blockIdx.x * nl;
+  for (int t = threadIdx.x; t < X * nl; t += blockDim.x) {
+    const int line = t / X, i = t % X;
+    const int64_t gl = l0 + line;
+    b0[line * X + i] = (gl < nlines_total) ? A[gl * X + i] : czero<C>();
+  }
+  __syncthreads();
+  C* r = fft_lines<+1>(b0, b1, tw, fd, 1, X, nl, true);
+  for (int t = threadIdx.x; t < L * nl; t += blockDim.x) {
+    const int line = t / L, i = t % L;
+    const int64_t gl = l0 + line;
+    if (gl >= nlines_total) continue;
+    const int64_t y = gl % M;
+    const int64_t z = (gl / M) % N;
+    const int64_t c = (gl / ((int64_t)M * N)) % 5;
+    const int64_t b = gl / ((int64_t)M * N * 5);
+    const int32_t vid = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
+    if (vid < 0) continue;
+    const double2 conv = to_d(r[line * X + i]);
+    const double2 s = scale[b];
+    const double2 zz = zdiag[b * zstride + vid];
+    const double2 xj = xin[b * ldx + c * nv + vid];
+    const double ck = (c < 3 ? 1.0 : (c == 3 ? 1.0 / 6.0 : 0.5)) * inv_dx;
+    double2 out = cmul(s, conv);
+    out = cadd(out, cscale(cmul(zz, xj), ck));
+    yout[b * ldy + c * nv + vid] = out;
+  }
+}
+
+// fN_all (column-major 2L,2M,2N,7) -> internal [ky][kz][k][kx] divided by X*Y*Z
+template <typename C>
+__global__ void k_tensor_permute(const double2* __restrict__ raw, C* __restrict__ out, int X, int Y, int Z, double s) {
+  const int64_t P = (int64_t)X * Y * Z;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < 7 * P; idx += (int64_t)gridDim.x * blockDim.x) {
+    // idx over the OUTPUT layout
+    const int kx = idx % X;
+    const int k = (idx / X) % 7;
+    const int kz = (idx / (7 * (int64_t)X)) % Z;
+    const int ky = idx / (7 * (int64_t)X * Z);
+    const double2 v = raw[kx + (int64_t)X * (ky + (int64_t)Y * (kz + (int64_t)Z * k))];
+    out[idx] = to_c(cscale(v, s), C());
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2* fN_all_dev, int64_t nv,
+                      const int64_t* idxS_host, bool want32, cudaStream_t st) {
+  p.L = L; p.M = M; p.N = N; p.X = 2 * L; p.Y = 2 * M; p.Z = 2 * N; p.nv = nv; p.dx = dx;
+  VH_REQUIRE(fft_factor(p.X, p.fx) && fft_factor(p.Y, p.fy) && fft_factor(p.Z, p.fz), ERR_UNSUPPORTED,
+             "padded grid dimensions must factor into 2, 3, 5 and 7");
+  VH_REQUIRE(p.X <= 4096 && p.Y <= 4096 && p.Z <= 1024, ERR_UNSUPPORTED, "padded grid dimension too large");
+  // voxel map
+  const int64_t lmn = p.lmn();
+  std::vector<int32_t> vm(lmn, -1);
+  for (int64_t v = 0; v < nv; ++v) {
+    const int64_t li = idxS_host[v] - 1;
+    VH_REQUIRE(li >= 0 && li < lmn, ERR_BAD_ARG, "idxS entry out of range");
+    VH_REQUIRE(v == 0 || idxS_host[v] > idxS_host[v - 1], ERR_BAD_ARG, "idxS must be strictly increasing");
+    vm[li] = (int32_t)v;
+  }
+  VH_CUDA_TRY(cudaMalloc(&p.vmap, lmn * sizeof(int32_t)));
+  VH_CUDA_TRY(cudaMemcpyAsync(p.vmap, vm.data(), lmn * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  // twiddles
+  const int dims[3] = {p.X, p.Y, p.Z};
+  for (int a = 0; a < 3; ++a) {
+    auto t = twiddles(dims[a]);
+    VH_CUDA_TRY(cudaMalloc(&p.tw64[a], dims[a] * sizeof(double2)));
+    VH_CUDA_TRY(cudaMemcpy(p.tw64[a], t.data(), dims[a] * sizeof(double2), cudaMemcpyHostToDevice));
+    std::vector<float2> tf(dims[a]);
+    for (int i = 0; i < dims[a]; ++i) tf[i] = make_float2((float)t[i].x, (float)t[i].y);
+    VH_CUDA_TRY(cudaMalloc(&p.tw32[a], dims[a] * sizeof(float2)));
+    VH_CUDA_TRY(cudaMemcpy(p.tw32[a], tf.data(), dims[a] * sizeof(float2), cudaMemcpyHostToDevice));
+  }
+  // tensor
+  const int64_t P = p.points();
+  const double s = 1.0 / (double)P;
+  VH_CUDA_TRY(cudaMalloc(&p.tens64, 7 * P * sizeof(double2)));
+  k_tensor_permute<double2><<<1024, 256, 0, st>>>(fN_all_dev, p.tens64, p.X, p.Y, p.Z, s);
+  VH_CUDA_TRY(cudaGetLastError());
+  if (want32) {
+    VH_CUDA_TRY(cudaMalloc(&p.tens32, 7 * P * sizeof(float2)));
+    k_tensor_permute<float2><<<1024, 256, 0, st>>>(fN_all_dev, p.tens32, p.X, p.Y, p.Z, s);
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+void conv_plan_destroy(ConvPlan& p) {
+  cudaFree(p.vmap);
+  cudaFree(p.tens64);
+  cudaFree(p.tens32);
+  for (int a = 0; a < 3; ++a) { cudaFree(p.tw64[a]); cudaFree(p.tw32[a]); }
+  cudaFree(p.scratchA);
+  cudaFree(p.scratchB);
+  p = ConvPlan{};
+}
+
+void conv_plan_reserve(ConvPlan& p, int B, Prec prec) {
+  const size_t cs = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
+  const size_t needA = (size_t)B * 5 * p.N * p.M * p.X * cs;
+  const size_t needB = (size_t)B * 5 * p.N * p.Y * p.X * cs;
+  if (needA > p.scratch_bytes_A) {
+    cudaFree(p.scratchA);
+    p.scratchA = nullptr;
+    p.scratch_bytes_A = 0;
+    VH_CUDA_TRY(cudaMalloc(&p.scratchA, needA));
+    p.scratch_bytes_A = needA;
+  }
+  if (needB > p.scratch_bytes_B) {
+    cudaFree(p.scratchB);
+    p.scratchB = nullptr;
+    p.scratch_bytes_B = 0;
+    VH_CUDA_TRY(cudaMalloc(&p.scratchB, needB));
+    p.scratch_bytes_B = needB;
+  }
+}
+
+template <typename T>
+static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
+                         const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st) {
+  using C = cplx<T>;
+  const bool dbl = sizeof(T) == 8;
+  C* A = reinterpret_cast<C*>(p.scratchA);
+  C* Bf = reinterpret_cast<C*>(p.scratchB);
+  const C* tens = dbl ? reinterpret_cast<const C*>(p.tens64) : reinterpret_cast<const C*>(p.tens32);
+  C* const* twp = dbl ? reinterpret_cast<C* const*>(p.tw64) : reinterpret_cast<C* const*>(p.tw32);
+  VH_REQUIRE(tens != nullptr, ERR_BAD_ARG, "tensor for this precision was not built");
+  const int X = p.X, Y = p.Y, Z = p.Z, L = p.L, M = p.M, N = p.N;
+  // pass 1
+  {
+    const int nl = x_lines_per_cta(X, TileCfg<T>::target);
+    const int64_t lines = (int64_t)M * N * 5 * B;
+    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C);
+    const unsigned grid = (unsigned)ceil_div(lines, nl);
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_fwd_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_fwd_x<T><<<grid, 256, sm, st>>>(x, ldx, p.vmap, L, M, N, p.nv, lines, A, p.fx, twp[0], nl);
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+  // pass 2
+  {
+    const int tx = y_lines_per_cta(Y, X, dbl);
+    const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
+    dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * N * B));
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_pass_y<T, -1><<<grid, 256, sm, st>>>(A, M, M, Bf, Y, Y, X, p.fy, twp[1], tx);
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+  // pass 3
+  {
+    const int tx = z_lines_per_cta(Z, X);
+    const size_t sm = (size_t)(Z + 2 * Z * 5 * tx) * sizeof(C);
+    dim3 grid((unsigned)ceil_div(X, tx), (unsigned)Y);
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_zpass<T><<<grid, Z * tx, sm, st>>>(Bf, tens, N, Y, X, B, p.fz, twp[2], tx);
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+  // pass 4
+  {
+    const int tx = y_lines_per_cta(Y, X, dbl);
+    const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
+    dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * N * B));
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_pass_y<T, +1><<<grid, 256, sm, st>>>(Bf, Y, Y, A, M, M, X, p.fy, twp[1], tx);
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+  // pass 5
+  {
+    const int nl = x_lines_per_cta(X, TileCfg<T>::target);
+    const int64_t lines = (int64_t)M * N * 5 * B;
+    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C);
+    const unsigned grid = (unsigned)ceil_div(lines, nl);
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_inv_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_inv_x<T><<<grid, 256, sm, st>>>(A, p.vmap, L, M, N, p.nv, lines, x, ldx, y, ldy, scale, zdiag, zstride,
+                                      1.0 / p.dx, p.fx, twp[0], nl);
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+}
+
+void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
+                const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st) {
+  conv_plan_reserve(p, B, prec);
+  if (prec == PREC_FP64)
+    conv_apply_t<double>(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
+  else
+    conv_apply_t<float>(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
+}
+
+}  // namespace vh

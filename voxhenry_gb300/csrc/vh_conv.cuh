@@ -1,0 +1,52 @@
+// Circulant-embedded Toeplitz convolution of the VIE operator (the FFT part of
+// lse_matvect_mult.m:34-128) for a batch of right-hand sides.
+#pragma once
+#include <vector>
+
+#include "vh_common.cuh"
+#include "vh_fft.cuh"
+
+namespace vh {
+
+enum Prec { PREC_FP64 = 0, PREC_FP32 = 1 };
+
+// Factor n into the radices the FFT supports; false if n has another prime factor.
+bool fft_factor(int n, FftDesc& d);
+
+struct ConvPlan {
+  int L = 0, M = 0, N = 0;   // voxel grid
+  int X = 0, Y = 0, Z = 0;   // padded grid (2L, 2M, 2N)
+  int64_t nv = 0;            // non-empty voxels
+  double dx = 0;
+  FftDesc fx{}, fy{}, fz{};
+  int32_t* vmap = nullptr;   // (L*M*N) voxel -> compact index or -1, column-major
+  // internal tensor spectrum, layout [ky][kz][k][kx], already divided by X*Y*Z
+  double2* tens64 = nullptr;
+  float2* tens32 = nullptr;
+  double2* tw64[3] = {nullptr, nullptr, nullptr};
+  float2* tw32[3] = {nullptr, nullptr, nullptr};
+  // scratch: A (5 * N * M * X per RHS) and Bf (5 * N * Y * X per RHS), in bytes
+  void* scratchA = nullptr;
+  void* scratchB = nullptr;
+  size_t scratch_bytes_A = 0, scratch_bytes_B = 0;
+
+  int64_t points() const { return (int64_t)X * Y * Z; }
+  int64_t lmn() const { return (int64_t)L * M * N; }
+};
+
+// Builds the plan. `fN_all` is the reference's circulant tensor spectrum (complex,
+// column-major (2L, 2M, 2N, 7)), on the DEVICE. `idxS` (1-based, sorted) on the HOST.
+void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2* fN_all_dev, int64_t nv,
+                      const int64_t* idxS_host, bool want32, cudaStream_t st);
+void conv_plan_destroy(ConvPlan& p);
+// Ensures the scratch buffers hold `B` right-hand sides at precision `prec`.
+void conv_plan_reserve(ConvPlan& p, int B, Prec prec);
+
+// y_J[b] = scale[b] * conv(x_J[b]) + (c_k / dx) * zdiag[b] * x_J[b]  for the 5*nv current unknowns.
+//   x, y      : device, complex double, RHS b at x + b*ldx (only the first 5*nv entries used)
+//   scale     : device, B complex (j omega mu per RHS; 1 for the drop-in form)
+//   zdiag     : device, complex per voxel, RHS b uses zdiag + b*zstride (zstride 0 = shared)
+void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
+                const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st);
+
+}  // namespace vh

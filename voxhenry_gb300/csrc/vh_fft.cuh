@@ -1,0 +1,208 @@
+// Mixed-radix Stockham FFT on lines held in shared memory.
+//
+// A CTA transforms `nlines` lines of length n at once.  Element i of line l
+// lives at buf[i * es + l * ls] (es/ls chosen per pass so that the global
+// loads of that pass stay coalesced).  Stages use radices 2, 3, 4, 5, 7 or 8
+// (n = 2^a 3^b 5^c 7^d); each stage reads one buffer and writes the other
+// (self-sorting Stockham: output in natural order, no digit reversal pass).
+//
+// Stage with radix R after stages whose radices multiply to Ns:
+//   for each butterfly j in [0, n/R):   k = j mod Ns
+//     v_r = src[j + r n/R] * w^(r k),  w = exp(DIR 2 pi i / (Ns R))
+//     v   = DFT_R(v)
+//     dst[(j / Ns) Ns R + k + r Ns] = v_r
+// Twiddles come from a table tw[m] = exp(-2 pi i m / n) (conjugated for the
+// inverse transform): w^(r k) = tw[r k n / (Ns R)].
+#pragma once
+#include "vh_common.cuh"
+
+namespace vh {
+
+constexpr int kMaxStages = 24;
+
+struct FftDesc {
+  int n;
+  int nstages;
+  signed char radix[kMaxStages];
+};
+
+// ---------------------------------------------------------------- small DFTs
+template <int DIR, typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
+  C t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft4(C* v) {
+  C t0 = cadd(v[0], v[2]);
+  C t1 = csub(v[0], v[2]);
+  C t2 = cadd(v[1], v[3]);
+  C t3 = cmul_i<DIR>(csub(v[1], v[3]));
+  v[0] = cadd(t0, t2);
+  v[2] = csub(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[3] = csub(t1, t3);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft8(C* v) {
+  using T = decltype(v[0].x);
+  const T h = (T)0.70710678118654752440084436210484903928483593768847;
+  // radix-2 split into even / odd halves
+  C a[4] = {v[0], v[2], v[4], v[6]};
+  C b[4] = {v[1], v[3], v[5], v[7]};
+  dft4<DIR>(a);
+  dft4<DIR>(b);
+  // twiddles exp(DIR 2 pi i k / 8), k = 0..3
+  C b1, b2, b3;
+  if (DIR < 0) {
+    b1 = mk((b[1].x + b[1].y) * h, (b[1].y - b[1].x) * h);
+    b2 = cmul_i<DIR>(b[2]);
+    b3 = mk((b[3].y - b[3].x) * h, -(b[3].x + b[3].y) * h);
+  } else {
+    b1 = mk((b[1].x - b[1].y) * h, (b[1].x + b[1].y) * h);
+    b2 = cmul_i<DIR>(b[2]);
+    b3 = mk(-(b[3].x + b[3].y) * h, (b[3].x - b[3].y) * h);
+  }
+  v[0] = cadd(a[0], b[0]);
+  v[4] = csub(a[0], b[0]);
+  v[1] = cadd(a[1], b1);
+  v[5] = csub(a[1], b1);
+  v[2] = cadd(a[2], b2);
+  v[6] = csub(a[2], b2);
+  v[3] = cadd(a[3], b3);
+  v[7] = csub(a[3], b3);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft3(C* v) {
+  using T = decltype(v[0].x);
+  const T s3 = (T)0.86602540378443864676372317075293618347140262690519;  // sqrt(3)/2
+  C t1 = cadd(v[1], v[2]);
+  C t2 = csub(v[1], v[2]);
+  C m = mk(v[0].x - (T)0.5 * t1.x, v[0].y - (T)0.5 * t1.y);
+  // s = DIR * i * sqrt(3)/2 * t2
+  C s = cscale(cmul_i<DIR>(t2), s3);
+  v[0] = cadd(v[0], t1);
+  v[1] = cadd(m, s);
+  v[2] = csub(m, s);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft5(C* v) {
+  using T = decltype(v[0].x);
+  const T c1 = (T)0.30901699437494742410229341718281905886436448684462;   // cos(2pi/5)
+  const T c2 = (T)-0.80901699437494742410229341718281905886436448684462;  // cos(4pi/5)
+  const T s1 = (T)0.95105651629515357211643933337938214340569863412575;   // sin(2pi/5)
+  const T s2 = (T)0.58778525229247312916870595463907276859765243764314;   // sin(4pi/5)
+  C a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+  C a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+  C m1 = mk(v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y);
+  C m2 = mk(v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y);
+  // DIR*i*(s1 b1 + s2 b2), DIR*i*(s2 b1 - s1 b2)
+  C n1 = cmul_i<DIR>(mk(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y));
+  C n2 = cmul_i<DIR>(mk(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y));
+  v[0] = mk(v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y);
+  v[1] = cadd(m1, n1);
+  v[4] = csub(m1, n1);
+  v[2] = cadd(m2, n2);
+  v[3] = csub(m2, n2);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft7(C* v) {
+  using T = decltype(v[0].x);
+  const T c[3] = {(T)0.62348980185873353052500488400423981063227473089640,    // cos(2pi/7)
+                  (T)-0.22252093395631440428890256449679475946635556876451,   // cos(4pi/7)
+                  (T)-0.90096886790241912623610231950744505116591916213189};  // cos(6pi/7)
+  const T s[3] = {(T)0.78183148246802980870844452667405775023233451870868,    // sin(2pi/7)
+                  (T)0.97492791218182360701813168299393121723278580062000,    // sin(4pi/7)
+                  (T)0.43388373911755812047576833284835875460999072778746};   // sin(6pi/7)
+  C a[3], b[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    a[k] = cadd(v[k + 1], v[6 - k]);
+    b[k] = csub(v[k + 1], v[6 - k]);
+  }
+  C x0 = v[0];
+  C out0 = x0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out0 = cadd(out0, a[k]);
+#pragma unroll
+  for (int m = 1; m <= 3; ++m) {
+    C re = x0, im = mk((T)0, (T)0);
+#pragma unroll
+    for (int k = 1; k <= 3; ++k) {
+      int idx = (m * k) % 7;  // angle index
+      T cc, ss;
+      if (idx <= 3) { cc = c[idx - 1]; ss = s[idx - 1]; } else { cc = c[7 - idx - 1]; ss = -s[7 - idx - 1]; }
+      re.x += cc * a[k - 1].x;
+      re.y += cc * a[k - 1].y;
+      im.x += ss * b[k - 1].x;
+      im.y += ss * b[k - 1].y;
+    }
+    C n = cmul_i<DIR>(im);
+    v[m] = cadd(re, n);
+    v[7 - m] = csub(re, n);
+  }
+  v[0] = out0;
+}
+
+// ---------------------------------------------------------------- one stage
+template <int R, int DIR, typename C>
+__device__ __forceinline__ void fft_stage(const C* __restrict__ src, C* __restrict__ dst, const C* __restrict__ tw,
+                                          int n, int Ns, int es, int ls, int nlines, bool jfast) {
+  const int nb = n / R;
+  const int total = nb * nlines;
+  const int twmul = n / (Ns * R);
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int line, j;
+    if (jfast) { j = t % nb; line = t / nb; } else { line = t % nlines; j = t / nlines; }
+    const int k = j % Ns;
+    const int base = line * ls;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[base + (j + r * nb) * es];
+    if (Ns > 1) {
+      const int step = k * twmul;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = tw[r * step];
+        v[r] = (DIR < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+      }
+    }
+    if constexpr (R == 2) dft2<DIR>(v[0], v[1]);
+    else if constexpr (R == 3) dft3<DIR>(v);
+    else if constexpr (R == 4) dft4<DIR>(v);
+    else if constexpr (R == 5) dft5<DIR>(v);
+    else if constexpr (R == 7) dft7<DIR>(v);
+    else if constexpr (R == 8) dft8<DIR>(v);
+    const int d0 = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[base + (d0 + r * Ns) * es] = v[r];
+  }
+}
+
+// Runs all stages; returns the buffer holding the result (buf0 or buf1).
+// Must be called by all threads of the CTA; ends with a __syncthreads().
+template <int DIR, typename C>
+__device__ C* fft_lines(C* buf0, C* buf1, const C* tw, const FftDesc& d, int es, int ls, int nlines, bool jfast) {
+  C* src = buf0;
+  C* dst = buf1;
+  int Ns = 1;
+  for (int s = 0; s < d.nstages; ++s) {
+    const int R = d.radix[s];
+    switch (R) {
+      case 2: fft_stage<2, DIR>(src, dst, tw, d.n, Ns, es, ls, nlines, jfast); break;
+      case 3: fft_stage<3, DIR>(src, dst, tw, d.n, Ns, es, ls, nlines, jfast); break;
+      case 4: fft_stage<4, DIR>(src, dst, tw, d.n, Ns, es, ls, nlines, jfast); break;
+      case 5: fft_stage<5, DIR>(src, dst, tw, d.n, Ns, es, ls, nlines, jfast); break;
+      case 7: fft_stage<7, DIR>(src, dst, tw, d.n, Ns, es, ls, nlines, jfast); break;
+      default: fft_stage<8, DIR>(src, dst, tw, d.n, Ns, es, ls, nlines, jfast); break;
+    }
+    __syncthreads();
+    C* t = src;
+    src = dst;
+    dst = t;
+    Ns *= R;
+  }
+  return src;
+}
+
+}  // namespace vh

@@ -1,0 +1,60 @@
+// Internal state behind the C ABI handles.
+#pragma once
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vh_common.cuh"
+#include "vh_conv.cuh"
+
+struct vh_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+};
+
+namespace vh {
+
+// Real CSR matrix on the device.
+struct Csr {
+  int64_t nrows = 0, ncols = 0, nnz = 0;
+  int32_t* rowptr = nullptr;  // nrows + 1 (nnz < 2^31 checked)
+  int32_t* col = nullptr;
+  double* val = nullptr;
+  void free_all() {
+    cudaFree(rowptr);
+    cudaFree(col);
+    cudaFree(val);
+    rowptr = nullptr; col = nullptr; val = nullptr;
+  }
+};
+
+// y[b*ldy + yoff + r] (mode 0: =, 1: +=, -1: -=) sum_j A(r, j) x[b*ldx + xoff + j]
+void spmv_batched(const Csr& A, int B, const double2* x, int64_t ldx, int64_t xoff, double2* y, int64_t ldy,
+                  int64_t yoff, int mode, cudaStream_t st);
+
+// Host CSC (num_node x ncol) -> device CSR of A and of A^T.
+void csc_upload(int64_t nrow, int64_t ncol, const int64_t* jc, const int64_t* ir, const double* pr, Csr& A, Csr& AT,
+                cudaStream_t st);
+
+}  // namespace vh
+
+struct vh_geom {
+  vh_ctx* ctx = nullptr;
+  int L = 0, M = 0, N = 0;
+  double dx = 0;
+  int64_t nv = 0, nc = 0, nphi = 0, n = 0;
+  std::vector<int64_t> idxS;       // host copy, 1-based
+  vh::ConvPlan conv;
+  vh::Csr Ae, AeT;                 // nphi x nc, nc x nphi
+  std::vector<double2*> zslots;    // per slot: nv complex (device)
+  double2* ones = nullptr;         // device, capacity ones_cap complex ones
+  int ones_cap = 0;
+  double2* io_x = nullptr;         // staging for host-pointer calls
+  double2* io_y = nullptr;
+  double2* io_s = nullptr;
+  size_t io_cap = 0;               // RHS capacity of io_x / io_y
+  double2* zgather = nullptr;      // B x nv gathered z for mixed slots
+  size_t zgather_cap = 0;
+};
