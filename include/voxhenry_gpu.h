@@ -86,6 +86,42 @@ vh_status vh_matvec(vh_geom* g, int B, const double* x, double* y, const double*
 vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, const void* scale_dev,
                            const int* zslot, vh_prec prec);
 
+/* ---- preconditioner: lse_sparse_precon_prepare(dx, z_real, z_imag, idxS, st_sparse_precon, ..., Ae)
+ *      (lse_sparse_precon_prepare.m:1).  A geometry created with fN_all == NULL serves a
+ *      preconditioner-only caller.  st_sparse_precon: 3 complex self terms (already multiplied by
+ *      j w mu, VoxHenry_executer.m:267); z is taken from slot `zslot` of the geometry (dx too).
+ *      The factor of the Schur complement is built on the device and kept in the handle (the
+ *      reference keeps it in MATLAB globals, lse_sparse_precon_prepare.m:2).                    */
+vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_sparse_precon, int zslot,
+                           vh_precon** out);
+void vh_precon_destroy(vh_precon* p);
+/* factor statistics: entries of L, factorisation flops, fronts, largest front order */
+vh_status vh_precon_stats(const vh_precon* p, int64_t* nnz_factor, double* flops, int* nfronts, int* max_front);
+/* host-only symbolic analysis of S = Ae diag Ae^T (no device needed): same statistics plus the bytes of
+ * one frequency's factor storage -- used to admit jobs by device-memory footprint. */
+vh_status vh_schur_analyze(int L, int M, int N, int64_t nv, const int64_t* idxS, int64_t num_node,
+                           const int64_t* Ae_jc, const int64_t* Ae_ir, const double* Ae_pr, int64_t* nnz_factor,
+                           double* flops, int* nfronts, int* max_front, int64_t* factor_bytes);
+
+/* ---- JOut_full_out = lse_sparse_precon_multiply(JOut_full_in, Ae, ...) (lse_sparse_precon_multiply.m:1)
+ *      for B right-hand sides; RHS b uses pcs[b] (all of one kind).  x, y: HOST, B x n complex.   */
+vh_status vh_precon_apply(vh_geom* g, int B, vh_precon* const* pcs, const double* x, double* y);
+vh_status vh_precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const void* x_dev, void* y_dev);
+
+/* ---- [x,flag,relres,iter,resvec] = pgmres(A, b, restart, tol, maxit, L1)   (pgmres.m:70)
+ *      or fpgmres(A, b, restart, tol, maxit, R1)                             (fpgmres.m:58)
+ *      for B right-hand sides at once, A = lse_matvect_mult of geometry g with per-RHS scale/zslot,
+ *      the preconditioner pcs[b] (NULL: none) on the left (flexible = 0) or right (flexible = 1).
+ *      x0 = 0.  b, x: HOST B x n complex.  tol: B values.  Outputs per RHS: flag (0 converged),
+ *      relres = |b - A x| / |b|, iter = [inner iterations of the last cycle, outer cycles] (2 ints),
+ *      resvec (first resvec_len entries, row b at b*resvec_len), nres = its full length.
+ *      prec = VH_PREC_FP32: mixed precision -- FP64 iterative refinement around left-preconditioned
+ *      GMRES whose FFT matvec runs in complex64; iter then counts inner iterations / cycles summed
+ *      over refinement steps and resvec holds the preconditioned residual after each step.     */
+vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
+                   int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
+                   double* relres, int* iter, double* resvec, int resvec_len, int* nres);
+
 #ifdef __cplusplus
 }
 #endif

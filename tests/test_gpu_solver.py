@@ -1,0 +1,172 @@
+"""Preconditioner, (F)GMRES and R/L extraction on the GPU vs the CPU oracle and the reference's results."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_vhr_text
+from oracle import circulant, solver, structure, vhr
+
+pytestmark = pytest.mark.gpu
+
+PRECON_TOL = 1e-10     # preconditioner apply, relative 2-norm (different exact factorisation of S)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from voxhenry_gb300 import executer, vie
+
+    return vie, executer
+
+
+def problem_of(w):
+    from voxhenry_gb300.executer import Problem
+
+    S = structure.build_system(w.sigma_e, w.lambdaL, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, st = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
+    P = Problem(S.L, S.M, S.N, S.dx, w.sigma_e, w.lambdaL, S.idxS, S.Ar, S.rhs, fN, st)
+    return S, P
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def assert_port_matrix_close(a, b, rtol):
+    """Per frequency, |a - b| <= rtol * max|b| over the port matrix (off-diagonal mutual terms of
+    decoupled conductors sit at the rounding floor of the diagonal ones)."""
+    for f in range(b.shape[0]):
+        scale = np.abs(b[f]).max()
+        assert np.abs(a[f] - b[f]).max() <= rtol * scale, (f, a[f], b[f])
+
+
+@pytest.fixture(scope="module")
+def blob(lib):
+    from voxhenry_gb300 import geometry
+
+    w = geometry.random_blob((10, 7, 6), fill=0.7, seed=5)
+    return w, *problem_of(w)
+
+
+@pytest.mark.parametrize("f", [1e3, 1e8, 2e10])
+def test_precon_apply_matches_oracle(lib, blob, f):
+    vie, ex = lib
+    w, S, P = blob
+    om = 2 * np.pi * f
+    jwmu = 1j * om * solver.MU0
+    z_real, z_imag = solver.z_arrays(w.sigma_e, None, om)
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, z_imag, S.idxS, jwmu * P.st2, S.Ar)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS)
+    pc = g.precon(jwmu * P.st2)
+    rng = np.random.default_rng(7)
+    X = rng.standard_normal((3, S.n)) + 1j * rng.standard_normal((3, S.n))
+    Y = vie.apply_precons(g, [pc], X)
+    for k in range(3):
+        assert rel(Y[k], ref.multiply(X[k])) < PRECON_TOL
+    st = pc.stats()
+    assert st["fronts"] >= 1 and st["nnz_factor"] > 0
+
+
+def test_dropin_calls_match_oracle(lib, blob):
+    """lse_sparse_precon_prepare / lse_sparse_precon_multiply / pgmres with the reference's arguments."""
+    vie, ex = lib
+    w, S, P = blob
+    f = 2.5e9
+    om = 2 * np.pi * f
+    jwmu = 1j * om * solver.MU0
+    fN = jwmu * P.fN_all2
+    st = jwmu * P.st2
+    z_real, z_imag = solver.z_arrays(w.sigma_e, None, om)
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, z_imag, S.idxS, st, S.Ar)
+    vie.lse_sparse_precon_prepare(S.dx, z_real, z_imag, S.idxS, st, S.nodeid_4_grnd, S.nodeid_4_injectcurr, S.Ar)
+    x = np.random.default_rng(3).standard_normal(S.n) + 0j
+    assert rel(vie.lse_sparse_precon_multiply(x, S.Ar, None, None, 0.1), ref.multiply(x)) < PRECON_TOL
+    A = vie.matvec_handle(fN, S.Ar, z_real, z_imag, S.dx, S.idxS5)
+    b = S.rhs[:, 0].astype(complex)
+    xg, flag, relres, it, resvec = vie.pgmres(A, b, 100, 1e-12, 10, vie.precon_handle())
+    Aref = lambda J: solver.lse_matvect_mult(J, fN, S.Ar, z_real, z_imag, S.dx, S.idxS5)
+    xo, flag_o, relres_o, it_o, resvec_o = solver.pgmres(Aref, b, 100, 1e-12, 10, ref.multiply)
+    assert rel(xg, xo) < 1e-9
+    assert abs(len(resvec) - len(resvec_o)) <= 1
+    np.testing.assert_allclose(resvec[:3], resvec_o[:3], rtol=1e-6)
+    assert relres < 1e-10 and flag == flag_o
+
+
+def test_fpgmres_matches_oracle(lib, blob):
+    vie, ex = lib
+    w, S, P = blob
+    f = 1e9
+    om = 2 * np.pi * f
+    jwmu = 1j * om * solver.MU0
+    z_real, _ = solver.z_arrays(w.sigma_e, None, om)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS)
+    pc = g.precon(jwmu * P.st2)
+    b = S.rhs[:, 0].astype(complex)
+    out = g.solve(b[None], pcs=[pc], scale=jwmu, restart=30, tol=1e-11, maxit=10, flexible=True)
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, None, S.idxS, jwmu * P.st2, S.Ar)
+    Aref = lambda J: solver.lse_matvect_mult(J, jwmu * P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS5)
+    xo, *_ = solver.fpgmres(Aref, b, 30, 1e-11, 10, ref.multiply)
+    assert rel(out["x"][0], xo) < 1e-9
+
+
+def test_sweep_rl_matches_oracle_and_batching_invariant(lib):
+    """All frequencies x ports in one batch == the oracle per frequency; one RHS alone == in the batch."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.two_bars(L=24, M=14, N=6, xr=(2, 22), zr=(1, 4), y1=(2, 5), y2=(9, 12))
+    S, P = problem_of(w)
+    freqs = np.array([1e3, 1e7, 5e9])
+    sw = ex.Sweep(P, freqs).prepare()
+    out = sw.solve(restart=50, tol=1e-12, maxit=10)
+    ref = solver.solve_frequencies(S, P.fN_all2, P.st2, freqs, restart=50, tol=1e-12)
+    assert_port_matrix_close(out["R"], ref["R"], 1e-9)
+    assert_port_matrix_close(out["L"], ref["L"], 1e-9)
+    # batching invariance: the last frequency's port-1 solve alone, bitwise
+    g = sw.geom
+    k = 2 * P.num_ports
+    alone = g.solve(P.rhs[:, 0].astype(complex)[None], pcs=[sw.pcs[2]], scale=1j * 2 * np.pi * freqs[2] * solver.MU0,
+                    restart=50, tol=1e-12, maxit=10)
+    assert np.array_equal(alone["x"][0], out["x"][k])
+
+
+def test_mixed_precision_rl(lib):
+    """complex64 FFT inside FP64 refinement: R, L within 1e-6 of the FP64 oracle."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.bar(L=24, M=6, N=6, dx=0.5e-6)
+    S, P = problem_of(w)
+    freqs = np.array([1e3, 1e8, 1e10])
+    sw = ex.Sweep(P, freqs).prepare()
+    out = sw.solve(restart=50, tol=1e-10, maxit=10, prec="fp32")
+    ref = solver.solve_frequencies(S, P.fN_all2, P.st2, freqs, restart=50, tol=1e-12)
+    assert_port_matrix_close(out["R"], ref["R"], 1e-6)
+    assert_port_matrix_close(out["L"], ref["L"], 1e-6)
+    out64 = sw.solve(restart=50, tol=1e-12, maxit=10)
+    assert_port_matrix_close(out64["R"], ref["R"], 1e-9)
+    assert_port_matrix_close(out64["L"], ref["L"], 1e-9)
+
+
+def test_numex1_matches_reference_results(lib):
+    """The reference's numex1 input: GPU R, L vs results_numex1_straight_conductor/data_R_jL_mat.mat."""
+    vie, ex = lib
+    gold = np.load(os.path.join(GOLDEN, "reference_results.npz"))
+    inp = vhr.read_vhr_text(golden_vhr_text("straight_cond1_len30.0u_wid10.0u_dist20.0u.vhr"))
+    from voxhenry_gb300 import geometry
+
+    w = geometry.Workload("numex1", inp.sigma_e, inp.dx, inp.pnt_lft, inp.pnt_rght, inp.freq)
+    S, P = problem_of(w)
+    sel = [0, 24, 37, 40]        # 1 Hz, 1 MHz, 2.5 GHz, 10 GHz
+    freqs = gold["numex1_freq"][sel]
+    out = ex.Sweep(P, freqs).prepare().solve(restart=100, tol=None, maxit=10)
+    RjL = gold["numex1_RjL"][sel]
+    np.testing.assert_allclose(out["R"][:, 0, 0], RjL.real, rtol=1e-7)
+    np.testing.assert_allclose(out["L"][:, 1 - 1, 0][1:], RjL.imag[1:], rtol=1e-7)
+    np.testing.assert_allclose(out["L"][0, 0, 0], RjL.imag[0], rtol=1e-5)   # 1 Hz: L from a 1e-8 part of Z
+    x = out["x"][2]
+    idx = gold["numex1_x_sample_idx"]
+    np.testing.assert_allclose(x[idx], gold["numex1_x_sample"], rtol=0, atol=1e-6 * np.abs(gold["numex1_x_sample"]).max())

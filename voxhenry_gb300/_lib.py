@@ -38,6 +38,15 @@ SIGNATURES = {
     "vh_geom_set_z": (C.c_int, [_p, C.c_int, _dp, _dp]),
     "vh_matvec": (C.c_int, [_p, C.c_int, _dp, _dp, _dp, _ip, C.c_int]),
     "vh_matvec_device": (C.c_int, [_p, C.c_int, _p, _p, _p, _ip, C.c_int]),
+    "vh_precon_create": (C.c_int, [_p, C.c_int, _dp, C.c_int, C.POINTER(_p)]),
+    "vh_precon_destroy": (None, [_p]),
+    "vh_precon_stats": (C.c_int, [_p, _i64p, _dp, _ip, _ip]),
+    "vh_schur_analyze": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, _i64p, C.c_int64, _i64p, _i64p, _dp,
+                                   _i64p, _dp, _ip, _ip, _i64p]),
+    "vh_precon_apply": (C.c_int, [_p, C.c_int, C.POINTER(_p), _dp, _dp]),
+    "vh_precon_apply_device": (C.c_int, [_p, C.c_int, C.POINTER(_p), _p, _p]),
+    "vh_gmres": (C.c_int, [_p, C.c_int, C.POINTER(_p), _dp, _dp, _ip, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp,
+                           _ip, _dp, _ip, _dp, C.c_int, _ip]),
 }
 
 _lib = None

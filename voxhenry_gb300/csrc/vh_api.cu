@@ -110,6 +110,7 @@ namespace vh {
 // Full operator of lse_matvect_mult.m for B right-hand sides (device pointers, leading dimension n).
 void matvec_device(vh_geom* g, int B, const double2* x, double2* y, const double2* scale, const int* zslot, Prec prec) {
   cudaStream_t st = g->ctx->stream;
+  VH_REQUIRE(g->has_conv, ERR_BAD_ARG, "geometry was created without a circulant tensor");
   if (!scale) {
     ensure_ones(g, B);
     scale = g->ones;
@@ -186,7 +187,7 @@ vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const doub
     VH_REQUIRE(L >= 2 && M >= 2 && N >= 2, ERR_UNSUPPORTED, "grids thinner than 2 voxels are not supported");
     VH_REQUIRE(dx > 0 && nv >= 0 && num_node >= 0, ERR_BAD_ARG, "bad sizes");
     VH_REQUIRE(nv <= (int64_t)L * M * N, ERR_BAD_ARG, "nv exceeds the grid");
-    VH_REQUIRE(fN_all && (nv == 0 || idxS) && Ae_jc && z_real, ERR_BAD_ARG, "null input");
+    VH_REQUIRE((nv == 0 || idxS) && Ae_jc && z_real, ERR_BAD_ARG, "null input");
     VH_REQUIRE(5 * nv < (1LL << 31), ERR_UNSUPPORTED, "too many current unknowns");
     VH_CUDA_TRY(cudaSetDevice(ctx->device));
     g->ctx = ctx;
@@ -194,21 +195,24 @@ vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const doub
     g->nv = nv; g->nc = 5 * nv; g->nphi = num_node; g->n = g->nc + g->nphi;
     g->idxS.assign(idxS, idxS + nv);
     cudaStream_t st = ctx->stream;
-    const int64_t P = 8LL * L * M * N;
-    double2* raw = nullptr;
-    VH_CUDA_TRY(cudaMalloc(&raw, 7 * P * sizeof(double2)));
-    cudaError_t e = cudaMemcpyAsync(raw, fN_all, 7 * P * sizeof(double2), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) {
-      try {
-        conv_plan_create(g->conv, L, M, N, dx, raw, nv, g->idxS.data(), want_fp32 != 0, st);
-      } catch (...) {
-        cudaFree(raw);
-        throw;
+    if (fN_all) {
+      const int64_t P = 8LL * L * M * N;
+      double2* raw = nullptr;
+      VH_CUDA_TRY(cudaMalloc(&raw, 7 * P * sizeof(double2)));
+      cudaError_t e = cudaMemcpyAsync(raw, fN_all, 7 * P * sizeof(double2), cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) {
+        try {
+          conv_plan_create(g->conv, L, M, N, dx, raw, nv, g->idxS.data(), want_fp32 != 0, st);
+        } catch (...) {
+          cudaFree(raw);
+          throw;
+        }
       }
+      cudaFree(raw);
+      VH_CUDA_TRY(e);
+      g->has_conv = true;
     }
-    cudaFree(raw);
-    VH_CUDA_TRY(e);
-    csc_upload(num_node, g->nc, Ae_jc, Ae_ir, Ae_pr, g->Ae, g->AeT, st);
+    csc_upload(num_node, g->nc, Ae_jc, Ae_ir, Ae_pr, g->Ae, g->AeT, g->hAe, g->hAeT, st);
     set_z_slot(g, 0, z_real, z_imag);
   });
   if (s != VH_OK) {
@@ -225,6 +229,9 @@ void vh_geom_destroy(vh_geom* g) {
   conv_plan_destroy(g->conv);
   g->Ae.free_all();
   g->AeT.free_all();
+  g->chol.free_all();
+  cudaFree(g->pc_tmp);
+  cudaFree(g->pc_ptrs);
   for (auto* z : g->zslots) cudaFree(z);
   cudaFree(g->ones);
   cudaFree(g->io_x);

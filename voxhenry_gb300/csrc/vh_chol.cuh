@@ -1,0 +1,76 @@
+// Sparse Cholesky of the Schur complement S = Ar diag(A_inv) Ar^T (nphi x nphi, SPD) used by the
+// 'schur_invert' preconditioner (lse_sparse_precon_prepare.m:90-191, lse_sparse_precon_multiply.m:61-117).
+//
+// Symbolic analysis (host, once per geometry): geometric nested dissection of the panel graph, a
+// front per dissection node, row structures, extend-add maps and assembly term lists.
+// Numeric factorisation (device, per frequency): multifrontal, level by level from the leaves.
+// Solves (device): forward pass from the leaves with per-front update vectors, backward pass
+// from the root.  The factor is real; right-hand sides are complex.
+#pragma once
+#include <vector>
+
+#include "vh_common.cuh"
+
+namespace vh {
+
+struct FrontInfo {
+  int32_t ns;          // pivots (own panels)
+  int32_t nb;          // boundary rows
+  int32_t nf;          // ns + nb
+  int32_t parent;      // -1 for a root
+  int32_t child[2];    // -1 if absent
+  int64_t w_off;       // dense nf x nf column-major front in the factor storage
+  int64_t rows_off;    // rows[rows_off .. + nf): global panel index (own first)
+  int64_t relmap_off;  // relmap[relmap_off .. + nb): local row in the parent for each boundary row
+  int64_t asm_off;     // assembly entries [asm_off, asm_off + asm_cnt)
+  int32_t asm_cnt;
+  int32_t pad_;
+  int64_t u_off;       // per-RHS update vector offset (nb entries)
+};
+
+struct AsmEntry {
+  int32_t li, lj;      // local row / column (li >= lj, lj < ns)
+  int32_t t0, t1;      // terms [t0, t1) in asm_q / asm_c
+};
+
+struct CholSymbolic {
+  int64_t n = 0;                    // nphi
+  int nfronts = 0;
+  int max_nf = 0;
+  int64_t w_total = 0;              // doubles of factor storage (sum nf^2)
+  int64_t u_total = 0;              // sum nb (update vector length per RHS)
+  int64_t nnz_l = 0;                // entries of L (sum over fronts of ns*(ns+1)/2 + nb*ns)
+  double flops = 0;                 // factorisation flops
+  std::vector<FrontInfo> fronts;
+  std::vector<std::vector<int32_t>> levels;  // fronts per height (leaves first)
+  std::vector<int32_t> level_max_ns, level_max_nf;
+  // device copies
+  FrontInfo* d_fronts = nullptr;
+  int32_t* d_rows = nullptr;
+  int32_t* d_relmap = nullptr;
+  AsmEntry* d_asm = nullptr;
+  int32_t* d_asm_q = nullptr;
+  double* d_asm_c = nullptr;
+  std::vector<int32_t*> d_levels;   // per height: front ids
+  int* d_err = nullptr;             // factorisation status flag
+  int64_t n_asm = 0;
+  void free_all();
+};
+
+// Builds the symbolic structure from the host CSR of Ar (nphi x nc) and of Ar^T (nc x nphi),
+// and the voxel linear indices (1-based) of the nv voxels.  Throws ERR_UNSUPPORTED when Ar does
+// not have the VoxHenry incidence structure.
+void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64_t* idxS, int64_t nphi,
+                   const std::vector<int32_t>& a_rp, const std::vector<int32_t>& a_col, const std::vector<double>& a_val,
+                   const std::vector<int32_t>& t_rp, const std::vector<int32_t>& t_col, const std::vector<double>& t_val,
+                   int leaf_size, cudaStream_t st, bool to_device = true);
+
+// Numeric factorisation into W (sym.w_total doubles), with D = A_inv (nc reals, device).
+void chol_factor(const CholSymbolic& s, const double* A_inv, double* W, cudaStream_t st);
+
+// Solves S x = b in place for B right-hand sides.  x: device, complex, RHS b at x + b*ldx + xoff
+// (panel indexing); Wp: device array of B factor pointers; U: device scratch of B * u_total complex.
+void chol_solve(const CholSymbolic& s, int B, double* const* Wp, double2* x, int64_t ldx, int64_t xoff, double2* U,
+                cudaStream_t st);
+
+}  // namespace vh

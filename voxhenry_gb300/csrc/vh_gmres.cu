@@ -1,0 +1,697 @@
+// Batched restarted GMRES (pgmres.m / pgmres_iter.m, left preconditioner) and flexible GMRES
+// (fpgmres.m / fpgmres_iter.m, right preconditioner), one Krylov space per right-hand side, plus
+// the mixed-precision iterative-refinement driver (complex64 FFT matvec inside FP64 refinement).
+//
+// Device: matvec, preconditioner, classical Gram-Schmidt as a fused multi-dot and a fused
+// update + norm, normalisation, and the basis combinations x += V y, r = V res.
+// Host: per-RHS Givens rotations of the Hessenberg column (the least-squares residual of
+// Hc \ rhs, pgmres_iter.m:113-121), restart bookkeeping and convergence tests.  Right-hand sides
+// that converged inside a cycle drop out of the batch (the active set is compacted).
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "../../include/voxhenry_gpu.h"
+#include "vh_internal.cuh"
+
+namespace vh {
+void matvec_device(vh_geom* g, int B, const double2* x, double2* y, const double2* scale, const int* zslot, Prec prec);
+void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* x, double2* y);
+}  // namespace vh
+
+using namespace vh;
+using cd = std::complex<double>;
+
+namespace {
+
+constexpr int kChunkThreads = 256;
+constexpr int kChunkElems = 4096;   // elements per reduction chunk
+
+// partial[a][c][j] = sum_{i in chunk c} conj(V_b[j][i]) z_a[i],  j < nj,  b = act[a]
+__global__ void k_multidot(const double2* __restrict__ V, int64_t ldv, int64_t ldb, const double2* __restrict__ z,
+                           int64_t ldz, const int* __restrict__ act, int nj, int64_t n, double2* __restrict__ partial) {
+  const int a = blockIdx.y;
+  const int c = blockIdx.x;
+  const int nch = gridDim.x;
+  const double2* Vb = V + (int64_t)act[a] * ldb;
+  const double2* za = z + (int64_t)a * ldz;
+  const int64_t i0 = (int64_t)c * kChunkElems;
+  const int64_t i1 = min(n, i0 + kChunkElems);
+  __shared__ double2 red[kChunkThreads / 32];
+  for (int j = 0; j < nj; ++j) {
+    const double2* v = Vb + (int64_t)j * ldv;
+    double sx = 0.0, sy = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const double2 p = v[i], q = za[i];
+      sx = fma(p.x, q.x, fma(p.y, q.y, sx));
+      sy = fma(p.x, q.y, fma(-p.y, q.x, sy));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(sx, sy);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double2 t = make_double2(0.0, 0.0);
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t.x += red[w].x; t.y += red[w].y; }
+      partial[((int64_t)a * nch + c) * nj + j] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// out[a * ldo + j] = sum_c partial[a][c][j]   (fixed order: deterministic)
+__global__ void k_reduce_partials(const double2* __restrict__ partial, int nch, int nj, double2* __restrict__ out,
+                                  int ldo) {
+  const int a = blockIdx.x;
+  for (int j = threadIdx.x; j < nj; j += blockDim.x) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int c = 0; c < nch; ++c) {
+      const double2 p = partial[((int64_t)a * nch + c) * nj + j];
+      t.x += p.x;
+      t.y += p.y;
+    }
+    out[(int64_t)a * ldo + j] = t;
+  }
+}
+
+// z_a -= sum_{j<nj} h[a][j] V_b[j];  partial[a][c] = sum |z_a|^2 over the chunk
+__global__ void k_cgs_update(const double2* __restrict__ V, int64_t ldv, int64_t ldb, double2* __restrict__ z,
+                             int64_t ldz, const int* __restrict__ act, const double2* __restrict__ h, int ldh, int nj,
+                             int64_t n, double* __restrict__ partial) {
+  const int a = blockIdx.y;
+  const int c = blockIdx.x;
+  const int nch = gridDim.x;
+  const double2* Vb = V + (int64_t)act[a] * ldb;
+  double2* za = z + (int64_t)a * ldz;
+  const double2* ha = h + (int64_t)a * ldh;
+  const int64_t i0 = (int64_t)c * kChunkElems;
+  const int64_t i1 = min(n, i0 + kChunkElems);
+  double s = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    double2 q = za[i];
+    for (int j = 0; j < nj; ++j) {
+      const double2 v = Vb[(int64_t)j * ldv + i];
+      const double2 hj = ha[j];
+      q.x -= hj.x * v.x - hj.y * v.y;
+      q.y -= hj.x * v.y + hj.y * v.x;
+    }
+    za[i] = q;
+    s = fma(q.x, q.x, fma(q.y, q.y, s));
+  }
+  __shared__ double red[kChunkThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    partial[(int64_t)a * nch + c] = t;
+  }
+}
+
+// norms2[a] partial sums of |x_a|^2 (x_a = x + row(a) * ldx)
+__global__ void k_norm2_partial(const double2* __restrict__ x, int64_t ldx, const int* __restrict__ rows, int64_t n,
+                                double* __restrict__ partial) {
+  const int a = blockIdx.y;
+  const int c = blockIdx.x;
+  const double2* xa = x + (int64_t)(rows ? rows[a] : a) * ldx;
+  const int64_t i0 = (int64_t)c * kChunkElems;
+  const int64_t i1 = min(n, i0 + kChunkElems);
+  double s = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const double2 q = xa[i];
+    s = fma(q.x, q.x, fma(q.y, q.y, s));
+  }
+  __shared__ double red[kChunkThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    partial[(int64_t)a * gridDim.x + c] = t;
+  }
+}
+
+__global__ void k_reduce_norm(const double* __restrict__ partial, int nch, double* __restrict__ out) {
+  const int a = blockIdx.x;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int c = 0; c < nch; ++c) t += partial[(int64_t)a * nch + c];
+    out[a] = sqrt(t);
+  }
+}
+
+// dst_b = src_a * (1 / nrm[a])  (zero when nrm == 0: breakdown)
+__global__ void k_scale_into(const double2* __restrict__ src, int64_t lds, double2* __restrict__ dst, int64_t ldd,
+                             const int* __restrict__ act, const double* __restrict__ nrm, int64_t n) {
+  const int a = blockIdx.y;
+  const double s = nrm[a] > 0.0 ? 1.0 / nrm[a] : 0.0;
+  const double2* sa = src + (int64_t)a * lds;
+  double2* db = dst + (int64_t)act[a] * ldd;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = sa[i];
+    db[i] = make_double2(v.x * s, v.y * s);
+  }
+}
+
+// dst_a = src_b  (gather rows of a batch)
+__global__ void k_gather(const double2* __restrict__ src, int64_t lds, double2* __restrict__ dst, int64_t ldd,
+                         const int* __restrict__ act, int64_t n) {
+  const int a = blockIdx.y;
+  const double2* sb = src + (int64_t)act[a] * lds;
+  double2* da = dst + (int64_t)a * ldd;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    da[i] = sb[i];
+}
+
+// out_b (+)= sum_{j<cnt[a]} coef[a][j] V_b[j]   (mode 1: add, 0: assign)
+__global__ void k_combine(const double2* __restrict__ V, int64_t ldv, int64_t ldb, const int* __restrict__ act,
+                          const double2* __restrict__ coef, int ldc, const int* __restrict__ cnt,
+                          double2* __restrict__ out, int64_t ldo, int64_t n, int mode) {
+  const int a = blockIdx.y;
+  const int b = act[a];
+  const double2* Vb = V + (int64_t)b * ldb;
+  const double2* ca = coef + (int64_t)a * ldc;
+  double2* ob = out + (int64_t)b * ldo;
+  const int nj = cnt[a];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double2 acc = mode ? ob[i] : make_double2(0.0, 0.0);
+    for (int j = 0; j < nj; ++j) {
+      const double2 v = Vb[(int64_t)j * ldv + i];
+      const double2 c = ca[j];
+      acc.x += c.x * v.x - c.y * v.y;
+      acc.y += c.x * v.y + c.y * v.x;
+    }
+    ob[i] = acc;
+  }
+}
+
+// x_b = b_b - y_b  (residual)
+__global__ void k_sub(const double2* __restrict__ bvec, const double2* __restrict__ y, double2* __restrict__ out,
+                      int64_t n_total) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_total; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_double2(bvec[i].x - y[i].x, bvec[i].y - y[i].y);
+}
+
+__global__ void k_axpy_rows(double2* __restrict__ x, const double2* __restrict__ d, int64_t ld,
+                            const int* __restrict__ act, int64_t n) {
+  const int a = blockIdx.y;
+  double2* xb = x + (int64_t)act[a] * ld;
+  const double2* da = d + (int64_t)a * ld;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    xb[i].x += da[i].x;
+    xb[i].y += da[i].y;
+  }
+}
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t n) {
+    if (n <= cap) return;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    VH_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)));
+    cap = n;
+  }
+  ~DevBuf() { cudaFree(p); }
+};
+
+unsigned grid1(int64_t n) { return (unsigned)std::min<int64_t>(4096, std::max<int64_t>(1, ceil_div(n, 256))); }
+
+// Norms of rows (device) -> host
+std::vector<double> row_norms(const double2* x, int64_t ldx, const std::vector<int>& rows, int64_t n,
+                              DevBuf<int>& d_rows, DevBuf<double>& part, DevBuf<double>& out, cudaStream_t st) {
+  const int na = (int)rows.size();
+  std::vector<double> res(na, 0.0);
+  if (na == 0) return res;
+  d_rows.ensure(na);
+  VH_CUDA_TRY(cudaMemcpyAsync(d_rows.p, rows.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
+  const int nch = (int)std::max<int64_t>(1, ceil_div(n, kChunkElems));
+  part.ensure((size_t)na * nch);
+  out.ensure(na);
+  k_norm2_partial<<<dim3(nch, na), kChunkThreads, 0, st>>>(x, ldx, d_rows.p, n, part.p);
+  k_reduce_norm<<<na, 32, 0, st>>>(part.p, nch, out.p);
+  VH_CUDA_TRY(cudaGetLastError());
+  VH_CUDA_TRY(cudaMemcpyAsync(res.data(), out.p, na * sizeof(double), cudaMemcpyDeviceToHost, st));
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
+  return res;
+}
+
+}  // namespace
+
+namespace vh {
+
+struct GmresOut {
+  std::vector<int> flag, inner, outer;
+  std::vector<double> relres;
+  std::vector<std::vector<double>> resvec;
+  int64_t matvecs = 0;   // RHS-matvecs performed
+  int64_t precons = 0;
+};
+
+// Restarted (F)GMRES for B right-hand sides.  b, x: device, B x n (ld n).  x holds x0 on entry
+// (zero vector allowed).  scale/zslot: host arrays of B.  pcs: B preconditioners or nullptr.
+void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, const double2* scale_h,
+                  const int* zslot_h, const double* tol, int m, int maxit, bool flexible, Prec prec, double2* x,
+                  GmresOut& out) {
+  cudaStream_t st = g->ctx->stream;
+  const int64_t n = g->n;
+  VH_REQUIRE(m >= 1 && maxit >= 1 && B >= 1, ERR_BAD_ARG, "restart and maxit must be positive");
+  // ---- workspace
+  DevBuf<double2> V, Zs, Xc, Wc, Zc, R, hbuf, coef, partc, d_scale;
+  DevBuf<double> partr, nrm;
+  DevBuf<int> d_act, d_cnt, d_rows;
+  const int64_t ldv = n, ldb = (int64_t)(m + 1) * n;
+  V.ensure((size_t)B * (m + 1) * n);
+  if (flexible) Zs.ensure((size_t)B * m * n);
+  Xc.ensure((size_t)B * n);
+  Wc.ensure((size_t)B * n);
+  Zc.ensure((size_t)B * n);
+  R.ensure((size_t)B * n);
+  hbuf.ensure((size_t)B * (m + 2));
+  coef.ensure((size_t)B * (m + 2));
+  d_scale.ensure(B);
+  d_act.ensure(B);
+  d_cnt.ensure(B);
+  const int nch = (int)std::max<int64_t>(1, ceil_div(n, kChunkElems));
+  partc.ensure((size_t)B * nch * (m + 1));
+  partr.ensure((size_t)B * nch);
+  nrm.ensure(B);
+  std::vector<int> pc_dummy;
+  auto apply_A = [&](const std::vector<int>& act, const double2* xin, double2* yout, Prec p) {
+    const int na = (int)act.size();
+    std::vector<double2> sc(na);
+    std::vector<int> zs(na);
+    for (int a = 0; a < na; ++a) {
+      sc[a] = scale_h ? scale_h[act[a]] : make_double2(1.0, 0.0);
+      zs[a] = zslot_h ? zslot_h[act[a]] : 0;
+    }
+    VH_CUDA_TRY(cudaMemcpyAsync(d_scale.p, sc.data(), na * sizeof(double2), cudaMemcpyHostToDevice, st));
+    matvec_device(g, na, xin, yout, d_scale.p, zs.data(), p);
+    VH_CUDA_TRY(cudaStreamSynchronize(st));   // host arrays above must outlive the copies
+    out.matvecs += na;
+  };
+  auto apply_M = [&](const std::vector<int>& act, const double2* xin, double2* yout) {
+    const int na = (int)act.size();
+    if (!pcs) {
+      VH_CUDA_TRY(cudaMemcpyAsync(yout, xin, (size_t)na * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      return;
+    }
+    std::vector<vh_precon*> ps(na);
+    for (int a = 0; a < na; ++a) ps[a] = pcs[act[a]];
+    precon_apply_device(g, na, ps.data(), xin, yout);
+    out.precons += na;
+  };
+  auto upload_act = [&](const std::vector<int>& act) {
+    VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  };
+  std::vector<int> all(B);
+  for (int i = 0; i < B; ++i) all[i] = i;
+
+  out.flag.assign(B, 1);
+  out.inner.assign(B, 0);
+  out.outer.assign(B, 0);
+  out.relres.assign(B, 0.0);
+  out.resvec.assign(B, {});
+
+  // ---- initial residual r = b - A x0 (only if x0 != 0), left preconditioning of r and b
+  const std::vector<double> x0n = row_norms(x, n, all, n, d_rows, partr, nrm, st);
+  upload_act(all);
+  bool any_x0 = false;
+  for (double v : x0n) any_x0 = any_x0 || v > 0;
+  if (any_x0) {
+    apply_A(all, x, Wc.p, PREC_FP64);
+    k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
+  } else {
+    VH_CUDA_TRY(cudaMemcpyAsync(R.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  }
+  std::vector<double> bnorm(B);
+  if (!flexible && pcs) {
+    apply_M(all, R.p, Zc.p);
+    VH_CUDA_TRY(cudaMemcpyAsync(R.p, Zc.p, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    if (any_x0) {
+      apply_M(all, b, Zc.p);
+      bnorm = row_norms(Zc.p, n, all, n, d_rows, partr, nrm, st);
+    }
+  } else if (any_x0) {
+    bnorm = row_norms(b, n, all, n, d_rows, partr, nrm, st);
+  }
+  std::vector<double> rn = row_norms(R.p, n, all, n, d_rows, partr, nrm, st);
+  if (!any_x0) bnorm = rn;
+  std::vector<int> active;
+  for (int i = 0; i < B; ++i) {
+    VH_REQUIRE(bnorm[i] > 0.0, ERR_BAD_ARG, "zero right-hand side");
+    out.resvec[i].push_back(rn[i] / bnorm[i]);
+    if (out.resvec[i].back() > tol[i]) active.push_back(i);
+  }
+  // ---- restart cycles (lock-step across the batch, per-RHS early exit)
+  std::vector<std::vector<cd>> H(B), Rr(B);   // unrotated / rotated Hessenberg, column-major (m+1) x m
+  std::vector<std::vector<cd>> cs(B), sn(B), gv(B);
+  while (!active.empty()) {
+    const int na = (int)active.size();
+    for (int b0 : active) {
+      out.outer[b0]++;
+      H[b0].assign((size_t)(m + 1) * m, cd(0));
+      Rr[b0].assign((size_t)(m + 1) * m, cd(0));
+      cs[b0].assign(m, cd(0));
+      sn[b0].assign(m, cd(0));
+      gv[b0].assign(m + 1, cd(0));
+    }
+    // V_0 = r / |r|
+    upload_act(active);
+    std::vector<double> r0 = row_norms(R.p, n, active, n, d_rows, partr, nrm, st);
+    VH_CUDA_TRY(cudaMemcpyAsync(nrm.p, r0.data(), na * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(R.p, n, Xc.p, n, d_act.p, n);
+    k_scale_into<<<dim3(grid1(n), na), 256, 0, st>>>(Xc.p, n, V.p, ldb, d_act.p, nrm.p, n);
+    VH_CUDA_TRY(cudaGetLastError());
+    for (int a = 0; a < na; ++a) gv[active[a]][0] = cd(r0[a], 0.0);
+    std::vector<int> kdone(na, 0);           // iterations performed in this cycle
+    std::vector<int> run = active;           // RHS still iterating in this cycle
+    std::vector<int> pos(na);                // index of each run entry in `active`
+    for (int a = 0; a < na; ++a) pos[a] = a;
+    for (int k = 0; k < m && !run.empty(); ++k) {
+      const int nr = (int)run.size();
+      upload_act(run);
+      // w = M^-1 A v_k  (left)   or   z_k = M^-1 v_k, w = A z_k  (flexible)
+      k_gather<<<dim3(grid1(n), nr), 256, 0, st>>>(V.p + (int64_t)k * n, ldb, Xc.p, n, d_act.p, n);
+      if (flexible) {
+        apply_M(run, Xc.p, Zc.p);
+        upload_act(run);
+        for (int a = 0; a < nr; ++a)
+          VH_CUDA_TRY(cudaMemcpyAsync(Zs.p + (int64_t)run[a] * m * n + (int64_t)k * n, Zc.p + (int64_t)a * n,
+                                      n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        apply_A(run, Zc.p, Wc.p, prec);
+      } else {
+        apply_A(run, Xc.p, Wc.p, prec);
+        if (pcs) apply_M(run, Wc.p, Zc.p);
+      }
+      upload_act(run);
+      double2* w = (flexible || !pcs) ? Wc.p : Zc.p;
+      // classical Gram-Schmidt: h = V^H w ; w -= V h ; h_{k+1} = |w| (pgmres_iter.m:107-110)
+      k_multidot<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, k + 1, n, partc.p);
+      k_reduce_partials<<<nr, 128, 0, st>>>(partc.p, nch, k + 1, hbuf.p, m + 2);
+      k_cgs_update<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, hbuf.p, m + 2, k + 1, n,
+                                                            partr.p);
+      k_reduce_norm<<<nr, 32, 0, st>>>(partr.p, nch, nrm.p);
+      k_scale_into<<<dim3(grid1(n), nr), 256, 0, st>>>(w, n, V.p + (int64_t)(k + 1) * n, ldb, d_act.p, nrm.p, n);
+      VH_CUDA_TRY(cudaGetLastError());
+      std::vector<double2> hh((size_t)nr * (m + 2));
+      std::vector<double> hn(nr);
+      VH_CUDA_TRY(cudaMemcpyAsync(hh.data(), hbuf.p, hh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+      VH_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm.p, nr * sizeof(double), cudaMemcpyDeviceToHost, st));
+      VH_CUDA_TRY(cudaStreamSynchronize(st));
+      std::vector<int> next, next_pos;
+      for (int a = 0; a < nr; ++a) {
+        const int bb = run[a];
+        auto& Hb = H[bb];
+        auto& Rb = Rr[bb];
+        for (int j = 0; j <= k; ++j) Hb[j + (size_t)k * (m + 1)] = cd(hh[(size_t)a * (m + 2) + j].x, hh[(size_t)a * (m + 2) + j].y);
+        Hb[k + 1 + (size_t)k * (m + 1)] = cd(hn[a], 0.0);
+        // Givens: apply previous rotations to the new column, then annihilate h_{k+1,k}
+        for (int j = 0; j <= k + 1; ++j) Rb[j + (size_t)k * (m + 1)] = Hb[j + (size_t)k * (m + 1)];
+        for (int j = 0; j < k; ++j) {
+          const cd t1 = Rb[j + (size_t)k * (m + 1)], t2 = Rb[j + 1 + (size_t)k * (m + 1)];
+          Rb[j + (size_t)k * (m + 1)] = std::conj(cs[bb][j]) * t1 + std::conj(sn[bb][j]) * t2;
+          Rb[j + 1 + (size_t)k * (m + 1)] = -sn[bb][j] * t1 + cs[bb][j] * t2;
+        }
+        const cd p = Rb[k + (size_t)k * (m + 1)], q = Rb[k + 1 + (size_t)k * (m + 1)];
+        const double den = std::sqrt(std::norm(p) + std::norm(q));
+        cd c = 1.0, s = 0.0;
+        if (den > 0) {
+          c = p / den;
+          s = q / den;
+        }
+        cs[bb][k] = c;
+        sn[bb][k] = s;
+        Rb[k + (size_t)k * (m + 1)] = std::conj(c) * p + std::conj(s) * q;
+        Rb[k + 1 + (size_t)k * (m + 1)] = 0.0;
+        const cd gk = gv[bb][k];
+        gv[bb][k] = std::conj(c) * gk;
+        gv[bb][k + 1] = -s * gk;
+        const double res = std::abs(gv[bb][k + 1]);
+        const int ai = pos[a];
+        kdone[ai] = k + 1;
+        out.resvec[bb].push_back(res / bnorm[bb]);
+        const bool breakdown = !(hn[a] > 0.0);
+        if (!(res < tol[bb] * bnorm[bb]) && !breakdown) {   // pgmres_iter.m:126
+          next.push_back(bb);
+          next_pos.push_back(ai);
+        }
+      }
+      run.swap(next);
+      pos.swap(next_pos);
+    }
+    // ---- cycle end: y = R^-1 g, res = rnorm e1 - H y, x += V y (or Z y), r = V res
+    std::vector<double2> cy((size_t)na * (m + 2)), cr((size_t)na * (m + 2));
+    std::vector<int> cnty(na), cntr(na);
+    for (int a = 0; a < na; ++a) {
+      const int bb = active[a];
+      const int k = kdone[a];
+      std::vector<cd> y(k);
+      for (int i = k - 1; i >= 0; --i) {
+        cd s = gv[bb][i];
+        for (int j = i + 1; j < k; ++j) s -= Rr[bb][i + (size_t)j * (m + 1)] * y[j];
+        y[i] = s / Rr[bb][i + (size_t)i * (m + 1)];
+      }
+      std::vector<cd> res(k + 1, cd(0));
+      res[0] = cd(r0[a], 0.0);
+      for (int j = 0; j < k; ++j)
+        for (int i = 0; i <= j + 1; ++i) res[i] -= H[bb][i + (size_t)j * (m + 1)] * y[j];
+      for (int j = 0; j < k; ++j) cy[(size_t)a * (m + 2) + j] = make_double2(y[j].real(), y[j].imag());
+      for (int j = 0; j <= k; ++j) cr[(size_t)a * (m + 2) + j] = make_double2(res[j].real(), res[j].imag());
+      cnty[a] = k;
+      cntr[a] = k + 1;
+      out.inner[bb] = k;
+    }
+    upload_act(active);
+    VH_CUDA_TRY(cudaMemcpyAsync(coef.p, cy.data(), cy.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VH_CUDA_TRY(cudaMemcpyAsync(d_cnt.p, cnty.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (flexible)
+      k_combine<<<dim3(grid1(n), na), 256, 0, st>>>(Zs.p, n, (int64_t)m * n, d_act.p, coef.p, m + 2, d_cnt.p, x, n, n, 1);
+    else
+      k_combine<<<dim3(grid1(n), na), 256, 0, st>>>(V.p, ldv, ldb, d_act.p, coef.p, m + 2, d_cnt.p, x, n, n, 1);
+    VH_CUDA_TRY(cudaGetLastError());
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    VH_CUDA_TRY(cudaMemcpyAsync(coef.p, cr.data(), cr.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VH_CUDA_TRY(cudaMemcpyAsync(d_cnt.p, cntr.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_combine<<<dim3(grid1(n), na), 256, 0, st>>>(V.p, ldv, ldb, d_act.p, coef.p, m + 2, d_cnt.p, R.p, n, n, 0);
+    VH_CUDA_TRY(cudaGetLastError());
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    // outer loop condition of pgmres.m:153: resvec(it) > tol && outit < maxit
+    std::vector<int> still;
+    for (int bb : active)
+      if (out.resvec[bb].back() > tol[bb] && out.outer[bb] < maxit) still.push_back(bb);
+    active.swap(still);
+  }
+  // ---- true relative residual |b - A x| / |b|  (pgmres.m:181)
+  upload_act(all);
+  apply_A(all, x, Wc.p, PREC_FP64);
+  k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
+  VH_CUDA_TRY(cudaGetLastError());
+  const std::vector<double> rr = row_norms(R.p, n, all, n, d_rows, partr, nrm, st);
+  const std::vector<double> bb = row_norms(b, n, all, n, d_rows, partr, nrm, st);
+  for (int i = 0; i < B; ++i) {
+    out.relres[i] = rr[i] / bb[i];
+    out.flag[i] = out.relres[i] <= tol[i] ? 0 : 1;
+  }
+}
+
+// Mixed precision: iterative refinement in FP64 around complex64-matvec GMRES.
+//   r = b - A x (FP64);  s = M^-1 r;  stop when |s| <= tol |M^-1 b|  (the preconditioned residual
+//   that pgmres monitors);  else solve A d = r with GMRES (complex64 FFT, FP64 Krylov), x += d.
+void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, const double2* scale_h,
+                        const int* zslot_h, const double* tol, int m, int maxit, double inner_tol, int max_refine,
+                        double2* x, GmresOut& out, std::vector<int>& refine_steps) {
+  cudaStream_t st = g->ctx->stream;
+  const int64_t n = g->n;
+  DevBuf<double2> R, S, D, Wc, Rc;
+  DevBuf<double> partr, nrm;
+  DevBuf<int> d_rows, d_act;
+  R.ensure((size_t)B * n);
+  S.ensure((size_t)B * n);
+  Wc.ensure((size_t)B * n);
+  std::vector<int> all(B);
+  for (int i = 0; i < B; ++i) all[i] = i;
+  auto A64 = [&](const std::vector<int>& act, const double2* xin, double2* yout) {
+    const int na = (int)act.size();
+    std::vector<int> zs(na);
+    std::vector<double2> sc(na);
+    for (int a = 0; a < na; ++a) {
+      zs[a] = zslot_h ? zslot_h[act[a]] : 0;
+      sc[a] = scale_h ? scale_h[act[a]] : make_double2(1.0, 0.0);
+    }
+    DevBuf<double2> dsc;
+    dsc.ensure(na);
+    VH_CUDA_TRY(cudaMemcpyAsync(dsc.p, sc.data(), na * sizeof(double2), cudaMemcpyHostToDevice, st));
+    matvec_device(g, na, xin, yout, dsc.p, zs.data(), PREC_FP64);
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    out.matvecs += na;
+  };
+  auto M = [&](const std::vector<int>& act, const double2* xin, double2* yout) {
+    const int na = (int)act.size();
+    if (!pcs) {
+      VH_CUDA_TRY(cudaMemcpyAsync(yout, xin, (size_t)na * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      return;
+    }
+    std::vector<vh_precon*> ps(na);
+    for (int a = 0; a < na; ++a) ps[a] = pcs[act[a]];
+    precon_apply_device(g, na, ps.data(), xin, yout);
+    out.precons += na;
+  };
+  out.flag.assign(B, 1);
+  out.inner.assign(B, 0);
+  out.outer.assign(B, 0);
+  out.relres.assign(B, 0.0);
+  out.resvec.assign(B, {});
+  refine_steps.assign(B, 0);
+  VH_CUDA_TRY(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(double2), st));
+  // |M^-1 b|
+  M(all, b, S.p);
+  std::vector<double> mb = row_norms(S.p, n, all, n, d_rows, partr, nrm, st);
+  std::vector<int> active = all;
+  VH_CUDA_TRY(cudaMemcpyAsync(R.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  std::vector<double> sn = mb;   // |M^-1 r| with x = 0
+  for (int i = 0; i < B; ++i) out.resvec[i].push_back(1.0);
+  for (int step = 0; step < max_refine && !active.empty(); ++step) {
+    const int na = (int)active.size();
+    // compact r of the active RHS and solve A d = r in reduced precision
+    Rc.ensure((size_t)na * n);
+    D.ensure((size_t)na * n);
+    d_act.ensure(na);
+    VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, active.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(R.p, n, Rc.p, n, d_act.p, n);
+    VH_CUDA_TRY(cudaMemsetAsync(D.p, 0, (size_t)na * n * sizeof(double2), st));
+    std::vector<double2> sc(na);
+    std::vector<int> zs(na);
+    std::vector<double> tl(na);
+    std::vector<vh_precon*> ps(na);
+    for (int a = 0; a < na; ++a) {
+      const int bb = active[a];
+      sc[a] = scale_h ? scale_h[bb] : make_double2(1.0, 0.0);
+      zs[a] = zslot_h ? zslot_h[bb] : 0;
+      // ask the inner solve for what is still missing, but not below its precision floor
+      tl[a] = std::max(inner_tol, 0.5 * tol[bb] * mb[bb] / std::max(sn[bb], 1e-300));
+      ps[a] = pcs ? pcs[bb] : nullptr;
+    }
+    GmresOut inner;
+    gmres_device(g, na, pcs ? ps.data() : nullptr, Rc.p, sc.data(), zs.data(), tl.data(), m, maxit, false, PREC_FP32,
+                 D.p, inner);
+    out.matvecs += inner.matvecs;
+    out.precons += inner.precons;
+    VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, active.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_axpy_rows<<<dim3(grid1(n), na), 256, 0, st>>>(x, D.p, n, d_act.p, n);
+    VH_CUDA_TRY(cudaGetLastError());
+    for (int a = 0; a < na; ++a) {
+      const int bb = active[a];
+      refine_steps[bb]++;
+      out.inner[bb] += (int)inner.resvec[a].size() - 1;
+      out.outer[bb] += inner.outer[a];
+    }
+    // r = b - A x (FP64), s = M^-1 r, on compact copies of the active rows
+    std::vector<int> still;
+    {
+      DevBuf<double2> Xa, Ya, Ba, Sa;
+      Xa.ensure((size_t)na * n);
+      Ya.ensure((size_t)na * n);
+      Ba.ensure((size_t)na * n);
+      Sa.ensure((size_t)na * n);
+      k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(x, n, Xa.p, n, d_act.p, n);
+      k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(b, n, Ba.p, n, d_act.p, n);
+      A64(active, Xa.p, Ya.p);
+      k_sub<<<grid1((int64_t)na * n), 256, 0, st>>>(Ba.p, Ya.p, Ya.p, (int64_t)na * n);
+      std::vector<int> seq(na);
+      for (int a = 0; a < na; ++a) seq[a] = a;
+      M(active, Ya.p, Sa.p);
+      std::vector<double> snorm = row_norms(Sa.p, n, seq, n, d_rows, partr, nrm, st);
+      // scatter residuals back
+      for (int a = 0; a < na; ++a)
+        VH_CUDA_TRY(cudaMemcpyAsync(R.p + (int64_t)active[a] * n, Ya.p + (int64_t)a * n, n * sizeof(double2),
+                                    cudaMemcpyDeviceToDevice, st));
+      VH_CUDA_TRY(cudaStreamSynchronize(st));
+      for (int a = 0; a < na; ++a) {
+        const int bb = active[a];
+        sn[bb] = snorm[a];
+        out.resvec[bb].push_back(snorm[a] / mb[bb]);
+        if (snorm[a] > tol[bb] * mb[bb]) still.push_back(bb);
+      }
+    }
+    active.swap(still);
+  }
+  // true relative residual
+  A64(all, x, Wc.p);
+  k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
+  const std::vector<double> rr = row_norms(R.p, n, all, n, d_rows, partr, nrm, st);
+  const std::vector<double> bb = row_norms(b, n, all, n, d_rows, partr, nrm, st);
+  for (int i = 0; i < B; ++i) {
+    out.relres[i] = rr[i] / bb[i];
+    out.flag[i] = out.relres[i] <= tol[i] ? 0 : 1;   // same rule as pgmres.m:182-186
+  }
+}
+
+}  // namespace vh
+
+namespace {
+template <typename F>
+vh_status guarded_g(vh_ctx* ctx, F&& f) {
+  try {
+    f();
+    return VH_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->last_error = e.msg;
+    return (vh_status)e.st;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->last_error = "host allocation failed";
+    return VH_ERR_OOM;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
+                   int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
+                   double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded_g(g->ctx, [&] {
+    VH_REQUIRE(B >= 1 && b && x && tol, ERR_BAD_ARG, "bad gmres arguments");
+    VH_REQUIRE(!(flexible && prec == VH_PREC_FP32), ERR_UNSUPPORTED, "mixed precision uses the left-preconditioned form");
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    cudaStream_t st = g->ctx->stream;
+    const int64_t n = g->n;
+    DevBuf<double2> db, dx;
+    db.ensure((size_t)B * n);
+    dx.ensure((size_t)B * n);
+    VH_CUDA_TRY(cudaMemcpyAsync(db.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VH_CUDA_TRY(cudaMemsetAsync(dx.p, 0, (size_t)B * n * sizeof(double2), st));
+    GmresOut o;
+    std::vector<int> steps;
+    if (prec == VH_PREC_FP32)
+      solve_mixed_device(g, B, pcs, db.p, (const double2*)scale, zslot, tol, restart, maxit, 1e-4, 20, dx.p, o, steps);
+    else
+      gmres_device(g, B, pcs, db.p, (const double2*)scale, zslot, tol, restart, maxit, flexible != 0, PREC_FP64, dx.p, o);
+    VH_CUDA_TRY(cudaMemcpyAsync(x, dx.p, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int i = 0; i < B; ++i) {
+      if (flag) flag[i] = o.flag[i];
+      if (relres) relres[i] = o.relres[i];
+      if (iter) {
+        iter[2 * i] = o.inner[i];
+        iter[2 * i + 1] = o.outer[i];
+      }
+      if (nres) nres[i] = (int)o.resvec[i].size();
+      if (resvec)
+        for (int k = 0; k < resvec_len && k < (int)o.resvec[i].size(); ++k) resvec[(size_t)i * resvec_len + k] = o.resvec[i][k];
+    }
+  });
+}
+
+}  // extern "C"

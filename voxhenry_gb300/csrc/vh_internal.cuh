@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "vh_common.cuh"
+#include "vh_chol.cuh"
 #include "vh_conv.cuh"
 
 struct vh_ctx {
@@ -34,9 +35,19 @@ struct Csr {
 void spmv_batched(const Csr& A, int B, const double2* x, int64_t ldx, int64_t xoff, double2* y, int64_t ldy,
                   int64_t yoff, int mode, cudaStream_t st);
 
-// Host CSC (num_node x ncol) -> device CSR of A and of A^T.
+// Host copy of a CSR matrix.
+struct HostCsr {
+  std::vector<int32_t> rp, col;
+  std::vector<double> val;
+};
+
+// Host CSC (nrow x ncol) -> host CSR of A and of A^T.
+void csc_to_host(int64_t nrow, int64_t ncol, const int64_t* jc, const int64_t* ir, const double* pr, HostCsr& hA,
+                 HostCsr& hAT);
+
+// Host CSC (num_node x ncol) -> device CSR of A and of A^T (host copies returned too).
 void csc_upload(int64_t nrow, int64_t ncol, const int64_t* jc, const int64_t* ir, const double* pr, Csr& A, Csr& AT,
-                cudaStream_t st);
+                HostCsr& hA, HostCsr& hAT, cudaStream_t st);
 
 }  // namespace vh
 
@@ -48,6 +59,14 @@ struct vh_geom {
   std::vector<int64_t> idxS;       // host copy, 1-based
   vh::ConvPlan conv;
   vh::Csr Ae, AeT;                 // nphi x nc, nc x nphi
+  vh::HostCsr hAe, hAeT;           // host copies (symbolic analysis)
+  bool has_conv = false;           // false for a preconditioner-only geometry (no tensor)
+  vh::CholSymbolic chol;           // built on the first 'schur_invert' preconditioner
+  bool chol_ready = false;
+  double2* pc_tmp = nullptr;       // chol_solve update vectors, B * u_total
+  size_t pc_tmp_cap = 0;
+  double** pc_ptrs = nullptr;      // device pointer tables (A_inv, W) for batched applies
+  int pc_ptrs_cap = 0;
   std::vector<double2*> zslots;    // per slot: nv complex (device)
   double2* ones = nullptr;         // device, capacity ones_cap complex ones
   int ones_cap = 0;

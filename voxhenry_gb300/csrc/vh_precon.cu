@@ -1,0 +1,274 @@
+// Schur-complement block preconditioner of the [Z -Ar^T; Ar 0] system.
+//
+// prepare (lse_sparse_precon_prepare.m:33-64, 90-154):
+//   A_inv = |1 / (z/dx + st1)| (Jx,Jy,Jz), |1 / (z/(6dx) + st2)| (J2D), |1 / (z/(2dx) + st3)| (J3D), real;
+//   S = Ar A_inv Ar^T, factored (sparse Cholesky; the reference uses CHOLMOD LDL^T or LU).
+// multiply (lse_sparse_precon_multiply.m:61-88):
+//   bb = x_phi - Ar (A_inv x_J);  phi = S^-1 bb;  y_J = (x_J + Ar^T phi) A_inv;  y_phi = phi.
+#include <vector>
+
+#include "../../include/voxhenry_gpu.h"
+#include "vh_internal.cuh"
+
+struct vh_precon {
+  vh_geom* g = nullptr;
+  int kind = 0;
+  double* A_inv = nullptr;   // nc reals
+  double* W = nullptr;       // factor storage
+};
+
+namespace vh {
+
+constexpr int kLeafPanels = 64;
+
+__global__ void k_a_inv(const double2* __restrict__ z, int64_t nv, double dx, double2 s1, double2 s2, double2 s3,
+                        double* __restrict__ out) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const double2 zz = z[v];
+    const double2 st[3] = {s1, s2, s3};
+    const double sc[3] = {1.0 / dx, 1.0 / (6.0 * dx), 1.0 / (2.0 * dx)};
+    double a[3];
+    for (int k = 0; k < 3; ++k) {
+      const double re = zz.x * sc[k] + st[k].x, im = zz.y * sc[k] + st[k].y;
+      a[k] = 1.0 / hypot(re, im);        // |1/w| = 1/|w|
+    }
+    out[v] = a[0];
+    out[nv + v] = a[0];
+    out[2 * nv + v] = a[0];
+    out[3 * nv + v] = a[1];
+    out[4 * nv + v] = a[2];
+  }
+}
+
+// y_phi[b] = x_phi[b] - Ar (A_inv_b .* x_J[b])
+__global__ void k_precon_rhs(int64_t nphi, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                             const double* __restrict__ val, double* const* __restrict__ ainv,
+                             const double2* __restrict__ x, double2* __restrict__ y, int64_t ld, int64_t nc) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (r >= nphi) return;
+  const double2* xb = x + b * ld;
+  const double* ai = ainv[b];
+  double2 acc = xb[nc + r];
+  for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
+    const int32_t q = col[k];
+    const double a = val[k] * ai[q];
+    acc.x -= a * xb[q].x;
+    acc.y -= a * xb[q].y;
+  }
+  y[b * ld + nc + r] = acc;
+}
+
+// y_J[b] = (x_J[b] + Ar^T y_phi[b]) .* A_inv_b
+__global__ void k_precon_finish(int64_t nc, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                const double* __restrict__ val, double* const* __restrict__ ainv,
+                                const double2* __restrict__ x, double2* __restrict__ y, int64_t ld) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (q >= nc) return;
+  const double2* yb = y + b * ld + nc;
+  double2 acc = x[b * ld + q];
+  for (int32_t k = rp[q]; k < rp[q + 1]; ++k) {
+    const double a = val[k];
+    const double2 v = yb[col[k]];
+    acc.x = fma(a, v.x, acc.x);
+    acc.y = fma(a, v.y, acc.y);
+  }
+  const double s = ainv[b][q];
+  y[b * ld + q] = make_double2(acc.x * s, acc.y * s);
+}
+
+void ensure_symbolic(vh_geom* g) {
+  if (g->chol_ready) return;
+  chol_symbolic(g->chol, g->L, g->M, g->N, g->nv, g->idxS.data(), g->nphi, g->hAe.rp, g->hAe.col, g->hAe.val,
+                g->hAeT.rp, g->hAeT.col, g->hAeT.val, kLeafPanels, g->ctx->stream);
+  g->chol_ready = true;
+}
+
+// Applies B preconditioners (one per RHS, all of the same kind); x, y device, leading dimension n.
+void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* x, double2* y) {
+  cudaStream_t st = g->ctx->stream;
+  const int kind = pcs[0]->kind;
+  for (int b = 0; b < B; ++b) {
+    VH_REQUIRE(pcs[b] && pcs[b]->g == g, ERR_BAD_ARG, "preconditioner belongs to another geometry");
+    VH_REQUIRE(pcs[b]->kind == kind, ERR_BAD_ARG, "mixed preconditioner kinds in one batch");
+  }
+  if (kind == VH_PRECON_NONE) {
+    if (x != y) VH_CUDA_TRY(cudaMemcpyAsync(y, x, (size_t)B * g->n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    return;
+  }
+  VH_REQUIRE(x != y, ERR_BAD_ARG, "preconditioner apply cannot run in place");
+  if (B > g->pc_ptrs_cap) {
+    cudaFree(g->pc_ptrs);
+    g->pc_ptrs = nullptr;
+    g->pc_ptrs_cap = 0;
+    VH_CUDA_TRY(cudaMalloc(&g->pc_ptrs, 2 * (size_t)B * sizeof(double*)));
+    g->pc_ptrs_cap = B;
+  }
+  std::vector<double*> h(2 * (size_t)B);
+  for (int b = 0; b < B; ++b) {
+    h[b] = pcs[b]->A_inv;
+    h[B + b] = pcs[b]->W;
+  }
+  double** d_ainv = g->pc_ptrs;
+  double** d_w = g->pc_ptrs + B;
+  VH_CUDA_TRY(cudaMemcpyAsync(g->pc_ptrs, h.data(), 2 * (size_t)B * sizeof(double*), cudaMemcpyHostToDevice, st));
+  const size_t need = (size_t)B * std::max<int64_t>(1, g->chol.u_total);
+  if (need > g->pc_tmp_cap) {
+    cudaFree(g->pc_tmp);
+    g->pc_tmp = nullptr;
+    g->pc_tmp_cap = 0;
+    VH_CUDA_TRY(cudaMalloc(&g->pc_tmp, need * sizeof(double2)));
+    g->pc_tmp_cap = need;
+  }
+  if (g->nphi > 0) {
+    k_precon_rhs<<<dim3((unsigned)ceil_div(g->nphi, 256), B), 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val,
+                                                                           d_ainv, x, y, g->n, g->nc);
+    VH_CUDA_TRY(cudaGetLastError());
+    chol_solve(g->chol, B, d_w, y, g->n, g->nc, g->pc_tmp, st);
+  }
+  if (g->nc > 0) {
+    k_precon_finish<<<dim3((unsigned)ceil_div(g->nc, 256), B), 256, 0, st>>>(g->nc, g->AeT.rowptr, g->AeT.col,
+                                                                            g->AeT.val, d_ainv, x, y, g->n);
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+  // keep the host pointer table alive until the copy has been consumed
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+}  // namespace vh
+
+using namespace vh;
+
+namespace {
+template <typename F>
+vh_status guarded_pc(vh_ctx* ctx, F&& f) {
+  try {
+    f();
+    return VH_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->last_error = e.msg;
+    return (vh_status)e.st;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->last_error = "host allocation failed";
+    return VH_ERR_OOM;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_sparse_precon, int zslot,
+                           vh_precon** out) {
+  if (!g || !out) return VH_ERR_BAD_ARG;
+  *out = nullptr;
+  auto* p = new vh_precon();
+  p->g = g;
+  p->kind = kind;
+  vh_status s = guarded_pc(g->ctx, [&] {
+    VH_REQUIRE(kind == VH_PRECON_NONE || kind == VH_PRECON_SCHUR_INVERT, ERR_UNSUPPORTED,
+               "preconditioner kind not supported (schur_approx / schur_gmres / schur_invert_original)");
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    if (kind == VH_PRECON_NONE) return;
+    VH_REQUIRE(st_sparse_precon, ERR_BAD_ARG, "st_sparse_precon is required");
+    VH_REQUIRE(zslot >= 0 && zslot < (int)g->zslots.size() && g->zslots[zslot], ERR_BAD_ARG, "z slot not set");
+    cudaStream_t st = g->ctx->stream;
+    VH_CUDA_TRY(cudaMalloc(&p->A_inv, std::max<int64_t>(1, g->nc) * sizeof(double)));
+    const double2 s1 = make_double2(st_sparse_precon[0], st_sparse_precon[1]);
+    const double2 s2 = make_double2(st_sparse_precon[2], st_sparse_precon[3]);
+    const double2 s3 = make_double2(st_sparse_precon[4], st_sparse_precon[5]);
+    if (g->nv) k_a_inv<<<256, 256, 0, st>>>(g->zslots[zslot], g->nv, g->dx, s1, s2, s3, p->A_inv);
+    VH_CUDA_TRY(cudaGetLastError());
+    ensure_symbolic(g);
+    VH_CUDA_TRY(cudaMalloc(&p->W, std::max<int64_t>(1, g->chol.w_total) * sizeof(double)));
+    chol_factor(g->chol, p->A_inv, p->W, st);
+  });
+  if (s != VH_OK) {
+    vh_precon_destroy(p);
+    return s;
+  }
+  *out = p;
+  return VH_OK;
+}
+
+void vh_precon_destroy(vh_precon* p) {
+  if (!p) return;
+  if (p->g) cudaSetDevice(p->g->ctx->device);
+  cudaFree(p->A_inv);
+  cudaFree(p->W);
+  delete p;
+}
+
+vh_status vh_precon_stats(const vh_precon* p, int64_t* nnz_factor, double* flops, int* nfronts, int* max_front) {
+  if (!p || !p->g) return VH_ERR_BAD_ARG;
+  const CholSymbolic& s = p->g->chol;
+  if (nnz_factor) *nnz_factor = s.nnz_l;
+  if (flops) *flops = s.flops;
+  if (nfronts) *nfronts = s.nfronts;
+  if (max_front) *max_front = s.max_nf;
+  return VH_OK;
+}
+
+vh_status vh_schur_analyze(int L, int M, int N, int64_t nv, const int64_t* idxS, int64_t num_node,
+                           const int64_t* Ae_jc, const int64_t* Ae_ir, const double* Ae_pr, int64_t* nnz_factor,
+                           double* flops, int* nfronts, int* max_front, int64_t* factor_bytes) {
+  try {
+    VH_REQUIRE(L >= 1 && M >= 1 && N >= 1 && nv >= 0 && num_node >= 0 && Ae_jc && (nv == 0 || idxS), ERR_BAD_ARG,
+               "bad arguments");
+    HostCsr hA, hAT;
+    csc_to_host(num_node, 5 * nv, Ae_jc, Ae_ir, Ae_pr, hA, hAT);
+    CholSymbolic s;
+    chol_symbolic(s, L, M, N, nv, idxS, num_node, hA.rp, hA.col, hA.val, hAT.rp, hAT.col, hAT.val, kLeafPanels,
+                  nullptr, false);
+    if (nnz_factor) *nnz_factor = s.nnz_l;
+    if (flops) *flops = s.flops;
+    if (nfronts) *nfronts = s.nfronts;
+    if (max_front) *max_front = s.max_nf;
+    if (factor_bytes) *factor_bytes = s.w_total * (int64_t)sizeof(double);
+    return VH_OK;
+  } catch (const Error& e) {
+    return (vh_status)e.st;
+  } catch (const std::bad_alloc&) {
+    return VH_ERR_OOM;
+  }
+}
+
+vh_status vh_precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const void* x_dev, void* y_dev) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded_pc(g->ctx, [&] {
+    VH_REQUIRE(B >= 1 && pcs && x_dev && y_dev, ERR_BAD_ARG, "bad preconditioner arguments");
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    precon_apply_device(g, B, pcs, (const double2*)x_dev, (double2*)y_dev);
+  });
+}
+
+vh_status vh_precon_apply(vh_geom* g, int B, vh_precon* const* pcs, const double* x, double* y) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded_pc(g->ctx, [&] {
+    VH_REQUIRE(B >= 1 && pcs && x && y, ERR_BAD_ARG, "bad preconditioner arguments");
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    cudaStream_t st = g->ctx->stream;
+    const size_t bytes = (size_t)B * g->n * sizeof(double2);
+    double2 *dx = nullptr, *dy = nullptr;
+    VH_CUDA_TRY(cudaMalloc(&dx, bytes));
+    cudaError_t e = cudaMalloc(&dy, bytes);
+    if (e != cudaSuccess) {
+      cudaFree(dx);
+      VH_CUDA_TRY(e);
+    }
+    try {
+      VH_CUDA_TRY(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, st));
+      precon_apply_device(g, B, pcs, dx, dy);
+      VH_CUDA_TRY(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, st));
+      VH_CUDA_TRY(cudaStreamSynchronize(st));
+    } catch (...) {
+      cudaFree(dx);
+      cudaFree(dy);
+      throw;
+    }
+    cudaFree(dx);
+    cudaFree(dy);
+  });
+}
+
+}  // extern "C"

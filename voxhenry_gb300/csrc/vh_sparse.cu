@@ -59,35 +59,42 @@ static void upload_csr(int64_t nrows, int64_t ncols, const std::vector<int32_t>&
   VH_CUDA_TRY(cudaStreamSynchronize(st));
 }
 
-void csc_upload(int64_t nrow, int64_t ncol, const int64_t* jc, const int64_t* ir, const double* pr, Csr& A, Csr& AT,
-                cudaStream_t st) {
+void csc_to_host(int64_t nrow, int64_t ncol, const int64_t* jc, const int64_t* ir, const double* pr, HostCsr& hA,
+                 HostCsr& hAT) {
   const int64_t nnz = jc[ncol];
   VH_REQUIRE(jc[0] == 0 && nnz >= 0 && nnz < (1LL << 31), ERR_BAD_ARG, "bad CSC column offsets");
-  // CSC of A is CSR of A^T
-  std::vector<int32_t> rpT(ncol + 1), colT(nnz);
-  std::vector<double> valT(nnz);
-  for (int64_t j = 0; j <= ncol; ++j) rpT[j] = (int32_t)jc[j];
-  for (int64_t k = 0; k < nnz; ++k) {
-    VH_REQUIRE(ir[k] >= 0 && ir[k] < nrow, ERR_BAD_ARG, "CSC row index out of range");
-    colT[k] = (int32_t)ir[k];
-    valT[k] = pr[k];
-  }
   for (int64_t j = 0; j < ncol; ++j)
     VH_REQUIRE(jc[j + 1] >= jc[j], ERR_BAD_ARG, "CSC column offsets must be non-decreasing");
+  // CSC of A is CSR of A^T
+  hAT.rp.assign(ncol + 1, 0);
+  hAT.col.assign(nnz, 0);
+  hAT.val.assign(nnz, 0.0);
+  for (int64_t j = 0; j <= ncol; ++j) hAT.rp[j] = (int32_t)jc[j];
+  for (int64_t k = 0; k < nnz; ++k) {
+    VH_REQUIRE(ir[k] >= 0 && ir[k] < nrow, ERR_BAD_ARG, "CSC row index out of range");
+    hAT.col[k] = (int32_t)ir[k];
+    hAT.val[k] = pr[k];
+  }
   // transpose -> CSR of A
-  std::vector<int32_t> rp(nrow + 1, 0), col(nnz);
-  std::vector<double> val(nnz);
-  for (int64_t k = 0; k < nnz; ++k) rp[ir[k] + 1]++;
-  for (int64_t r = 0; r < nrow; ++r) rp[r + 1] += rp[r];
-  std::vector<int32_t> pos(rp.begin(), rp.end() - 1);
+  hA.rp.assign(nrow + 1, 0);
+  hA.col.assign(nnz, 0);
+  hA.val.assign(nnz, 0.0);
+  for (int64_t k = 0; k < nnz; ++k) hA.rp[ir[k] + 1]++;
+  for (int64_t r = 0; r < nrow; ++r) hA.rp[r + 1] += hA.rp[r];
+  std::vector<int32_t> pos(hA.rp.begin(), hA.rp.end() - 1);
   for (int64_t j = 0; j < ncol; ++j)
     for (int64_t k = jc[j]; k < jc[j + 1]; ++k) {
       const int32_t q = pos[ir[k]]++;
-      col[q] = (int32_t)j;
-      val[q] = pr[k];
+      hA.col[q] = (int32_t)j;
+      hA.val[q] = pr[k];
     }
-  upload_csr(nrow, ncol, rp, col, val, A, st);
-  upload_csr(ncol, nrow, rpT, colT, valT, AT, st);
+}
+
+void csc_upload(int64_t nrow, int64_t ncol, const int64_t* jc, const int64_t* ir, const double* pr, Csr& A, Csr& AT,
+                HostCsr& hA, HostCsr& hAT, cudaStream_t st) {
+  csc_to_host(nrow, ncol, jc, ir, pr, hA, hAT);
+  upload_csr(nrow, ncol, hA.rp, hA.col, hA.val, A, st);
+  upload_csr(ncol, nrow, hAT.rp, hAT.col, hAT.val, AT, st);
 }
 
 }  // namespace vh

@@ -1,0 +1,127 @@
+"""Batched frequency sweep of VoxHenry_executer.m:215-329 on the GPU.
+
+All frequencies and ports of a job are solved as one batch of right-hand sides: one FFT
+matvec call per Krylov step for the whole batch (the tensor spectrum fN_all2 is shared, each RHS
+carries its own j*omega*mu), one Schur-complement factor per frequency (shared by the ports of
+that frequency), one Krylov space per RHS.  Y(:, p) = sum(rhs .* x) (no conjugate,
+VoxHenry_executer.m:311-316), Z = inv(Y), R = |Re Z|, L = |Im Z| / (2 pi f) (:327-328).
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import vie
+
+MU0 = 4 * np.pi * 1e-7     # EMconstants.m:13
+
+
+@dataclass
+class Problem:
+    """Inputs of the solve loop (the executer's state after VoxHenry_executer.m:200)."""
+    L: int
+    M: int
+    N: int
+    dx: float
+    sigma_e: np.ndarray               # (L, M, N)
+    lambdaL: np.ndarray | None
+    idxS: np.ndarray                  # 1-based
+    Ar: sp.csc_matrix                 # Ae with port rows removed
+    rhs: np.ndarray                   # (n, num_ports) real
+    fN_all2: np.ndarray               # (2L, 2M, 2N, 7) complex, without j*omega*mu
+    st2: np.ndarray                   # (3,) complex self terms, without j*omega*mu
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def num_ports(self):
+        return self.rhs.shape[1]
+
+
+def z_arrays(sigma_e, lambdaL, omega):
+    """VoxHenry_executer.m:231-259 -> (z_real, z_imag or None)."""
+    if lambdaL is None:
+        with np.errstate(divide="ignore"):
+            return 1.0 / sigma_e, None
+    den = (omega * MU0 * sigma_e * lambdaL**2) ** 2 + 1
+    z_real = (sigma_e * (omega * MU0 * lambdaL**2) ** 2) / den
+    z_imag = (1j * omega * MU0 * lambdaL**2) / den
+    sel = (np.abs(lambdaL) <= 1e-12) & (np.abs(sigma_e) > 1e-12)
+    with np.errstate(divide="ignore"):
+        inv = 1.0 / sigma_e
+    return np.where(sel, inv, z_real), np.where(sel, 0.0, z_imag)
+
+
+def executer_tol(f: float) -> float:
+    """VoxHenry_executer.m:219-223."""
+    return 1e-12 if f < 1e6 else 1e-8
+
+
+class Sweep:
+    """Device-resident job: geometry (tensor, Ae, z slots) plus one factor per frequency."""
+
+    def __init__(self, prob: Problem, freqs, want_fp32=True, precon="schur_invert"):
+        self.prob = prob
+        self.freqs = np.asarray(freqs, dtype=np.float64)
+        t0 = time.perf_counter()
+        z0, zi0 = z_arrays(prob.sigma_e, prob.lambdaL, 2 * np.pi * self.freqs[0])
+        self.geom = vie.Geometry(prob.fN_all2, prob.Ar, z0, zi0, prob.dx, prob.idxS, want_fp32=want_fp32)
+        self.super = prob.lambdaL is not None
+        self.zslot = np.zeros(len(self.freqs), dtype=np.int32)
+        if self.super:                                   # omega-dependent z: one slot per frequency
+            for i, f in enumerate(self.freqs):
+                zr, zi = z_arrays(prob.sigma_e, prob.lambdaL, 2 * np.pi * f)
+                self.geom.set_z(i, zr, zi)
+                self.zslot[i] = i
+        self.t_setup = time.perf_counter() - t0
+        self.precon_kind = precon
+        self.pcs = None
+        self.t_factor = 0.0
+
+    def prepare(self):
+        """lse_sparse_precon_prepare for every frequency (VoxHenry_executer.m:273)."""
+        t0 = time.perf_counter()
+        self.pcs = []
+        for i, f in enumerate(self.freqs):
+            jwmu = 1j * 2 * np.pi * f * MU0
+            self.pcs.append(self.geom.precon(jwmu * self.prob.st2, zslot=int(self.zslot[i]), kind=self.precon_kind))
+        self.t_factor = time.perf_counter() - t0
+        return self
+
+    def solve(self, restart=50, tol=None, maxit=10, prec="fp64", flexible=False):
+        """Solves every (frequency, port) RHS in one batch; returns R, L, Y, Z and solver stats."""
+        if self.pcs is None:
+            self.prepare()
+        P = self.prob.num_ports
+        F = len(self.freqs)
+        B = F * P
+        rhs = self.prob.rhs.astype(np.complex128)
+        b = np.empty((B, self.geom.n), dtype=np.complex128)
+        scale = np.empty(B, dtype=np.complex128)
+        zsl = np.empty(B, dtype=np.int32)
+        tolv = np.empty(B)
+        pcs = []
+        for fi, f in enumerate(self.freqs):
+            for p in range(P):
+                k = fi * P + p
+                b[k] = rhs[:, p]
+                scale[k] = 1j * 2 * np.pi * f * MU0
+                zsl[k] = self.zslot[fi]
+                tolv[k] = executer_tol(f) if tol is None else tol
+                pcs.append(self.pcs[fi])
+        t0 = time.perf_counter()
+        out = self.geom.solve(b, pcs=pcs, scale=scale, zslot=zsl, restart=restart, tol=tolv, maxit=maxit,
+                              flexible=flexible, prec=prec)
+        t_solve = time.perf_counter() - t0
+        x = out["x"]
+        Y = np.zeros((F, P, P), dtype=np.complex128)
+        for fi in range(F):
+            for p in range(P):
+                Y[fi, :, p] = self.prob.rhs.T @ x[fi * P + p]
+        Z = np.linalg.inv(Y)
+        R = np.abs(Z.real)
+        Lh = np.abs(Z.imag) / (2 * np.pi * self.freqs)[:, None, None]
+        return {"R": R, "L": Lh, "Y": Y, "Z": Z, "x": x, "flag": out["flag"], "relres": out["relres"],
+                "iter": out["iter"], "resvec": out["resvec"], "t_solve": t_solve, "t_factor": self.t_factor}

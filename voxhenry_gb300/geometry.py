@@ -50,18 +50,20 @@ def bar(L=64, M=16, N=16, dx=0.5e-6, sigma=5.8e7, freqs=None) -> Workload:
     return Workload("bar", s, dx, [lft], [rgt], f, tol=1e-8, restart=50)
 
 
-def two_bars(L=128, M=64, N=32, dx=1e-6, freqs=None) -> Workload:
-    """Copper (5.8e7) and aluminium (3.5e7) bars 100 x 10 x 10 voxels, 20-voxel gap, one port each."""
+def two_bars(L=128, M=64, N=32, dx=1e-6, freqs=None, xr=(14, 114), zr=(11, 21), y1=(12, 22), y2=(42, 52),
+             sigmas=(5.8e7, 3.5e7)) -> Workload:
+    """Copper (5.8e7) and aluminium (3.5e7) bars 100 x 10 x 10 voxels, 20-voxel gap, one port each
+    (0-based half-open voxel ranges)."""
     s = np.zeros((L, M, N), order="F")
-    xs, zs = slice(14, 114), slice(11, 21)
-    s[xs, 12:22, zs] = 5.8e7
-    s[xs, 42:52, zs] = 3.5e7
+    xs, zs = slice(*xr), slice(*zr)
+    s[xs, slice(*y1), zs] = sigmas[0]
+    s[xs, slice(*y2), zs] = sigmas[1]
     lft, rgt = [], []
-    for ys in (slice(12, 22), slice(42, 52)):
+    for ys in (slice(*y1), slice(*y2)):
         m1 = np.zeros(s.shape, bool)
-        m1[14, ys, zs] = True
+        m1[xr[0], ys, zs] = True
         m2 = np.zeros(s.shape, bool)
-        m2[113, ys, zs] = True
+        m2[xr[1] - 1, ys, zs] = True
         lft.append(face_nodes(m1, "-x"))
         rgt.append(face_nodes(m2, "+x"))
     f = np.logspace(3, 10, 16) if freqs is None else np.asarray(freqs, dtype=np.float64)
