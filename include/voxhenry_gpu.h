@@ -69,6 +69,13 @@ vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const doub
                          const int64_t* idxS, int64_t num_node, const int64_t* Ae_jc, const int64_t* Ae_ir,
                          const double* Ae_pr, const double* z_real, const double* z_imag, int want_fp32,
                          vh_geom** out);
+/* same, with the circulant tensor generated on the device (lse_generate_circulant_tensor(dx, 1, L, M, N, 0),
+ * lse_generate_circulant_tensor.m:1; the batched-solver form fN_all2 of VoxHenry_executer.m:141).
+ * st_sparse_precon (out, may be NULL): the 3 complex self terms st_sparse_precon2.              */
+vh_status vh_geom_create_generated(vh_ctx* ctx, int L, int M, int N, double dx, int64_t nv, const int64_t* idxS,
+                                   int64_t num_node, const int64_t* Ae_jc, const int64_t* Ae_ir, const double* Ae_pr,
+                                   const double* z_real, const double* z_imag, int want_fp32, double* st_sparse_precon,
+                                   vh_geom** out);
 void vh_geom_destroy(vh_geom* g);
 /* sizes: n_curr = 5 nv, n_node = rows of Ae, n = n_curr + n_node */
 vh_status vh_geom_sizes(const vh_geom* g, int64_t* n_curr, int64_t* n_node, int64_t* n);
@@ -121,6 +128,35 @@ vh_status vh_precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const
 vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
                    int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
                    double* relres, int* iter, double* resvec, int resvec_len, int* nres);
+/* same with b and x in DEVICE memory (B x n complex); returns after the solve has finished */
+vh_status vh_gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const void* b_dev, const double* scale,
+                          const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
+                          void* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres);
+
+/* ---- instrumentation (no counterpart in the reference, which times with tic/toc) --------------
+ * vh_ctx_stream: the CUDA stream (cudaStream_t) all work of the context is enqueued on.
+ * vh_ctx_profile: enable/disable per-section CUDA-event timing (clears recorded sections).
+ * vh_ctx_profile_read: milliseconds, call counts and work units (RHS) per section since the last read/enable:
+ *   0 FFT convolution complex128, 1 FFT convolution complex64, 2 Ae/Ae^T products of the matvec,
+ *   3 Schur factorisation, 4 preconditioner apply, 5 Krylov vector work, 6 tensor generation.
+ * vh_launch_count: kernels launched by the library since it was loaded.                       */
+void* vh_ctx_stream(vh_ctx* ctx);
+vh_status vh_ctx_profile(vh_ctx* ctx, int enable);
+vh_status vh_ctx_profile_read(vh_ctx* ctx, double* ms, int64_t* calls, int64_t* units, int nsec);
+int64_t vh_launch_count(void);
+
+/* ---- setup: the inputs of the solve path --------------------------------------------------------
+ * [all_panels_ids, num_nodes] = lse_generate_panelIDs(idxS, L, M, N)   (lse_generate_panelIDs.m:1)
+ *   all_panels_ids: nv x 6 column-major, 1-based node ids (-x,+x,-y,+y,-z,+z); no device needed. */
+vh_status vh_panel_ids(int L, int M, int N, int64_t nv, const int64_t* idxS, int64_t* all_panels_ids,
+                       int64_t* num_nodes);
+/* Ae = lse_compute_Ae_matrix(idxS, all_panels_ids, num_nodes) (lse_compute_Ae_matrix.m:1) as CSC:
+ *   jc: 5nv+1, ir (0-based rows) and pr: 16 nv entries each; no device needed.                  */
+vh_status vh_incidence(int64_t nv, const int64_t* all_panels_ids, int64_t* Ae_jc, int64_t* Ae_ir, double* Ae_pr);
+/* [fN_all, st_sparse_precon] = lse_generate_circulant_tensor(dx, 1, L, M, N, 0)
+ *   (lse_generate_circulant_tensor.m:1), computed on the device; fN_all (HOST, may be NULL):
+ *   complex (2L, 2M, 2N, 7) column-major; st_sparse_precon (HOST, may be NULL): 3 complex.       */
+vh_status vh_circulant_tensor(vh_ctx* ctx, int L, int M, int N, double dx, double* fN_all, double* st_sparse_precon);
 
 #ifdef __cplusplus
 }

@@ -11,11 +11,15 @@ Restates:
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
+import scipy.fft as sfft
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 MU0 = 4 * np.pi * 1e-7          # EMconstants.m:13
+WORKERS = os.cpu_count() or 1   # FFTs threaded over the host cores (MATLAB's fftn is multithreaded)
 DIAG_SCALE = np.array([1.0, 1.0, 1.0, 1.0 / 6.0, 1.0 / 2.0])   # lse_matvect_mult.m:99-103
 
 
@@ -27,7 +31,7 @@ def lse_matvect_mult(JIn0, fN_all, Ae, z_real, z_imag, dx, idx):
     JIn = np.zeros(L * M * N * 5, dtype=np.complex128)
     JIn[idx - 1] = JIn0[:num_curr]
     JIn = JIn.reshape(L, M, N, 5, order="F")
-    f = lambda c: np.fft.fftn(JIn[:, :, :, c], s=(LfN, MfN, NfN))
+    f = lambda c: sfft.fftn(JIn[:, :, :, c], s=(LfN, MfN, NfN), workers=WORKERS)
     G = [fN_all[:, :, :, k] for k in range(7)]
     fJ = f(0)
     J1 = G[0] * fJ
@@ -51,7 +55,7 @@ def lse_matvect_mult(JIn0, fN_all, Ae, z_real, z_imag, dx, idx):
     J3 = J3 + G[4] * fJ
     J4 = J4 + G[5] * fJ
     J5 = J5 + G[6] * fJ
-    outs = [np.fft.ifftn(J) for J in (J1, J2, J3, J4, J5)]
+    outs = [sfft.ifftn(J, workers=WORKERS) for J in (J1, J2, J3, J4, J5)]
     zz = z_real if z_imag is None else (z_real + z_imag)
     JOut = np.zeros((L, M, N, 5), dtype=np.complex128, order="F")
     with np.errstate(invalid="ignore"):

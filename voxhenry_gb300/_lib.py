@@ -45,6 +45,17 @@ SIGNATURES = {
                                    _i64p, _dp, _ip, _ip, _i64p]),
     "vh_precon_apply": (C.c_int, [_p, C.c_int, C.POINTER(_p), _dp, _dp]),
     "vh_precon_apply_device": (C.c_int, [_p, C.c_int, C.POINTER(_p), _p, _p]),
+    "vh_geom_create_generated": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64, _i64p, C.c_int64,
+                                           _i64p, _i64p, _dp, _dp, _dp, C.c_int, _dp, C.POINTER(_p)]),
+    "vh_panel_ids": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, _i64p, _i64p, _i64p]),
+    "vh_incidence": (C.c_int, [C.c_int64, _i64p, _i64p, _i64p, _dp]),
+    "vh_circulant_tensor": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp]),
+    "vh_gmres_device": (C.c_int, [_p, C.c_int, C.POINTER(_p), _p, _dp, _ip, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
+                                  _p, _ip, _dp, _ip, _dp, C.c_int, _ip]),
+    "vh_ctx_stream": (C.c_void_p, [_p]),
+    "vh_ctx_profile": (C.c_int, [_p, C.c_int]),
+    "vh_ctx_profile_read": (C.c_int, [_p, _dp, _i64p, _i64p, C.c_int]),
+    "vh_launch_count": (C.c_int64, []),
     "vh_gmres": (C.c_int, [_p, C.c_int, C.POINTER(_p), _dp, _dp, _ip, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp,
                            _ip, _dp, _ip, _dp, C.c_int, _ip]),
 }

@@ -1,4 +1,5 @@
 // C ABI entry points (include/voxhenry_gpu.h): context, geometry and matvec.
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -6,6 +7,12 @@
 #include "vh_internal.cuh"
 
 using namespace vh;
+
+namespace vh {
+static std::atomic<int64_t> g_launches{0};
+int64_t launches_total() { return g_launches.load(std::memory_order_relaxed); }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace vh
 
 namespace {
 
@@ -57,7 +64,10 @@ void set_z_slot(vh_geom* g, int slot, const double* z_real, const double* z_imag
   VH_CUDA_TRY(cudaMemcpyAsync(d_zr, z_real, lmn * sizeof(double), cudaMemcpyHostToDevice, st));
   VH_CUDA_TRY(cudaMemcpyAsync(d_idx, g->idxS.data(), g->nv * sizeof(int64_t), cudaMemcpyHostToDevice, st));
   if (z_imag) VH_CUDA_TRY(cudaMemcpyAsync(d_zi, z_imag, lmn * sizeof(double2), cudaMemcpyHostToDevice, st));
-  if (g->nv) k_gather_z<<<256, 256, 0, st>>>(d_zr, d_zi, d_idx, g->nv, g->zslots[slot]);
+  if (g->nv) {
+    k_gather_z<<<256, 256, 0, st>>>(d_zr, d_zi, d_idx, g->nv, g->zslots[slot]);
+    count_launch();
+  }
   VH_CUDA_TRY(cudaGetLastError());
   VH_CUDA_TRY(cudaStreamSynchronize(st));
   cudaFree(d_zr);
@@ -72,6 +82,7 @@ void ensure_ones(vh_geom* g, int B) {
   g->ones_cap = 0;
   VH_CUDA_TRY(cudaMalloc(&g->ones, B * sizeof(double2)));
   k_fill_c<<<1, 256, 0, g->ctx->stream>>>(g->ones, B, make_double2(1.0, 0.0));
+  count_launch();
   VH_CUDA_TRY(cudaGetLastError());
   g->ones_cap = B;
 }
@@ -117,8 +128,12 @@ void matvec_device(vh_geom* g, int B, const double2* x, double2* y, const double
   }
   int64_t zstride = 0;
   const double2* z = resolve_z(g, B, zslot, zstride);
-  if (g->nv > 0) conv_apply(g->conv, prec, B, x, g->n, y, g->n, scale, z, zstride, st);
+  if (g->nv > 0) {
+    ProfScope ps(&g->ctx->prof, prec == PREC_FP64 ? SEC_CONV64 : SEC_CONV32, st, B);
+    conv_apply(g->conv, prec, B, x, g->n, y, g->n, scale, z, zstride, st);
+  }
   // y_J -= Ae^T phi ; y_phi = Ae J   (lse_matvect_mult.m:138-140)
+  ProfScope ps(&g->ctx->prof, SEC_INCID, st, B);
   spmv_batched(g->AeT, B, x, g->n, g->nc, y, g->n, 0, -1, st);
   spmv_batched(g->Ae, B, x, g->n, 0, y, g->n, g->nc, 0, st);
 }
@@ -127,6 +142,40 @@ void matvec_device(vh_geom* g, int B, const double2* x, double2* y, const double
 extern "C" {
 
 int vh_version(void) { return 100; }
+
+int64_t vh_launch_count(void) { return launches_total(); }
+
+void* vh_ctx_stream(vh_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+vh_status vh_ctx_profile(vh_ctx* ctx, int enable) {
+  if (!ctx) return VH_ERR_BAD_ARG;
+  return guarded(ctx, [&] {
+    VH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->prof.clear();
+    ctx->prof.on = enable != 0;
+  });
+}
+
+vh_status vh_ctx_profile_read(vh_ctx* ctx, double* ms, int64_t* calls, int64_t* units, int nsec) {
+  if (!ctx || nsec < 0) return VH_ERR_BAD_ARG;
+  return guarded(ctx, [&] {
+    VH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < nsec; ++i) {
+      if (ms) ms[i] = 0.0;
+      if (calls) calls[i] = 0;
+      if (units) units[i] = 0;
+    }
+    for (auto& r : ctx->prof.rec) {
+      if (r.sec >= nsec || !r.e1) continue;
+      float t = 0.f;
+      VH_CUDA_TRY(cudaEventElapsedTime(&t, r.e0, r.e1));
+      if (ms) ms[r.sec] += t;
+      if (calls) calls[r.sec] += 1;
+      if (units) units[r.sec] += r.units;
+    }
+    ctx->prof.clear();
+  });
+}
 
 const char* vh_status_string(vh_status s) {
   switch (s) {
@@ -214,6 +263,45 @@ vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const doub
     }
     csc_upload(num_node, g->nc, Ae_jc, Ae_ir, Ae_pr, g->Ae, g->AeT, g->hAe, g->hAeT, st);
     set_z_slot(g, 0, z_real, z_imag);
+  });
+  if (s != VH_OK) {
+    vh_geom_destroy(g);
+    return s;
+  }
+  *out = g;
+  return VH_OK;
+}
+
+vh_status vh_geom_create_generated(vh_ctx* ctx, int L, int M, int N, double dx, int64_t nv, const int64_t* idxS,
+                                   int64_t num_node, const int64_t* Ae_jc, const int64_t* Ae_ir, const double* Ae_pr,
+                                   const double* z_real, const double* z_imag, int want_fp32, double* st_sparse_precon,
+                                   vh_geom** out) {
+  if (!ctx || !out) return VH_ERR_BAD_ARG;
+  *out = nullptr;
+  vh_geom* g = nullptr;
+  vh_status s = vh_geom_create(ctx, L, M, N, dx, nullptr, nv, idxS, num_node, Ae_jc, Ae_ir, Ae_pr, z_real, z_imag,
+                               want_fp32, &g);
+  if (s != VH_OK) return s;
+  s = guarded(ctx, [&] {
+    cudaStream_t st = ctx->stream;
+    const int64_t P = 8LL * L * M * N;
+    double2* fn = nullptr;
+    VH_CUDA_TRY(cudaMalloc(&fn, 7 * P * sizeof(double2)));
+    try {
+      double2 s3[3];
+      circulant_tensor_device(L, M, N, dx, fn, s3, st);
+      conv_plan_create(g->conv, L, M, N, dx, fn, nv, g->idxS.data(), want_fp32 != 0, st);
+      g->has_conv = true;
+      if (st_sparse_precon)
+        for (int i = 0; i < 3; ++i) {
+          st_sparse_precon[2 * i] = s3[i].x;
+          st_sparse_precon[2 * i + 1] = s3[i].y;
+        }
+    } catch (...) {
+      cudaFree(fn);
+      throw;
+    }
+    cudaFree(fn);
   });
   if (s != VH_OK) {
     vh_geom_destroy(g);

@@ -177,6 +177,7 @@ void chol_factor(const CholSymbolic& s, const double* D, double* W, cudaStream_t
   VH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
   VH_CUDA_TRY(cudaMemsetAsync(W, 0, s.w_total * sizeof(double), st));
   k_chol_assemble<<<s.nfronts, 256, 0, st>>>(s.d_fronts, s.d_asm, s.d_asm_q, s.d_asm_c, D, W);
+  count_launch();
   VH_CUDA_TRY(cudaGetLastError());
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const unsigned nf = (unsigned)s.levels[h].size();
@@ -185,6 +186,7 @@ void chol_factor(const CholSymbolic& s, const double* D, double* W, cudaStream_t
       const unsigned cy = (unsigned)std::min(1024, std::max(1, s.level_max_nf[h]));
       for (int which = 0; which < 2; ++which) {
         k_chol_extend_add<<<dim3(nf, cy), 128, 0, st>>>(lev, s.d_fronts, s.d_relmap, W, which);
+        count_launch();
         VH_CUDA_TRY(cudaGetLastError());
       }
     }
@@ -192,12 +194,15 @@ void chol_factor(const CholSymbolic& s, const double* D, double* W, cudaStream_t
     const int max_nf = s.level_max_nf[h];
     for (int k0 = 0; k0 < max_ns; k0 += kNB) {
       k_chol_diag<<<nf, 256, 0, st>>>(lev, s.d_fronts, W, k0, d_err);
+      count_launch();
       const int rows = max_nf - k0;
       if (rows > 0) {
         k_chol_panel<<<dim3(nf, (unsigned)ceil_div(rows, 128)), 128, 0, st>>>(lev, s.d_fronts, W, k0);
+        count_launch();
         const int m = max_nf - k0;
         const int T = (int)ceil_div(m, kTS);
         k_chol_update<<<dim3(nf, (unsigned)(T * (T + 1) / 2)), 256, 0, st>>>(lev, s.d_fronts, W, k0);
+        count_launch();
       }
       VH_CUDA_TRY(cudaGetLastError());
     }
@@ -316,12 +321,14 @@ void chol_solve(const CholSymbolic& s, int B, double* const* Wp, double2* x, int
     const size_t smh = (size_t)s.level_max_nf[h] * sizeof(double2);
     k_chol_fsolve<<<dim3((unsigned)s.levels[h].size(), B), 256, smh, st>>>(s.d_levels[h], s.d_fronts, s.d_rows,
                                                                             s.d_relmap, Wp, x, ldx, xoff, U, s.u_total);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   for (size_t hh = s.levels.size(); hh-- > 0;) {
     const size_t smh = (size_t)s.level_max_nf[hh] * sizeof(double2);
     k_chol_bsolve<<<dim3((unsigned)s.levels[hh].size(), B), 256, smh, st>>>(s.d_levels[hh], s.d_fronts, s.d_rows, Wp,
                                                                              x, ldx, xoff);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
 }

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <utility>
+#include <vector>
 
 namespace vh {
 
@@ -86,5 +88,82 @@ struct Error {
   } while (0)
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------- instrumentation
+// Kernels launched by this library (every launch site calls count_launch()).
+int64_t launches_total();
+void count_launch();
+
+// Named sections timed with CUDA events on the launching stream (enabled per context).
+enum Section {
+  SEC_CONV64 = 0,    // FFT convolution, complex128 (the five passes)
+  SEC_CONV32 = 1,    // FFT convolution, complex64
+  SEC_INCID = 2,     // Ae / Ae^T products of the matvec
+  SEC_FACTOR = 3,    // Schur-complement factorisation
+  SEC_PRECON = 4,    // preconditioner apply (incl. triangular solves)
+  SEC_KRYLOV = 5,    // Gram-Schmidt, norms, combinations
+  SEC_TENSOR = 6,    // circulant tensor generation
+  SEC_COUNT = 7
+};
+
+struct ProfRecord {
+  int sec;
+  int64_t units;     // work units of the section (right-hand sides for the matvec)
+  cudaEvent_t e0, e1;
+};
+
+struct Profiler {
+  bool on = false;
+  std::vector<ProfRecord> rec;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  // returns the record index, or -1 when off
+  int begin(int sec, int64_t units, cudaStream_t st) {
+    if (!on) return -1;
+    cudaEvent_t e0 = get();
+    cudaEventRecord(e0, st);
+    rec.push_back({sec, units, e0, nullptr});
+    return (int)rec.size() - 1;
+  }
+  void end(int idx, cudaStream_t st) {
+    if (idx < 0 || idx >= (int)rec.size()) return;
+    cudaEvent_t e1 = get();
+    cudaEventRecord(e1, st);
+    rec[idx].e1 = e1;
+  }
+  void clear() {
+    for (auto& r : rec) {
+      pool.push_back(r.e0);
+      if (r.e1) pool.push_back(r.e1);
+    }
+    rec.clear();
+  }
+  ~Profiler() {
+    clear();
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+// Scoped section: records begin/end events on `st` when the profiler is on.
+struct ProfScope {
+  Profiler* p;
+  cudaStream_t st;
+  int idx = -1;
+  ProfScope(Profiler* prof, int sec, cudaStream_t s, int64_t units = 0) : p(prof), st(s) {
+    if (p) idx = p->begin(sec, units, st);
+  }
+  ~ProfScope() {
+    if (p) p->end(idx, st);
+  }
+};
 
 }  // namespace vh

@@ -300,10 +300,12 @@ void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2
   const double s = 1.0 / (double)P;
   VH_CUDA_TRY(cudaMalloc(&p.tens64, 7 * P * sizeof(double2)));
   k_tensor_permute<double2><<<1024, 256, 0, st>>>(fN_all_dev, p.tens64, p.X, p.Y, p.Z, s);
+  count_launch();
   VH_CUDA_TRY(cudaGetLastError());
   if (want32) {
     VH_CUDA_TRY(cudaMalloc(&p.tens32, 7 * P * sizeof(float2)));
     k_tensor_permute<float2><<<1024, 256, 0, st>>>(fN_all_dev, p.tens32, p.X, p.Y, p.Z, s);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   VH_CUDA_TRY(cudaStreamSynchronize(st));
@@ -358,6 +360,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const unsigned grid = (unsigned)ceil_div(lines, nl);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_fwd_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_fwd_x<T><<<grid, 256, sm, st>>>(x, ldx, p.vmap, L, M, N, p.nv, lines, A, p.fx, twp[0], nl);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 2
@@ -367,6 +370,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * N * B));
     VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_pass_y<T, -1><<<grid, 256, sm, st>>>(A, M, M, Bf, Y, Y, X, p.fy, twp[1], tx);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 3
@@ -376,6 +380,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)Y);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_zpass<T><<<grid, Z * tx, sm, st>>>(Bf, tens, N, Y, X, B, p.fz, twp[2], tx);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 4
@@ -385,6 +390,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * N * B));
     VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_pass_y<T, +1><<<grid, 256, sm, st>>>(Bf, Y, Y, A, M, M, X, p.fy, twp[1], tx);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 5
@@ -396,7 +402,94 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     VH_CUDA_TRY(cudaFuncSetAttribute(k_inv_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_inv_x<T><<<grid, 256, sm, st>>>(A, p.vmap, L, M, N, p.nv, lines, x, ldx, y, ldy, scale, zdiag, zstride,
                                       1.0 / p.dx, p.fx, twp[0], nl);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
+  }
+}
+
+// ---------------------------------------------------------------------------- plain 3-D FFT
+// Forward FFT along one axis of a column-major array, in place.  Element (i, col) of plane p
+// sits at data[p * n * inner + i * inner + col]; a CTA takes `tx` consecutive columns.
+__global__ void k_fft_axis_inplace(double2* data, int64_t inner, FftDesc fd, const double2* __restrict__ twg, int tx,
+                                   bool contiguous) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = fd.n;
+  double2* tw = reinterpret_cast<double2*>(smem_raw);
+  double2* b0 = tw + n;
+  double2* b1 = b0 + n * tx;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = twg[i];
+  const int64_t plane = blockIdx.y;
+  const int64_t c0 = (int64_t)blockIdx.x * tx;
+  double2* base = data + plane * n * inner;
+  if (contiguous) {   // lines are contiguous (inner == 1 axis is x): column = line index
+    for (int t = threadIdx.x; t < n * tx; t += blockDim.x) {
+      const int line = t / n, i = t % n;
+      const int64_t col = c0 + line;
+      b0[line * n + i] = (col < inner) ? base[col * n + i] : make_double2(0.0, 0.0);
+    }
+  } else {
+    for (int t = threadIdx.x; t < n * tx; t += blockDim.x) {
+      const int line = t % tx, i = t / tx;
+      const int64_t col = c0 + line;
+      b0[i * tx + line] = (col < inner) ? base[(int64_t)i * inner + col] : make_double2(0.0, 0.0);
+    }
+  }
+  __syncthreads();
+  double2* r = contiguous ? fft_lines<-1>(b0, b1, tw, fd, 1, n, tx, true) : fft_lines<-1>(b0, b1, tw, fd, tx, 1, tx, false);
+  if (contiguous) {
+    for (int t = threadIdx.x; t < n * tx; t += blockDim.x) {
+      const int line = t / n, i = t % n;
+      const int64_t col = c0 + line;
+      if (col < inner) base[col * n + i] = r[line * n + i];
+    }
+  } else {
+    for (int t = threadIdx.x; t < n * tx; t += blockDim.x) {
+      const int line = t % tx, i = t / tx;
+      const int64_t col = c0 + line;
+      if (col < inner) base[(int64_t)i * inner + col] = r[i * tx + line];
+    }
+  }
+}
+
+void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaStream_t st) {
+  const int dims[3] = {X, Y, Z};
+  for (int a = 0; a < 3; ++a) {
+    FftDesc fd;
+    VH_REQUIRE(fft_factor(dims[a], fd), ERR_UNSUPPORTED, "tensor grid dimensions must factor into 2, 3, 5 and 7");
+    VH_REQUIRE(dims[a] <= 4096, ERR_UNSUPPORTED, "tensor grid dimension too large");
+  }
+  for (int a = 0; a < 3; ++a) {
+    const int n = dims[a];
+    FftDesc fd;
+    fft_factor(n, fd);
+    auto t = twiddles(n);
+    double2* tw = nullptr;
+    VH_CUDA_TRY(cudaMalloc(&tw, n * sizeof(double2)));
+    VH_CUDA_TRY(cudaMemcpyAsync(tw, t.data(), n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    int64_t inner, planes;
+    bool contiguous = (a == 0);
+    int tx;
+    if (a == 0) {            // lines along x: "inner" counts the lines of one plane set
+      inner = (int64_t)Y * Z * batch;
+      planes = 1;
+      tx = std::max(1, std::min(16, 2048 / n));
+    } else if (a == 1) {
+      inner = X;
+      planes = (int64_t)Z * batch;
+      tx = std::max(1, std::min(16, 4096 / n));
+    } else {
+      inner = (int64_t)X * Y;
+      planes = batch;
+      tx = std::max(1, std::min(16, 4096 / n));
+    }
+    const size_t sm = (size_t)(n + 2 * n * tx) * sizeof(double2);
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_fft_axis_inplace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    dim3 grid((unsigned)ceil_div(inner, tx), (unsigned)planes);
+    k_fft_axis_inplace<<<grid, 256, sm, st>>>(data, inner, fd, tw, tx, contiguous);
+    count_launch();
+    VH_CUDA_TRY(cudaGetLastError());
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(tw);
   }
 }
 

@@ -49,4 +49,11 @@ void conv_plan_reserve(ConvPlan& p, int B, Prec prec);
 void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
                 const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st);
 
+// In-place forward 3-D FFT of `batch` column-major X x Y x Z complex arrays (device).
+void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaStream_t st);
+
+// Circulant tensor spectrum fN_all (column-major (2L, 2M, 2N, 7), device, caller-allocated) and
+// the three self terms st (host) of lse_generate_circulant_tensor(dx, 1, L, M, N, 0).
+void circulant_tensor_device(int L, int M, int N, double dx, double2* fN_dev, double2 st_out[3], cudaStream_t st);
+
 }  // namespace vh

@@ -239,7 +239,9 @@ std::vector<double> row_norms(const double2* x, int64_t ldx, const std::vector<i
   part.ensure((size_t)na * nch);
   out.ensure(na);
   k_norm2_partial<<<dim3(nch, na), kChunkThreads, 0, st>>>(x, ldx, d_rows.p, n, part.p);
+  count_launch();
   k_reduce_norm<<<na, 32, 0, st>>>(part.p, nch, out.p);
+  count_launch();
   VH_CUDA_TRY(cudaGetLastError());
   VH_CUDA_TRY(cudaMemcpyAsync(res.data(), out.p, na * sizeof(double), cudaMemcpyDeviceToHost, st));
   VH_CUDA_TRY(cudaStreamSynchronize(st));
@@ -331,6 +333,7 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
   if (any_x0) {
     apply_A(all, x, Wc.p, PREC_FP64);
     k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
+    count_launch();
   } else {
     VH_CUDA_TRY(cudaMemcpyAsync(R.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
   }
@@ -371,7 +374,9 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
     std::vector<double> r0 = row_norms(R.p, n, active, n, d_rows, partr, nrm, st);
     VH_CUDA_TRY(cudaMemcpyAsync(nrm.p, r0.data(), na * sizeof(double), cudaMemcpyHostToDevice, st));
     k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(R.p, n, Xc.p, n, d_act.p, n);
+    count_launch();
     k_scale_into<<<dim3(grid1(n), na), 256, 0, st>>>(Xc.p, n, V.p, ldb, d_act.p, nrm.p, n);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     for (int a = 0; a < na; ++a) gv[active[a]][0] = cd(r0[a], 0.0);
     std::vector<int> kdone(na, 0);           // iterations performed in this cycle
@@ -383,6 +388,7 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
       upload_act(run);
       // w = M^-1 A v_k  (left)   or   z_k = M^-1 v_k, w = A z_k  (flexible)
       k_gather<<<dim3(grid1(n), nr), 256, 0, st>>>(V.p + (int64_t)k * n, ldb, Xc.p, n, d_act.p, n);
+      count_launch();
       if (flexible) {
         apply_M(run, Xc.p, Zc.p);
         upload_act(run);
@@ -397,12 +403,18 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
       upload_act(run);
       double2* w = (flexible || !pcs) ? Wc.p : Zc.p;
       // classical Gram-Schmidt: h = V^H w ; w -= V h ; h_{k+1} = |w| (pgmres_iter.m:107-110)
+      ProfScope ps(&g->ctx->prof, SEC_KRYLOV, st, nr);
       k_multidot<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, k + 1, n, partc.p);
+      count_launch();
       k_reduce_partials<<<nr, 128, 0, st>>>(partc.p, nch, k + 1, hbuf.p, m + 2);
+      count_launch();
       k_cgs_update<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, hbuf.p, m + 2, k + 1, n,
                                                             partr.p);
+      count_launch();
       k_reduce_norm<<<nr, 32, 0, st>>>(partr.p, nch, nrm.p);
+      count_launch();
       k_scale_into<<<dim3(grid1(n), nr), 256, 0, st>>>(w, n, V.p + (int64_t)(k + 1) * n, ldb, d_act.p, nrm.p, n);
+      count_launch();
       VH_CUDA_TRY(cudaGetLastError());
       std::vector<double2> hh((size_t)nr * (m + 2));
       std::vector<double> hn(nr);
@@ -479,11 +491,13 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
       k_combine<<<dim3(grid1(n), na), 256, 0, st>>>(Zs.p, n, (int64_t)m * n, d_act.p, coef.p, m + 2, d_cnt.p, x, n, n, 1);
     else
       k_combine<<<dim3(grid1(n), na), 256, 0, st>>>(V.p, ldv, ldb, d_act.p, coef.p, m + 2, d_cnt.p, x, n, n, 1);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     VH_CUDA_TRY(cudaStreamSynchronize(st));
     VH_CUDA_TRY(cudaMemcpyAsync(coef.p, cr.data(), cr.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
     VH_CUDA_TRY(cudaMemcpyAsync(d_cnt.p, cntr.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
     k_combine<<<dim3(grid1(n), na), 256, 0, st>>>(V.p, ldv, ldb, d_act.p, coef.p, m + 2, d_cnt.p, R.p, n, n, 0);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     VH_CUDA_TRY(cudaStreamSynchronize(st));
     // outer loop condition of pgmres.m:153: resvec(it) > tol && outit < maxit
@@ -496,6 +510,7 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
   upload_act(all);
   apply_A(all, x, Wc.p, PREC_FP64);
   k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
+  count_launch();
   VH_CUDA_TRY(cudaGetLastError());
   const std::vector<double> rr = row_norms(R.p, n, all, n, d_rows, partr, nrm, st);
   const std::vector<double> bb = row_norms(b, n, all, n, d_rows, partr, nrm, st);
@@ -569,6 +584,7 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
     d_act.ensure(na);
     VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, active.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
     k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(R.p, n, Rc.p, n, d_act.p, n);
+    count_launch();
     VH_CUDA_TRY(cudaMemsetAsync(D.p, 0, (size_t)na * n * sizeof(double2), st));
     std::vector<double2> sc(na);
     std::vector<int> zs(na);
@@ -589,6 +605,7 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
     out.precons += inner.precons;
     VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, active.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
     k_axpy_rows<<<dim3(grid1(n), na), 256, 0, st>>>(x, D.p, n, d_act.p, n);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     for (int a = 0; a < na; ++a) {
       const int bb = active[a];
@@ -605,9 +622,12 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       Ba.ensure((size_t)na * n);
       Sa.ensure((size_t)na * n);
       k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(x, n, Xa.p, n, d_act.p, n);
+      count_launch();
       k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(b, n, Ba.p, n, d_act.p, n);
+      count_launch();
       A64(active, Xa.p, Ya.p);
       k_sub<<<grid1((int64_t)na * n), 256, 0, st>>>(Ba.p, Ya.p, Ya.p, (int64_t)na * n);
+      count_launch();
       std::vector<int> seq(na);
       for (int a = 0; a < na; ++a) seq[a] = a;
       M(active, Ya.p, Sa.p);
@@ -629,6 +649,7 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
   // true relative residual
   A64(all, x, Wc.p);
   k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
+  count_launch();
   const std::vector<double> rr = row_norms(R.p, n, all, n, d_rows, partr, nrm, st);
   const std::vector<double> bb = row_norms(b, n, all, n, d_rows, partr, nrm, st);
   for (int i = 0; i < B; ++i) {
@@ -655,7 +676,47 @@ vh_status guarded_g(vh_ctx* ctx, F&& f) {
 }
 }  // namespace
 
+namespace {
+void gmres_dispatch(vh_geom* g, int B, vh_precon* const* pcs, const double2* b_dev, const double* scale,
+                    const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
+                    double2* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+  VH_REQUIRE(B >= 1 && b_dev && x_dev && tol, ERR_BAD_ARG, "bad gmres arguments");
+  VH_REQUIRE(!(flexible && prec == VH_PREC_FP32), ERR_UNSUPPORTED, "mixed precision uses the left-preconditioned form");
+  cudaStream_t st = g->ctx->stream;
+  VH_CUDA_TRY(cudaMemsetAsync(x_dev, 0, (size_t)B * g->n * sizeof(double2), st));
+  GmresOut o;
+  std::vector<int> steps;
+  if (prec == VH_PREC_FP32)
+    solve_mixed_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, 1e-4, 20, x_dev, o, steps);
+  else
+    gmres_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, flexible != 0, PREC_FP64, x_dev, o);
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int i = 0; i < B; ++i) {
+    if (flag) flag[i] = o.flag[i];
+    if (relres) relres[i] = o.relres[i];
+    if (iter) {
+      iter[2 * i] = o.inner[i];
+      iter[2 * i + 1] = o.outer[i];
+    }
+    if (nres) nres[i] = (int)o.resvec[i].size();
+    if (resvec)
+      for (int k = 0; k < resvec_len && k < (int)o.resvec[i].size(); ++k) resvec[(size_t)i * resvec_len + k] = o.resvec[i][k];
+  }
+}
+}  // namespace
+
 extern "C" {
+
+vh_status vh_gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const void* b_dev, const double* scale,
+                          const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
+                          void* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded_g(g->ctx, [&] {
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    gmres_dispatch(g, B, pcs, (const double2*)b_dev, scale, zslot, restart, tol, maxit, flexible, prec,
+                   (double2*)x_dev, flag, relres, iter, resvec, resvec_len, nres);
+  });
+}
 
 vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
                    int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
@@ -663,7 +724,6 @@ vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, co
   if (!g) return VH_ERR_BAD_ARG;
   return guarded_g(g->ctx, [&] {
     VH_REQUIRE(B >= 1 && b && x && tol, ERR_BAD_ARG, "bad gmres arguments");
-    VH_REQUIRE(!(flexible && prec == VH_PREC_FP32), ERR_UNSUPPORTED, "mixed precision uses the left-preconditioned form");
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     cudaStream_t st = g->ctx->stream;
     const int64_t n = g->n;
@@ -671,26 +731,10 @@ vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, co
     db.ensure((size_t)B * n);
     dx.ensure((size_t)B * n);
     VH_CUDA_TRY(cudaMemcpyAsync(db.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyHostToDevice, st));
-    VH_CUDA_TRY(cudaMemsetAsync(dx.p, 0, (size_t)B * n * sizeof(double2), st));
-    GmresOut o;
-    std::vector<int> steps;
-    if (prec == VH_PREC_FP32)
-      solve_mixed_device(g, B, pcs, db.p, (const double2*)scale, zslot, tol, restart, maxit, 1e-4, 20, dx.p, o, steps);
-    else
-      gmres_device(g, B, pcs, db.p, (const double2*)scale, zslot, tol, restart, maxit, flexible != 0, PREC_FP64, dx.p, o);
+    gmres_dispatch(g, B, pcs, db.p, scale, zslot, restart, tol, maxit, flexible, prec, dx.p, flag, relres, iter,
+                   resvec, resvec_len, nres);
     VH_CUDA_TRY(cudaMemcpyAsync(x, dx.p, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VH_CUDA_TRY(cudaStreamSynchronize(st));
-    for (int i = 0; i < B; ++i) {
-      if (flag) flag[i] = o.flag[i];
-      if (relres) relres[i] = o.relres[i];
-      if (iter) {
-        iter[2 * i] = o.inner[i];
-        iter[2 * i + 1] = o.outer[i];
-      }
-      if (nres) nres[i] = (int)o.resvec[i].size();
-      if (resvec)
-        for (int k = 0; k < resvec_len && k < (int)o.resvec[i].size(); ++k) resvec[(size_t)i * resvec_len + k] = o.resvec[i][k];
-    }
   });
 }
 

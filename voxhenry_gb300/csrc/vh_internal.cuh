@@ -13,6 +13,7 @@ struct vh_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string last_error;
+  vh::Profiler prof;
 };
 
 namespace vh {

@@ -98,6 +98,7 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
     return;
   }
   VH_REQUIRE(x != y, ERR_BAD_ARG, "preconditioner apply cannot run in place");
+  ProfScope ps(&g->ctx->prof, SEC_PRECON, st, B);
   if (B > g->pc_ptrs_cap) {
     cudaFree(g->pc_ptrs);
     g->pc_ptrs = nullptr;
@@ -124,12 +125,14 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
   if (g->nphi > 0) {
     k_precon_rhs<<<dim3((unsigned)ceil_div(g->nphi, 256), B), 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val,
                                                                            d_ainv, x, y, g->n, g->nc);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     chol_solve(g->chol, B, d_w, y, g->n, g->nc, g->pc_tmp, st);
   }
   if (g->nc > 0) {
     k_precon_finish<<<dim3((unsigned)ceil_div(g->nc, 256), B), 256, 0, st>>>(g->nc, g->AeT.rowptr, g->AeT.col,
                                                                             g->AeT.val, d_ainv, x, y, g->n);
+    count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   // keep the host pointer table alive until the copy has been consumed
@@ -177,10 +180,14 @@ vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_spa
     const double2 s1 = make_double2(st_sparse_precon[0], st_sparse_precon[1]);
     const double2 s2 = make_double2(st_sparse_precon[2], st_sparse_precon[3]);
     const double2 s3 = make_double2(st_sparse_precon[4], st_sparse_precon[5]);
-    if (g->nv) k_a_inv<<<256, 256, 0, st>>>(g->zslots[zslot], g->nv, g->dx, s1, s2, s3, p->A_inv);
+    if (g->nv) {
+      k_a_inv<<<256, 256, 0, st>>>(g->zslots[zslot], g->nv, g->dx, s1, s2, s3, p->A_inv);
+      count_launch();
+    }
     VH_CUDA_TRY(cudaGetLastError());
     ensure_symbolic(g);
     VH_CUDA_TRY(cudaMalloc(&p->W, std::max<int64_t>(1, g->chol.w_total) * sizeof(double)));
+    ProfScope ps(&g->ctx->prof, SEC_FACTOR, st);
     chol_factor(g->chol, p->A_inv, p->W, st);
   });
   if (s != VH_OK) {

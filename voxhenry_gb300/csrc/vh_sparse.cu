@@ -40,6 +40,7 @@ void spmv_batched(const Csr& A, int B, const double2* x, int64_t ldx, int64_t xo
   if (A.nrows == 0 || B == 0) return;
   dim3 grid((unsigned)ceil_div(A.nrows, 256), (unsigned)B);
   k_spmv<<<grid, 256, 0, st>>>(A.nrows, A.rowptr, A.col, A.val, x, ldx, xoff, y, ldy, yoff, mode);
+  count_launch();
   VH_CUDA_TRY(cudaGetLastError());
 }
 

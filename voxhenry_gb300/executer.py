@@ -67,7 +67,11 @@ class Sweep:
         self.freqs = np.asarray(freqs, dtype=np.float64)
         t0 = time.perf_counter()
         z0, zi0 = z_arrays(prob.sigma_e, prob.lambdaL, 2 * np.pi * self.freqs[0])
-        self.geom = vie.Geometry(prob.fN_all2, prob.Ar, z0, zi0, prob.dx, prob.idxS, want_fp32=want_fp32)
+        if prob.fN_all2 is None:     # tensor generated on the device (lse_generate_circulant_tensor)
+            self.geom, prob.st2 = vie.Geometry.generated(prob.L, prob.M, prob.N, prob.dx, prob.Ar, z0, zi0, prob.idxS,
+                                                         want_fp32=want_fp32)
+        else:
+            self.geom = vie.Geometry(prob.fN_all2, prob.Ar, z0, zi0, prob.dx, prob.idxS, want_fp32=want_fp32)
         self.super = prob.lambdaL is not None
         self.zslot = np.zeros(len(self.freqs), dtype=np.int32)
         if self.super:                                   # omega-dependent z: one slot per frequency

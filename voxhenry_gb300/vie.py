@@ -90,6 +90,34 @@ class Geometry:
         _lib.check(lib.vh_geom_sizes(h, C.byref(nc), C.byref(nn), C.byref(n)), self.ctx.handle)
         self.n_curr, self.n_node, self.n = nc.value, nn.value, n.value
 
+    @classmethod
+    def generated(cls, L, M, N, dx, Ae, z_real, z_imag, idxS, want_fp32=False, ctx: Context | None = None):
+        """Geometry whose circulant tensor fN_all2 is generated on the device.  Returns (geom, st2)."""
+        g = cls.__new__(cls)
+        g.ctx = ctx or default_context()
+        lib = g.ctx._lib
+        g.L, g.M, g.N, g.dx = int(L), int(M), int(N), float(dx)
+        idx = np.ascontiguousarray(np.asarray(idxS, dtype=np.int64).ravel())
+        A = sp.csc_matrix(Ae)
+        A.sort_indices()
+        jc = np.ascontiguousarray(A.indptr, dtype=np.int64)
+        ir = np.ascontiguousarray(A.indices, dtype=np.int64)
+        pr = np.ascontiguousarray(A.data, dtype=np.float64)
+        zr = _fortran_flat(z_real, np.float64)
+        zi = None if z_imag is None or np.size(z_imag) == 0 else _fortran_flat(z_imag, np.complex128)
+        st2 = np.zeros(3, dtype=np.complex128)
+        h = C.c_void_p()
+        _lib.check(lib.vh_geom_create_generated(g.ctx.handle, g.L, g.M, g.N, g.dx, idx.size, _lib.i64ptr(idx),
+                                                A.shape[0], _lib.i64ptr(jc), _lib.i64ptr(ir), _lib.dptr(pr),
+                                                _lib.dptr(zr), _lib.cview(zi) if zi is not None else None,
+                                                int(bool(want_fp32)), _lib.cview(st2), C.byref(h)), g.ctx.handle)
+        g.handle = h
+        g._z0_real, g._z0_imag = z_real, (None if zi is None else z_imag)
+        nc, nn, n = C.c_int64(), C.c_int64(), C.c_int64()
+        _lib.check(lib.vh_geom_sizes(h, C.byref(nc), C.byref(nn), C.byref(n)), g.ctx.handle)
+        g.n_curr, g.n_node, g.n = nc.value, nn.value, n.value
+        return g, st2
+
     def set_z(self, slot, z_real, z_imag=None):
         zr = _fortran_flat(z_real, np.float64)
         zi = None if z_imag is None else _fortran_flat(z_imag, np.complex128)
