@@ -34,7 +34,10 @@ import numpy as np  # noqa: E402
 
 METRIC = "freq-points/s, mixed-prec batched vs plain FP64 on GB300 @1e-6 R,L; p50/p99 lat"
 UNIT = "freq-points/s"
-TOL = 1e-8
+# GMRES tolerance: the loosest that keeps R and L within 1e-6 of the converged solution for both the
+# FP64 and the mixed path on this workload (tol 1e-8 leaves 3.8e-6 (FP64) / 5.1e-6 (mixed) in R, L;
+# tol 1e-9 leaves 4.0e-7 / 7.6e-7, measured against a tol-1e-12 FP64 solve)
+TOL = 1e-9
 RESTART = 50
 MAXIT = 10
 
@@ -170,12 +173,15 @@ def run_ours(args, rank, world):
     iters = np.zeros(2 * B, dtype=np.int32)
     nres = np.zeros(B, dtype=np.int32)
 
-    def device_step(prec):
+    st_all = (1j * 2 * np.pi * freqs * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
+
+    def device_step(prec, tol=None, maxit=MAXIT):
         """One sweep with device-resident inputs: factors + batched solve + R, L."""
-        pcs = [g.precon(1j * 2 * np.pi * f * executer.MU0 * prob.st2, zslot=int(sw.zslot[i])) for i, f in enumerate(freqs)]
+        pcs = g.precons(st_all, sw.zslot)
         parr = (C.c_void_p * B)(*[pcs[k // prob.num_ports].handle for k in range(B)])
+        tv = tolv if tol is None else np.full(B, tol)
         st = lib.vh_gmres_device(g.handle, B, parr, C.c_void_p(b_dev.data_ptr()), _lib.cview(scale),
-                                 zsl.ctypes.data_as(ip), RESTART, _lib.dptr(tolv), MAXIT, 0, _lib.PREC[prec],
+                                 zsl.ctypes.data_as(ip), RESTART, _lib.dptr(tv), maxit, 0, _lib.PREC[prec],
                                  C.c_void_p(x_dev.data_ptr()), flag.ctypes.data_as(ip), _lib.dptr(relres),
                                  iters.ctypes.data_as(ip), None, 0, nres.ctypes.data_as(ip))
         _lib.check(st, g.ctx.handle)
@@ -226,6 +232,9 @@ def run_ours(args, rank, world):
             t = float(tt.item())
         return t, out, launches, prof
 
+    # accuracy reference: the FP64 GPU path converged to 1e-12 (untimed); the FP64 GPU path matches
+    # the oracle to 1e-9 in the parity tests
+    R_t, L_t, _ = device_step("fp64", tol=1e-12, maxit=40)
     clocks = ClockSampler(0)
     # warm-up + timed, mixed precision (headline) with live section timing
     clocks.start()
@@ -246,9 +255,13 @@ def run_ours(args, rank, world):
 
     R_m, L_m, nres_m = out_mixed
     R_d, L_d, nres_d = out_fp64
-    err_R = float(np.max(np.abs(R_m - R_d) / np.abs(R_d)))
-    err_L = float(np.max(np.abs(L_m - L_d) / np.abs(L_d)))
-    err_e2e = float(max(np.max(np.abs(e2e_out["R"] - R_d) / np.abs(R_d)), np.max(np.abs(e2e_out["L"] - L_d) / np.abs(L_d))))
+
+    def rl_err(R, L):
+        return float(np.max(np.abs(R - R_t) / np.abs(R_t))), float(np.max(np.abs(L - L_t) / np.abs(L_t)))
+
+    err_R, err_L = rl_err(R_m, L_m)
+    err_R64, err_L64 = rl_err(R_d, L_d)
+    err_e2e = max(rl_err(e2e_out["R"], e2e_out["L"]))
     pts = args.steps * F * world
     value = pts / t_mixed
     # roofline of the FFT matvec (complex64), the dominant kernel group of the mixed path
@@ -282,8 +295,10 @@ def run_ours(args, rank, world):
         "fp64": {"value": round(pts / t_fp64, 4), "ms_per_step": round(1e3 * t_fp64 / args.steps, 3),
                  "dtype": "f64 (complex128 FFT matvec)"},
         "mixed_over_fp64": round(t_fp64 / t_mixed, 3),
-        "accuracy": {"max_rel_err_R_mixed_vs_fp64": err_R, "max_rel_err_L_mixed_vs_fp64": err_L,
-                     "max_rel_err_RL_e2e_vs_fp64": err_e2e, "bar": 1e-6,
+        "accuracy": {"reference": "FP64 GPU path converged to GMRES tol 1e-12 (matches the oracle to 1e-9 in tests)",
+                     "max_rel_err_R_mixed": err_R, "max_rel_err_L_mixed": err_L,
+                     "max_rel_err_R_fp64": err_R64, "max_rel_err_L_fp64": err_L64,
+                     "max_rel_err_RL_e2e": err_e2e, "bar": 1e-6,
                      "gmres_iterations_mixed_total": int(nres_m.sum()), "gmres_iterations_fp64_total": int(nres_d.sum())},
         "e2e": {"value": round(args.steps * F * world / t_e2e, 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(b_host.nbytes + scale.nbytes + 16 * B),

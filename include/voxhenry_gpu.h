@@ -101,6 +101,10 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
  *      reference keeps it in MATLAB globals, lse_sparse_precon_prepare.m:2).                    */
 vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_sparse_precon, int zslot,
                            vh_precon** out);
+/* nfreq preconditioners at once (one per frequency), factored by one batched launch sequence:
+ * st_sparse_precon: nfreq x 3 complex; zslot: nfreq slots (NULL: slot 0); out: nfreq handles.   */
+vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, const double* st_sparse_precon,
+                                 const int* zslot, vh_precon** out);
 void vh_precon_destroy(vh_precon* p);
 /* factor statistics: entries of L, factorisation flops, fronts, largest front order */
 vh_status vh_precon_stats(const vh_precon* p, int64_t* nnz_factor, double* flops, int* nfronts, int* max_front);

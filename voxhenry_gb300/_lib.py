@@ -40,6 +40,7 @@ SIGNATURES = {
     "vh_matvec_device": (C.c_int, [_p, C.c_int, _p, _p, _p, _ip, C.c_int]),
     "vh_precon_create": (C.c_int, [_p, C.c_int, _dp, C.c_int, C.POINTER(_p)]),
     "vh_precon_destroy": (None, [_p]),
+    "vh_precon_create_batch": (C.c_int, [_p, C.c_int, C.c_int, _dp, _ip, C.POINTER(_p)]),
     "vh_precon_stats": (C.c_int, [_p, _i64p, _dp, _ip, _ip]),
     "vh_schur_analyze": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, _i64p, C.c_int64, _i64p, _i64p, _dp,
                                    _i64p, _dp, _ip, _ip, _i64p]),

@@ -6,6 +6,8 @@
 // launches; heights run from the leaves up.  Dense partial Cholesky of a front: blocks of 32
 // columns -- diagonal block (one CTA), panel triangular solve (row chunks), symmetric rank-32
 // update of the trailing lower triangle (64 x 64 tiles).
+#include <vector>
+
 #include "vh_chol.cuh"
 
 namespace vh {
@@ -14,10 +16,14 @@ constexpr int kNB = 32;   // panel width
 constexpr int kTS = 64;   // update tile
 
 // ---- assembly of the original entries of S: F(li, lj) = sum_t c_t D(q_t)
+// Every factorisation kernel handles gridDim.z factors at once (one per frequency): factor z
+// lives at Wp[z] and is built from the diagonal Dp[z].
 __global__ void k_chol_assemble(const FrontInfo* __restrict__ fr, const AsmEntry* __restrict__ ae,
                                 const int32_t* __restrict__ aq, const double* __restrict__ ac,
-                                const double* __restrict__ D, double* __restrict__ W) {
+                                const double* const* __restrict__ Dp, double* const* __restrict__ Wp) {
   const FrontInfo f = fr[blockIdx.x];
+  const double* D = Dp[blockIdx.z];
+  double* W = Wp[blockIdx.z];
   double* F = W + f.w_off;
   for (int e = threadIdx.x; e < f.asm_cnt; e += blockDim.x) {
     const AsmEntry a = ae[f.asm_off + e];
@@ -29,8 +35,9 @@ __global__ void k_chol_assemble(const FrontInfo* __restrict__ fr, const AsmEntry
 
 // ---- extend-add of child `which` of every front in the level list
 __global__ void k_chol_extend_add(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                                  const int32_t* __restrict__ relmap, double* __restrict__ W, int which) {
+                                  const int32_t* __restrict__ relmap, double* const* __restrict__ Wp, int which) {
   const FrontInfo f = fr[lev[blockIdx.x]];
+  double* W = Wp[blockIdx.z];
   const int ci = f.child[which];
   if (ci < 0) return;
   const FrontInfo c = fr[ci];
@@ -47,9 +54,10 @@ __global__ void k_chol_extend_add(const int32_t* __restrict__ lev, const FrontIn
 }
 
 // ---- Cholesky of the diagonal block [k0, k0+w)
-__global__ void k_chol_diag(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr, double* __restrict__ W,
-                            int k0, int* __restrict__ err) {
+__global__ void k_chol_diag(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
+                            double* const* __restrict__ Wp, int k0, int* __restrict__ err) {
   const FrontInfo f = fr[lev[blockIdx.x]];
+  double* W = Wp[blockIdx.z];
   if (f.ns <= k0) return;
   const int w = min(kNB, f.ns - k0);
   __shared__ double A[kNB][kNB + 1];
@@ -84,9 +92,10 @@ __global__ void k_chol_diag(const int32_t* __restrict__ lev, const FrontInfo* __
 }
 
 // ---- panel rows [k0+w, nf): L(r, k0:k0+w) = F(r, k0:k0+w) L11^-T
-__global__ void k_chol_panel(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr, double* __restrict__ W,
-                             int k0) {
+__global__ void k_chol_panel(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
+                             double* const* __restrict__ Wp, int k0) {
   const FrontInfo f = fr[lev[blockIdx.x]];
+  double* W = Wp[blockIdx.z];
   if (f.ns <= k0) return;
   const int w = min(kNB, f.ns - k0);
   const int r = k0 + w + blockIdx.y * blockDim.x + threadIdx.x;
@@ -119,8 +128,9 @@ __global__ void k_chol_panel(const int32_t* __restrict__ lev, const FrontInfo* _
 
 // ---- trailing update F(r, c) -= sum_k L(r, k) L(c, k) for t0 <= c <= r < nf, k in [k0, k0+w)
 __global__ void __launch_bounds__(256) k_chol_update(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                                                     double* __restrict__ W, int k0) {
+                                                     double* const* __restrict__ Wp, int k0) {
   const FrontInfo f = fr[lev[blockIdx.x]];
+  double* W = Wp[blockIdx.z];
   if (f.ns <= k0) return;
   const int w = min(kNB, f.ns - k0);
   const int t0 = k0 + w;
@@ -171,163 +181,246 @@ __global__ void __launch_bounds__(256) k_chol_update(const int32_t* __restrict__
     }
 }
 
-void chol_factor(const CholSymbolic& s, const double* D, double* W, cudaStream_t st) {
-  if (s.nfronts == 0) return;
+void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, double* const* W, cudaStream_t st) {
+  if (s.nfronts == 0 || nfac == 0) return;
+  VH_REQUIRE(nfac <= 65535, ERR_BAD_ARG, "too many factors in one batch");
   int* d_err = s.d_err;
-  VH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-  VH_CUDA_TRY(cudaMemsetAsync(W, 0, s.w_total * sizeof(double), st));
-  k_chol_assemble<<<s.nfronts, 256, 0, st>>>(s.d_fronts, s.d_asm, s.d_asm_q, s.d_asm_c, D, W);
-  count_launch();
-  VH_CUDA_TRY(cudaGetLastError());
-  for (size_t h = 0; h < s.levels.size(); ++h) {
-    const unsigned nf = (unsigned)s.levels[h].size();
-    const int32_t* lev = s.d_levels[h];
-    if (h > 0) {
-      const unsigned cy = (unsigned)std::min(1024, std::max(1, s.level_max_nf[h]));
-      for (int which = 0; which < 2; ++which) {
-        k_chol_extend_add<<<dim3(nf, cy), 128, 0, st>>>(lev, s.d_fronts, s.d_relmap, W, which);
+  double** tab = nullptr;   // device: [D pointers | W pointers]
+  VH_CUDA_TRY(cudaMalloc(&tab, 2 * (size_t)nfac * sizeof(double*)));
+  std::vector<double*> h(2 * (size_t)nfac);
+  for (int i = 0; i < nfac; ++i) {
+    h[i] = const_cast<double*>(D[i]);
+    h[nfac + i] = W[i];
+  }
+  try {
+    VH_CUDA_TRY(cudaMemcpyAsync(tab, h.data(), h.size() * sizeof(double*), cudaMemcpyHostToDevice, st));
+    const double* const* Dp = tab;
+    double* const* Wp = tab + nfac;
+    VH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    for (int i = 0; i < nfac; ++i) VH_CUDA_TRY(cudaMemsetAsync(W[i], 0, s.w_total * sizeof(double), st));
+    const unsigned nz = (unsigned)nfac;
+    k_chol_assemble<<<dim3(s.nfronts, 1, nz), 256, 0, st>>>(s.d_fronts, s.d_asm, s.d_asm_q, s.d_asm_c, Dp, Wp);
+    count_launch();
+    VH_CUDA_TRY(cudaGetLastError());
+    for (size_t hl = 0; hl < s.levels.size(); ++hl) {
+      const unsigned nf = (unsigned)s.levels[hl].size();
+      const int32_t* lev = s.d_levels[hl];
+      if (hl > 0) {
+        const unsigned cy = (unsigned)std::min(1024, std::max(1, s.level_max_nf[hl]));
+        for (int which = 0; which < 2; ++which) {
+          k_chol_extend_add<<<dim3(nf, cy, nz), 128, 0, st>>>(lev, s.d_fronts, s.d_relmap, Wp, which);
+          count_launch();
+          VH_CUDA_TRY(cudaGetLastError());
+        }
+      }
+      const int max_ns = s.level_max_ns[hl];
+      const int max_nf = s.level_max_nf[hl];
+      for (int k0 = 0; k0 < max_ns; k0 += kNB) {
+        k_chol_diag<<<dim3(nf, 1, nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0, d_err);
         count_launch();
+        const int rows = max_nf - k0;
+        if (rows > 0) {
+          k_chol_panel<<<dim3(nf, (unsigned)ceil_div(rows, 128), nz), 128, 0, st>>>(lev, s.d_fronts, Wp, k0);
+          count_launch();
+          const int T = (int)ceil_div(rows, kTS);
+          k_chol_update<<<dim3(nf, (unsigned)(T * (T + 1) / 2), nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0);
+          count_launch();
+        }
         VH_CUDA_TRY(cudaGetLastError());
       }
     }
-    const int max_ns = s.level_max_ns[h];
-    const int max_nf = s.level_max_nf[h];
-    for (int k0 = 0; k0 < max_ns; k0 += kNB) {
-      k_chol_diag<<<nf, 256, 0, st>>>(lev, s.d_fronts, W, k0, d_err);
-      count_launch();
-      const int rows = max_nf - k0;
-      if (rows > 0) {
-        k_chol_panel<<<dim3(nf, (unsigned)ceil_div(rows, 128)), 128, 0, st>>>(lev, s.d_fronts, W, k0);
-        count_launch();
-        const int m = max_nf - k0;
-        const int T = (int)ceil_div(m, kTS);
-        k_chol_update<<<dim3(nf, (unsigned)(T * (T + 1) / 2)), 256, 0, st>>>(lev, s.d_fronts, W, k0);
-        count_launch();
-      }
-      VH_CUDA_TRY(cudaGetLastError());
-    }
+    int herr = 0;
+    VH_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    VH_REQUIRE(herr == 0, ERR_BAD_ARG, "Schur complement is not positive definite (check the port/ground nodes)");
+  } catch (...) {
+    cudaFree(tab);
+    throw;
   }
-  int herr = 0;
-  VH_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-  VH_CUDA_TRY(cudaStreamSynchronize(st));
-  VH_REQUIRE(herr == 0, ERR_BAD_ARG, "Schur complement is not positive definite (check the port/ground nodes)");
+  cudaFree(tab);
 }
 
-// ---- forward solve: L y = b, leaves first.  One CTA per (front, RHS).
-__global__ void k_chol_fsolve(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                              const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap,
-                              double* const* __restrict__ Wp, double2* __restrict__ x, int64_t ldx, int64_t xoff,
-                              double2* __restrict__ U, int64_t u_total) {
+// ---- triangular solves.  One warp per (front, RHS), kSolveWarps warps per CTA.  Each front's
+// dense triangle is processed in blocks of 32 columns: the 32 x 32 diagonal block is solved from
+// shared memory with warp shuffles (lane i owns row i of the block); the rest is coalesced
+// column-major GEMV / dot work whose loads are independent of one another.
+constexpr int kSolveWarps = 4;
+constexpr int kBlk = 32;
+
+struct SolveSmem {
+  static __host__ __device__ size_t per_warp(int max_nf) {
+    return (((size_t)max_nf * sizeof(double2) + 15) & ~(size_t)15) + kBlk * (kBlk + 1) * sizeof(double) +
+           kBlk * sizeof(double2);
+  }
+};
+
+__device__ __forceinline__ double2 shfl_c(double2 v, int src) {
+  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+__global__ void __launch_bounds__(32 * kSolveWarps)
+    k_chol_fsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
+                  const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, double* const* __restrict__ Wp,
+                  double2* __restrict__ x, int64_t ldx, int64_t xoff, double2* __restrict__ U, int64_t u_total,
+                  int max_nf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double2* t = reinterpret_cast<double2*>(smem_raw);
-  const FrontInfo f = fr[lev[blockIdx.x]];
-  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
+  if (item >= (int64_t)nlev * B) return;
+  unsigned char* base = smem_raw + warp * SolveSmem::per_warp(max_nf);
+  double2* t = reinterpret_cast<double2*>(base);
+  double(*Lb)[kBlk + 1] = reinterpret_cast<double(*)[kBlk + 1]>(base + (((size_t)max_nf * sizeof(double2) + 15) & ~(size_t)15));
+  double2* yb = reinterpret_cast<double2*>(reinterpret_cast<unsigned char*>(Lb) + kBlk * (kBlk + 1) * sizeof(double));
+  const FrontInfo f = fr[lev[item % nlev]];
+  const int b = (int)(item / nlev);
   const double* F = Wp[b] + f.w_off;
   double2* xb = x + b * ldx + xoff;
   double2* Ub = U + b * u_total;
   const int32_t* rw = rows + f.rows_off;
-  for (int r = threadIdx.x; r < f.nf; r += blockDim.x) t[r] = (r < f.ns) ? xb[rw[r]] : make_double2(0.0, 0.0);
-  __syncthreads();
+  const int nf = f.nf, ns = f.ns;
+  for (int r = lane; r < nf; r += 32) t[r] = (r < ns) ? xb[rw[r]] : make_double2(0.0, 0.0);
+  __syncwarp();
   for (int c = 0; c < 2; ++c) {
     if (f.child[c] < 0) continue;
     const FrontInfo ch = fr[f.child[c]];
     const int32_t* rm = relmap + ch.relmap_off;
-    for (int a = threadIdx.x; a < ch.nb; a += blockDim.x) {
+    for (int a = lane; a < ch.nb; a += 32) {
       const double2 u = Ub[ch.u_off + a];
       double2& d = t[rm[a]];
       d.x -= u.x;
       d.y -= u.y;
     }
-    __syncthreads();
+    __syncwarp();
   }
-  for (int j = 0; j < f.ns; ++j) {
-    const double inv = 1.0 / F[j + (int64_t)j * f.nf];
-    const double2 y = make_double2(t[j].x * inv, t[j].y * inv);
-    const double* col = F + (int64_t)j * f.nf;
-    for (int r = j + 1 + threadIdx.x; r < f.nf; r += blockDim.x) {
-      const double l = col[r];
-      t[r].x -= l * y.x;
-      t[r].y -= l * y.y;
+  for (int j0 = 0; j0 < ns; j0 += kBlk) {
+    const int w = min(kBlk, ns - j0);
+    for (int k = 0; k < w; ++k) Lb[lane][k] = (lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
+    double2 tv = lane < w ? t[j0 + lane] : make_double2(0.0, 0.0);
+    __syncwarp();
+    for (int k = 0; k < w; ++k) {
+      const double2 tk = shfl_c(tv, k);
+      const double inv = 1.0 / Lb[k][k];
+      const double2 yk = make_double2(tk.x * inv, tk.y * inv);
+      if (lane == k) tv = yk;
+      if (lane > k && lane < w) {
+        const double l = Lb[lane][k];
+        tv.x -= l * yk.x;
+        tv.y -= l * yk.y;
+      }
     }
-    __syncthreads();
+    if (lane < w) {
+      t[j0 + lane] = tv;
+      yb[lane] = tv;
+    }
+    __syncwarp();
+    for (int r = j0 + w + lane; r < nf; r += 32) {
+      double ax = 0.0, ay = 0.0;
+      const double* Lr = F + r + (int64_t)j0 * nf;
+#pragma unroll 8
+      for (int k = 0; k < w; ++k) {
+        const double l = Lr[(int64_t)k * nf];
+        ax = fma(l, yb[k].x, ax);
+        ay = fma(l, yb[k].y, ay);
+      }
+      t[r].x -= ax;
+      t[r].y -= ay;
+    }
+    __syncwarp();
   }
-  for (int j = threadIdx.x; j < f.ns; j += blockDim.x) {
-    const double inv = 1.0 / F[j + (int64_t)j * f.nf];
-    xb[rw[j]] = make_double2(t[j].x * inv, t[j].y * inv);
-  }
-  for (int a = threadIdx.x; a < f.nb; a += blockDim.x) {
-    const double2 v = t[f.ns + a];
+  for (int j = lane; j < ns; j += 32) xb[rw[j]] = t[j];
+  for (int a = lane; a < f.nb; a += 32) {
+    const double2 v = t[ns + a];
     Ub[f.u_off + a] = make_double2(-v.x, -v.y);
   }
 }
 
-// ---- backward solve: L^T x = y, root first.
-__global__ void k_chol_bsolve(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                              const int32_t* __restrict__ rows, double* const* __restrict__ Wp,
-                              double2* __restrict__ x, int64_t ldx, int64_t xoff) {
+__global__ void __launch_bounds__(32 * kSolveWarps)
+    k_chol_bsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
+                  const int32_t* __restrict__ rows, double* const* __restrict__ Wp, double2* __restrict__ x,
+                  int64_t ldx, int64_t xoff, int max_nf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double2* t = reinterpret_cast<double2*>(smem_raw);   // nf: [z_own ; x_boundary]
-  const FrontInfo f = fr[lev[blockIdx.x]];
-  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
+  if (item >= (int64_t)nlev * B) return;
+  unsigned char* base = smem_raw + warp * SolveSmem::per_warp(max_nf);
+  double2* t = reinterpret_cast<double2*>(base);
+  double(*Lb)[kBlk + 1] = reinterpret_cast<double(*)[kBlk + 1]>(base + (((size_t)max_nf * sizeof(double2) + 15) & ~(size_t)15));
+  const FrontInfo f = fr[lev[item % nlev]];
+  const int b = (int)(item / nlev);
   const double* F = Wp[b] + f.w_off;
   double2* xb = x + b * ldx + xoff;
   const int32_t* rw = rows + f.rows_off;
-  for (int r = threadIdx.x; r < f.nf; r += blockDim.x) t[r] = xb[rw[r]];
-  __syncthreads();
-  // z_j -= sum_a L(ns + a, j) x_a   (one warp per column)
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = warp; j < f.ns; j += nw) {
-    const double* col = F + (int64_t)j * f.nf + f.ns;
-    double sx = 0.0, sy = 0.0;
-    for (int a = lane; a < f.nb; a += 32) {
-      const double l = col[a];
-      sx = fma(l, t[f.ns + a].x, sx);
-      sy = fma(l, t[f.ns + a].y, sy);
-    }
+  const int nf = f.nf, ns = f.ns;
+  for (int r = lane; r < nf; r += 32) t[r] = xb[rw[r]];   // own rows: y; boundary rows: final x
+  __syncwarp();
+  const int nblk = (ns + kBlk - 1) / kBlk;
+  for (int bi = nblk - 1; bi >= 0; --bi) {
+    const int j0 = bi * kBlk;
+    const int w = min(kBlk, ns - j0);
+    // z_k -= sum_{r >= j0 + w} L(r, j0 + k) x_r   (all those x_r are final)
+    for (int k = 0; k < w; ++k) {
+      const double* col = F + (int64_t)(j0 + k) * nf;
+      double sx = 0.0, sy = 0.0;
+      for (int r = j0 + w + lane; r < nf; r += 32) {
+        const double l = col[r];
+        sx = fma(l, t[r].x, sx);
+        sy = fma(l, t[r].y, sy);
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+      }
+      if (lane == 0) {
+        t[j0 + k].x -= sx;
+        t[j0 + k].y -= sy;
+      }
     }
-    if (lane == 0) {
-      t[j].x -= sx;
-      t[j].y -= sy;
+    for (int k = 0; k < w; ++k) Lb[lane][k] = (lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
+    __syncwarp();
+    double2 tv = lane < w ? t[j0 + lane] : make_double2(0.0, 0.0);
+    // L_blk^T x_blk = z_blk, last unknown first: lane i < k subtracts L(k, i) x_k
+    for (int k = w - 1; k >= 0; --k) {
+      const double2 zk = shfl_c(tv, k);
+      const double inv = 1.0 / Lb[k][k];
+      const double2 xk = make_double2(zk.x * inv, zk.y * inv);
+      if (lane == k) tv = xk;
+      if (lane < k) {
+        const double l = Lb[k][lane];
+        tv.x -= l * xk.x;
+        tv.y -= l * xk.y;
+      }
     }
+    if (lane < w) t[j0 + lane] = tv;
+    __syncwarp();
   }
-  __syncthreads();
-  for (int j = f.ns - 1; j >= 0; --j) {
-    const double inv = 1.0 / F[j + (int64_t)j * f.nf];
-    const double2 xj = make_double2(t[j].x * inv, t[j].y * inv);
-    for (int k = threadIdx.x; k < j; k += blockDim.x) {
-      const double l = F[j + (int64_t)k * f.nf];
-      t[k].x -= l * xj.x;
-      t[k].y -= l * xj.y;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) t[j] = xj;
-    __syncthreads();
-  }
-  for (int j = threadIdx.x; j < f.ns; j += blockDim.x) xb[rw[j]] = t[j];
+  for (int j = lane; j < ns; j += 32) xb[rw[j]] = t[j];
 }
 
 void chol_solve(const CholSymbolic& s, int B, double* const* Wp, double2* x, int64_t ldx, int64_t xoff, double2* U,
                 cudaStream_t st) {
   if (s.nfronts == 0 || B == 0) return;
-  const size_t sm = (size_t)s.max_nf * sizeof(double2);
-  VH_REQUIRE(sm <= 200 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const size_t sm_max = kSolveWarps * SolveSmem::per_warp(s.max_nf);
+  VH_REQUIRE(sm_max <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
   for (size_t h = 0; h < s.levels.size(); ++h) {
-    const size_t smh = (size_t)s.level_max_nf[h] * sizeof(double2);
-    k_chol_fsolve<<<dim3((unsigned)s.levels[h].size(), B), 256, smh, st>>>(s.d_levels[h], s.d_fronts, s.d_rows,
-                                                                            s.d_relmap, Wp, x, ldx, xoff, U, s.u_total);
+    const int nlev = (int)s.levels[h].size();
+    const int mnf = s.level_max_nf[h];
+    const size_t smh = kSolveWarps * SolveSmem::per_warp(mnf);
+    const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
+    k_chol_fsolve<<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows, s.d_relmap, Wp, x,
+                                                        ldx, xoff, U, s.u_total, mnf);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   for (size_t hh = s.levels.size(); hh-- > 0;) {
-    const size_t smh = (size_t)s.level_max_nf[hh] * sizeof(double2);
-    k_chol_bsolve<<<dim3((unsigned)s.levels[hh].size(), B), 256, smh, st>>>(s.d_levels[hh], s.d_fronts, s.d_rows, Wp,
-                                                                             x, ldx, xoff);
+    const int nlev = (int)s.levels[hh].size();
+    const int mnf = s.level_max_nf[hh];
+    const size_t smh = kSolveWarps * SolveSmem::per_warp(mnf);
+    const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
+    k_chol_bsolve<<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp, x, ldx,
+                                                        xoff, mnf);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }

@@ -65,8 +65,10 @@ void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64
                    const std::vector<int32_t>& t_rp, const std::vector<int32_t>& t_col, const std::vector<double>& t_val,
                    int leaf_size, cudaStream_t st, bool to_device = true);
 
-// Numeric factorisation into W (sym.w_total doubles), with D = A_inv (nc reals, device).
-void chol_factor(const CholSymbolic& s, const double* A_inv, double* W, cudaStream_t st);
+// Numeric factorisation of `nfac` factors at once (one per frequency): factor i goes to W[i]
+// (sym.w_total doubles, device) from the diagonal D[i] = A_inv (nc reals, device).  The pointer
+// arrays are host arrays.
+void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, double* const* W, cudaStream_t st);
 
 // Solves S x = b in place for B right-hand sides.  x: device, complex, RHS b at x + b*ldx + xoff
 // (panel indexing); Wp: device array of B factor pointers; U: device scratch of B * u_total complex.

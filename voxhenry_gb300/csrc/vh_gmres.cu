@@ -264,7 +264,7 @@ struct GmresOut {
 // (zero vector allowed).  scale/zslot: host arrays of B.  pcs: B preconditioners or nullptr.
 void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, const double2* scale_h,
                   const int* zslot_h, const double* tol, int m, int maxit, bool flexible, Prec prec, double2* x,
-                  GmresOut& out) {
+                  GmresOut& out, bool true_relres = true) {
   cudaStream_t st = g->ctx->stream;
   const int64_t n = g->n;
   VH_REQUIRE(m >= 1 && maxit >= 1 && B >= 1, ERR_BAD_ARG, "restart and maxit must be positive");
@@ -506,7 +506,12 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
       if (out.resvec[bb].back() > tol[bb] && out.outer[bb] < maxit) still.push_back(bb);
     active.swap(still);
   }
-  // ---- true relative residual |b - A x| / |b|  (pgmres.m:181)
+  // ---- true relative residual |b - A x| / |b|  (pgmres.m:181); skipped for the inner solves of
+  // the refinement driver, which measures the FP64 residual itself
+  if (!true_relres) {
+    for (int i = 0; i < B; ++i) out.flag[i] = out.resvec[i].back() <= tol[i] ? 0 : 1;
+    return;
+  }
   upload_act(all);
   apply_A(all, x, Wc.p, PREC_FP64);
   k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
@@ -600,7 +605,7 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
     }
     GmresOut inner;
     gmres_device(g, na, pcs ? ps.data() : nullptr, Rc.p, sc.data(), zs.data(), tl.data(), m, maxit, false, PREC_FP32,
-                 D.p, inner);
+                 D.p, inner, false);
     out.matvecs += inner.matvecs;
     out.precons += inner.precons;
     VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, active.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -646,10 +651,7 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
     }
     active.swap(still);
   }
-  // true relative residual
-  A64(all, x, Wc.p);
-  k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
-  count_launch();
+  // true relative residual: R holds b - A x (FP64) from each RHS's last refinement check
   const std::vector<double> rr = row_norms(R.p, n, all, n, d_rows, partr, nrm, st);
   const std::vector<double> bb = row_norms(b, n, all, n, d_rows, partr, nrm, st);
   for (int i = 0; i < B; ++i) {

@@ -161,41 +161,57 @@ vh_status guarded_pc(vh_ctx* ctx, F&& f) {
 
 extern "C" {
 
-vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_sparse_precon, int zslot,
-                           vh_precon** out) {
-  if (!g || !out) return VH_ERR_BAD_ARG;
-  *out = nullptr;
-  auto* p = new vh_precon();
-  p->g = g;
-  p->kind = kind;
+vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, const double* st_sparse_precon,
+                                 const int* zslot, vh_precon** out) {
+  if (!g || !out || nfreq < 1) return VH_ERR_BAD_ARG;
+  for (int i = 0; i < nfreq; ++i) out[i] = nullptr;
+  std::vector<vh_precon*> ps(nfreq, nullptr);
+  for (int i = 0; i < nfreq; ++i) {
+    ps[i] = new vh_precon();
+    ps[i]->g = g;
+    ps[i]->kind = kind;
+  }
   vh_status s = guarded_pc(g->ctx, [&] {
     VH_REQUIRE(kind == VH_PRECON_NONE || kind == VH_PRECON_SCHUR_INVERT, ERR_UNSUPPORTED,
                "preconditioner kind not supported (schur_approx / schur_gmres / schur_invert_original)");
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     if (kind == VH_PRECON_NONE) return;
     VH_REQUIRE(st_sparse_precon, ERR_BAD_ARG, "st_sparse_precon is required");
-    VH_REQUIRE(zslot >= 0 && zslot < (int)g->zslots.size() && g->zslots[zslot], ERR_BAD_ARG, "z slot not set");
     cudaStream_t st = g->ctx->stream;
-    VH_CUDA_TRY(cudaMalloc(&p->A_inv, std::max<int64_t>(1, g->nc) * sizeof(double)));
-    const double2 s1 = make_double2(st_sparse_precon[0], st_sparse_precon[1]);
-    const double2 s2 = make_double2(st_sparse_precon[2], st_sparse_precon[3]);
-    const double2 s3 = make_double2(st_sparse_precon[4], st_sparse_precon[5]);
-    if (g->nv) {
-      k_a_inv<<<256, 256, 0, st>>>(g->zslots[zslot], g->nv, g->dx, s1, s2, s3, p->A_inv);
-      count_launch();
-    }
-    VH_CUDA_TRY(cudaGetLastError());
     ensure_symbolic(g);
-    VH_CUDA_TRY(cudaMalloc(&p->W, std::max<int64_t>(1, g->chol.w_total) * sizeof(double)));
-    ProfScope ps(&g->ctx->prof, SEC_FACTOR, st);
-    chol_factor(g->chol, p->A_inv, p->W, st);
+    std::vector<const double*> D(nfreq);
+    std::vector<double*> W(nfreq);
+    for (int i = 0; i < nfreq; ++i) {
+      const int zs = zslot ? zslot[i] : 0;
+      VH_REQUIRE(zs >= 0 && zs < (int)g->zslots.size() && g->zslots[zs], ERR_BAD_ARG, "z slot not set");
+      vh_precon* p = ps[i];
+      VH_CUDA_TRY(cudaMalloc(&p->A_inv, std::max<int64_t>(1, g->nc) * sizeof(double)));
+      VH_CUDA_TRY(cudaMalloc(&p->W, std::max<int64_t>(1, g->chol.w_total) * sizeof(double)));
+      const double* sp = st_sparse_precon + 6 * i;
+      const double2 s1 = make_double2(sp[0], sp[1]), s2 = make_double2(sp[2], sp[3]), s3 = make_double2(sp[4], sp[5]);
+      if (g->nv) {
+        k_a_inv<<<256, 256, 0, st>>>(g->zslots[zs], g->nv, g->dx, s1, s2, s3, p->A_inv);
+        count_launch();
+      }
+      VH_CUDA_TRY(cudaGetLastError());
+      D[i] = p->A_inv;
+      W[i] = p->W;
+    }
+    ProfScope prof(&g->ctx->prof, SEC_FACTOR, st, nfreq);
+    chol_factor(g->chol, nfreq, D.data(), W.data(), st);
   });
   if (s != VH_OK) {
-    vh_precon_destroy(p);
+    for (auto* p : ps) vh_precon_destroy(p);
     return s;
   }
-  *out = p;
+  for (int i = 0; i < nfreq; ++i) out[i] = ps[i];
   return VH_OK;
+}
+
+vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_sparse_precon, int zslot,
+                           vh_precon** out) {
+  if (!out) return VH_ERR_BAD_ARG;
+  return vh_precon_create_batch(g, kind, 1, st_sparse_precon, &zslot, out);
 }
 
 void vh_precon_destroy(vh_precon* p) {

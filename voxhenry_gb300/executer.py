@@ -87,10 +87,9 @@ class Sweep:
     def prepare(self):
         """lse_sparse_precon_prepare for every frequency (VoxHenry_executer.m:273)."""
         t0 = time.perf_counter()
-        self.pcs = []
-        for i, f in enumerate(self.freqs):
-            jwmu = 1j * 2 * np.pi * f * MU0
-            self.pcs.append(self.geom.precon(jwmu * self.prob.st2, zslot=int(self.zslot[i]), kind=self.precon_kind))
+        jwmu = 1j * 2 * np.pi * self.freqs * MU0
+        st = jwmu[:, None] * np.asarray(self.prob.st2)[None, :]
+        self.pcs = self.geom.precons(st, self.zslot, kind=self.precon_kind)
         self.t_factor = time.perf_counter() - t0
         return self
 

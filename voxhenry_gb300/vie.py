@@ -146,6 +146,16 @@ class Geometry:
         """lse_sparse_precon_prepare for this geometry (st already multiplied by j omega mu)."""
         return Precon(self, st_sparse_precon, zslot=zslot, kind=kind)
 
+    def precons(self, st_list, zslots=None, kind="schur_invert"):
+        """One preconditioner per frequency, factored together (vh_precon_create_batch)."""
+        st = _lib.as_c128(np.asarray(st_list).reshape(-1, 3))
+        F = st.shape[0]
+        zs = np.zeros(F, dtype=np.int32) if zslots is None else np.ascontiguousarray(zslots, dtype=np.int32)
+        hs = (C.c_void_p * F)()
+        _lib.check(self.ctx._lib.vh_precon_create_batch(self.handle, PRECON_KIND[kind], F, _lib.cview(st),
+                                                        zs.ctypes.data_as(C.POINTER(C.c_int)), hs), self.ctx.handle)
+        return [Precon._from_handle(self, C.c_void_p(h), kind) for h in hs]
+
     def solve(self, b, pcs=None, scale=None, zslot=None, restart=50, tol=1e-8, maxit=10, flexible=False,
               prec="fp64", resvec_len=None):
         """Batched pgmres / fpgmres (x0 = 0).  b: (B, n).  Returns dict(x, flag, relres, iter, resvec)."""
@@ -210,6 +220,12 @@ class Precon:
         _lib.check(lib.vh_precon_create(geom.handle, PRECON_KIND[kind], _lib.cview(st) if st.size else None, zslot,
                                         C.byref(h)), geom.ctx.handle)
         self.handle = h
+
+    @classmethod
+    def _from_handle(cls, geom, handle, kind):
+        p = cls.__new__(cls)
+        p.geom, p.kind, p.handle = geom, kind, handle
+        return p
 
     def stats(self):
         nnz, fl, nf, mf = C.c_int64(), C.c_double(), C.c_int(), C.c_int()
