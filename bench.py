@@ -3,7 +3,7 @@
 Workload (the batched configuration of the reference's solve path): 4-turn square spiral coil on a
 256 x 256 x 8 voxel grid (1 um voxels, 5 um trace, 4 voxels thick, 2 um turn spacing,
 sigma = 5.8e7 S/m), one port across the spiral ends, 32 frequencies log-spaced 1 MHz - 20 GHz,
-solved as 32 right-hand sides in one batch (GMRES tol 1e-8, restart 50).  A step is one sweep:
+solved as 32 right-hand sides in one batch (GMRES tol 1e-9, restart 50).  A step is one sweep:
 the Schur-complement factorisation of every frequency plus the batched Krylov solve and the
 R, L extraction.  The circulant tensor, Ae and the symbolic analysis are set up once before the
 timed region (resident in HBM).
@@ -205,6 +205,7 @@ def run_ours(args, rank, world):
         l0 = lib.vh_launch_count()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push(f"timed_{prec}")
         e0.record(stream)
         t0 = time.perf_counter()
         out = None
@@ -212,6 +213,7 @@ def run_ours(args, rank, world):
             out = device_step(prec)
         e1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         wall = time.perf_counter() - t0
         launches = lib.vh_launch_count() - l0
         prof = None
@@ -232,6 +234,9 @@ def run_ours(args, rank, world):
             t = float(tt.item())
         return t, out, launches, prof
 
+    if args.mixed_only:      # profiling aid: only the warm-up and timed mixed-precision steps
+        timed("fp32", args.steps, args.warmup)
+        return
     # accuracy reference: the FP64 GPU path converged to 1e-12 (untimed); the FP64 GPU path matches
     # the oracle to 1e-9 in the parity tests
     R_t, L_t, _ = device_step("fp64", tol=1e-12, maxit=40)
@@ -378,14 +383,56 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_probe(args):
+    """Kernel probe for profilers: a few calls of one operator of the workload's geometry (B RHS)."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from voxhenry_gb300 import _lib, executer, structure
+
+    w, _ = workload()
+    prob = structure.problem_from_workload(w)
+    sw = executer.Sweep(prob, w.freqs, want_fp32=True)
+    g = sw.geom
+    lib = g.ctx._lib
+    B = args.probe_rhs
+    x = torch.randn(B, g.n, 2, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    if args.probe in ("conv32", "conv64"):
+        prec = _lib.PREC["fp32" if args.probe == "conv32" else "fp64"]
+        for _ in range(args.probe_iters):
+            _lib.check(lib.vh_matvec_device(g.handle, B, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), None,
+                                            None, prec), g.ctx.handle)
+    else:
+        st = (1j * 2 * np.pi * w.freqs[:B] * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
+        pcs = g.precons(st, np.zeros(B, dtype=np.int32))
+        parr = (C.c_void_p * B)(*[p.handle for p in pcs])
+        for _ in range(args.probe_iters):
+            _lib.check(lib.vh_precon_apply_device(g.handle, B, parr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr())),
+                       g.ctx.handle)
+    g.ctx.synchronize()
+    print(json.dumps({"probe": args.probe, "rhs": B, "iters": args.probe_iters, "launches": int(lib.vh_launch_count())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--probe", choices=["conv32", "conv64", "precon"], default=None,
+                    help="profiling aid: run a few calls of one operator instead of the benchmark")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="profiling aid: run only the warm-up and timed mixed-precision sweeps, print nothing")
+    ap.add_argument("--probe-rhs", type=int, default=4)
+    ap.add_argument("--probe-iters", type=int, default=3)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.probe:
+        run_probe(args)
+        return
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
     if world > 1:

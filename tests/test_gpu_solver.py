@@ -70,6 +70,28 @@ def test_precon_apply_matches_oracle(lib, blob, f):
     assert st["fronts"] >= 1 and st["nnz_factor"] > 0
 
 
+def test_precon_apply_spiral_matches_oracle(lib):
+    """A 2-turn spiral: many fronts with partial 32-column blocks and empty separators."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.square_spiral(L=96, M=96, N=4, turns=2, thick=2)
+    S, P = problem_of(w)
+    f = 3e9
+    om = 2 * np.pi * f
+    jwmu = 1j * om * solver.MU0
+    z_real, _ = solver.z_arrays(w.sigma_e, None, om)
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, None, S.idxS, jwmu * P.st2, S.Ar)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS)
+    pcs = g.precons(np.stack([jwmu * P.st2] * 3))
+    rng = np.random.default_rng(17)
+    X = rng.standard_normal((3, S.n)) + 1j * rng.standard_normal((3, S.n))
+    Y = vie.apply_precons(g, pcs, X)
+    for k in range(3):
+        assert np.all(np.isfinite(Y[k]))
+        assert rel(Y[k], ref.multiply(X[k])) < PRECON_TOL
+
+
 def test_dropin_calls_match_oracle(lib, blob):
     """lse_sparse_precon_prepare / lse_sparse_precon_multiply / pgmres with the reference's arguments."""
     vie, ex = lib

@@ -85,9 +85,24 @@ __global__ void k_chol_diag(const int32_t* __restrict__ lev, const FrontInfo* __
     }
     __syncthreads();
   }
+  // Invert the factored block (lower triangular) and store the INVERSE in place of the block:
+  // the panel solve and both triangular solves then multiply by it (no divisions, no serial
+  // chain on the slow FP64 pipe).  Thread j computes column j: Linv(j,j) = 1/A(j,j),
+  // Linv(i,j) = -(sum_{k=j}^{i-1} A(i,k) Linv(k,j)) / A(i,i).
+  __shared__ double Iv[kNB][kNB + 1];
+  if (threadIdx.x < w) {
+    const int j = threadIdx.x;
+    Iv[j][j] = 1.0 / A[j][j];
+    for (int i = j + 1; i < w; ++i) {
+      double s = 0.0;
+      for (int k = j; k < i; ++k) s = fma(A[i][k], Iv[k][j], s);
+      Iv[i][j] = -s / A[i][i];
+    }
+  }
+  __syncthreads();
   for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
     const int i = t % w, j = t / w;
-    if (i >= j) F[(k0 + i) + (int64_t)(k0 + j) * f.nf] = A[i][j];
+    if (i >= j) F[(k0 + i) + (int64_t)(k0 + j) * f.nf] = Iv[i][j];
   }
 }
 
@@ -107,19 +122,17 @@ __global__ void k_chol_panel(const int32_t* __restrict__ lev, const FrontInfo* _
   }
   __syncthreads();
   if (r >= f.nf) return;
-  double x[kNB];
+  // the diagonal block holds L11^-1 (k_chol_diag): L(r, k0+j) = sum_{k <= j} F(r, k0+k) Linv(j, k)
+  double a[kNB], x[kNB];
 #pragma unroll
-  for (int j = 0; j < kNB; ++j)
-    if (j < w) x[j] = F[r + (int64_t)(k0 + j) * f.nf];
+  for (int j = 0; j < kNB; ++j) a[j] = j < w ? F[r + (int64_t)(k0 + j) * f.nf] : 0.0;
 #pragma unroll
   for (int j = 0; j < kNB; ++j) {
-    if (j < w) {
-      double s = x[j];
+    double s = 0.0;
 #pragma unroll
-      for (int k = 0; k < kNB; ++k)
-        if (k < j) s -= x[k] * A[j][k];
-      x[j] = s / A[j][j];
-    }
+    for (int k = 0; k < kNB; ++k)
+      if (k <= j) s = fma(a[k], A[j][k], s);
+    x[j] = s;
   }
 #pragma unroll
   for (int j = 0; j < kNB; ++j)
@@ -278,49 +291,69 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   double2* Ub = U + b * u_total;
   const int32_t* rw = rows + f.rows_off;
   const int nf = f.nf, ns = f.ns;
-  for (int r = lane; r < nf; r += 32) t[r] = (r < ns) ? xb[rw[r]] : make_double2(0.0, 0.0);
+  // gathers: 4 independent index loads, then 4 independent value loads per lane
+  for (int r0 = lane; r0 < nf; r0 += 128) {
+    int32_t ix[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ix[u] = (r0 + 32 * u < ns) ? rw[r0 + 32 * u] : -1;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (r0 + 32 * u < nf) t[r0 + 32 * u] = ix[u] >= 0 ? xb[ix[u]] : make_double2(0.0, 0.0);
+  }
   __syncwarp();
   for (int c = 0; c < 2; ++c) {
     if (f.child[c] < 0) continue;
     const FrontInfo ch = fr[f.child[c]];
     const int32_t* rm = relmap + ch.relmap_off;
-    for (int a = lane; a < ch.nb; a += 32) {
-      const double2 u = Ub[ch.u_off + a];
-      double2& d = t[rm[a]];
-      d.x -= u.x;
-      d.y -= u.y;
+    for (int a0 = lane; a0 < ch.nb; a0 += 128) {
+      int32_t ix[4];
+      double2 u[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int a = a0 + 32 * q;
+        ix[q] = a < ch.nb ? rm[a] : -1;
+        u[q] = a < ch.nb ? Ub[ch.u_off + a] : make_double2(0.0, 0.0);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (ix[q] >= 0) {
+          t[ix[q]].x -= u[q].x;
+          t[ix[q]].y -= u[q].y;
+        }
     }
     __syncwarp();
   }
   for (int j0 = 0; j0 < ns; j0 += kBlk) {
     const int w = min(kBlk, ns - j0);
-    for (int k = 0; k < w; ++k) Lb[lane][k] = (lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
-    double2 tv = lane < w ? t[j0 + lane] : make_double2(0.0, 0.0);
+    // the diagonal block holds L_blk^-1 (k_chol_diag): y_blk = L_blk^-1 t_blk, lane i owns row i
+#pragma unroll
+    for (int k = 0; k < kBlk; ++k)
+      Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
+    yb[lane] = lane < w ? t[j0 + lane] : make_double2(0.0, 0.0);   // every lane: yb is read for all 32 k
     __syncwarp();
-    for (int k = 0; k < w; ++k) {
-      const double2 tk = shfl_c(tv, k);
-      const double inv = 1.0 / Lb[k][k];
-      const double2 yk = make_double2(tk.x * inv, tk.y * inv);
-      if (lane == k) tv = yk;
-      if (lane > k && lane < w) {
+    double2 tv = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int k = 0; k < kBlk; ++k) {
+      if (k < w) {
         const double l = Lb[lane][k];
-        tv.x -= l * yk.x;
-        tv.y -= l * yk.y;
+        tv.x = fma(l, yb[k].x, tv.x);
+        tv.y = fma(l, yb[k].y, tv.y);
       }
     }
-    if (lane < w) {
-      t[j0 + lane] = tv;
-      yb[lane] = tv;
-    }
+    __syncwarp();
+    if (lane < w) t[j0 + lane] = tv;
+    yb[lane] = tv;   // zero for lanes >= w (their Lb rows are zero); the GEMV below reads all 32
     __syncwarp();
     for (int r = j0 + w + lane; r < nf; r += 32) {
       double ax = 0.0, ay = 0.0;
       const double* Lr = F + r + (int64_t)j0 * nf;
-#pragma unroll 8
-      for (int k = 0; k < w; ++k) {
-        const double l = Lr[(int64_t)k * nf];
-        ax = fma(l, yb[k].x, ax);
-        ay = fma(l, yb[k].y, ay);
+      double lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : 0.0;   // independent loads
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) {
+        ax = fma(lv[k], yb[k].x, ax);
+        ay = fma(lv[k], yb[k].y, ay);
       }
       t[r].x -= ax;
       t[r].y -= ay;
@@ -351,47 +384,80 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   double2* xb = x + b * ldx + xoff;
   const int32_t* rw = rows + f.rows_off;
   const int nf = f.nf, ns = f.ns;
-  for (int r = lane; r < nf; r += 32) t[r] = xb[rw[r]];   // own rows: y; boundary rows: final x
+  // own rows: y; boundary rows: final x (4 independent index loads, then value loads, per lane)
+  for (int r0 = lane; r0 < nf; r0 += 128) {
+    int32_t ix[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ix[u] = (r0 + 32 * u < nf) ? rw[r0 + 32 * u] : -1;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (ix[u] >= 0) t[r0 + 32 * u] = xb[ix[u]];
+  }
+  __syncwarp();
+  // z_own -= L21^T x_bnd, column-oriented: lane j walks its own column (contiguous rows, no
+  // cross-lane reductions)
+  for (int j = lane; j < ns; j += 32) {
+    const double* col = F + (int64_t)j * nf;
+    double sx = 0.0, sy = 0.0;
+    int r = ns;
+    for (; r + 4 <= nf; r += 4) {
+      double lv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) lv[u] = col[r + u];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        sx = fma(lv[u], t[r + u].x, sx);
+        sy = fma(lv[u], t[r + u].y, sy);
+      }
+    }
+    for (; r < nf; ++r) {
+      const double l = col[r];
+      sx = fma(l, t[r].x, sx);
+      sy = fma(l, t[r].y, sy);
+    }
+    t[j].x -= sx;
+    t[j].y -= sy;
+  }
   __syncwarp();
   const int nblk = (ns + kBlk - 1) / kBlk;
   for (int bi = nblk - 1; bi >= 0; --bi) {
     const int j0 = bi * kBlk;
     const int w = min(kBlk, ns - j0);
-    // z_k -= sum_{r >= j0 + w} L(r, j0 + k) x_r   (all those x_r are final)
-    for (int k = 0; k < w; ++k) {
-      const double* col = F + (int64_t)(j0 + k) * nf;
-      double sx = 0.0, sy = 0.0;
-      for (int r = j0 + w + lane; r < nf; r += 32) {
-        const double l = col[r];
-        sx = fma(l, t[r].x, sx);
-        sy = fma(l, t[r].y, sy);
-      }
+    // x_blk = L_blk^-T z_blk with the stored inverse (lower): lane i: x_i = sum_{k >= i} Linv(k, i) z_k
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        sx += __shfl_xor_sync(0xffffffffu, sx, o);
-        sy += __shfl_xor_sync(0xffffffffu, sy, o);
-      }
-      if (lane == 0) {
-        t[j0 + k].x -= sx;
-        t[j0 + k].y -= sy;
-      }
-    }
-    for (int k = 0; k < w; ++k) Lb[lane][k] = (lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
+    for (int k = 0; k < kBlk; ++k)
+      Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
     __syncwarp();
-    double2 tv = lane < w ? t[j0 + lane] : make_double2(0.0, 0.0);
-    // L_blk^T x_blk = z_blk, last unknown first: lane i < k subtracts L(k, i) x_k
-    for (int k = w - 1; k >= 0; --k) {
-      const double2 zk = shfl_c(tv, k);
-      const double inv = 1.0 / Lb[k][k];
-      const double2 xk = make_double2(zk.x * inv, zk.y * inv);
-      if (lane == k) tv = xk;
-      if (lane < k) {
+    double2 xv = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int k = 0; k < kBlk; ++k) {
+      if (k < w) {
         const double l = Lb[k][lane];
-        tv.x -= l * xk.x;
-        tv.y -= l * xk.y;
+        const double2 zk = t[j0 + k];
+        xv.x = fma(l, zk.x, xv.x);
+        xv.y = fma(l, zk.y, xv.y);
       }
     }
-    if (lane < w) t[j0 + lane] = tv;
+    __syncwarp();
+    if (lane < w) t[j0 + lane] = xv;
+    __syncwarp();
+    // z_j -= sum_{r in block} L(r, j) x_r for the own columns j < j0 (lane per column)
+    for (int j = lane; j < j0; j += 32) {
+      const double* col = F + (int64_t)j * nf + j0;
+      double lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? col[k] : 0.0;
+      double sx = 0.0, sy = 0.0;
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) {
+        if (k < w) {
+          sx = fma(lv[k], t[j0 + k].x, sx);
+          sy = fma(lv[k], t[j0 + k].y, sy);
+        }
+      }
+      t[j].x -= sx;
+      t[j].y -= sy;
+    }
     __syncwarp();
   }
   for (int j = lane; j < ns; j += 32) xb[rw[j]] = t[j];

@@ -55,18 +55,60 @@ static std::vector<double2> twiddles(int n) {
 // ------------------------------------------------------------------------------------------
 template <typename T> struct TileCfg;
 template <> struct TileCfg<double> { static constexpr int target = 2048; };
-template <> struct TileCfg<float> { static constexpr int target = 4096; };
+template <> struct TileCfg<float> { static constexpr int target = 2048; };
 
 static int x_lines_per_cta(int X, int target) { return std::max(1, std::min(64, target / X)); }
+// columns per y-pass tile: even (16-byte chunks of complex64), smem ping-pong buffers <= ~72 KB
 static int y_lines_per_cta(int Y, int X, bool dbl) {
-  int tx = dbl ? (Y <= 512 ? 8 : 4) : (Y <= 512 ? 16 : 8);
-  while (tx > 1 && (int64_t)2 * Y * tx * (dbl ? 16 : 8) > 160 * 1024) tx /= 2;
-  return std::max(1, std::min(tx, X));
+  int tx = dbl ? 4 : 8;
+  while (tx > 2 && (int64_t)2 * Y * tx * (dbl ? 16 : 8) > 72 * 1024) tx /= 2;
+  return std::max(dbl ? 1 : 2, std::min(tx, X));
 }
+
+// ---- asynchronous 16-byte global -> shared copies (many in flight per thread)
+__device__ __forceinline__ void cp_async16(void* s, const void* g) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// rows x cols tile from global (row stride gs elements) into shared memory (row stride ss).
+// Rows >= rv or columns >= cv read as zero.  Needs 16-byte aligned row starts and cols, cv, ss
+// multiples of the elements per 16 bytes (2 for complex64, 1 for complex128).
+template <typename C>
+__device__ __forceinline__ void tile_load(C* s, int ss, const C* g, int64_t gs, int rows, int rv, int cols, int cv) {
+  constexpr int E = 16 / sizeof(C);
+  const int cpr = cols / E, cvr = cv / E;
+  for (int q = threadIdx.x; q < rows * cpr; q += blockDim.x) {
+    const int r = q / cpr, ch = q - r * cpr;
+    C* dst = s + r * ss + ch * E;
+    if (r < rv && ch < cvr) {
+      cp_async16(dst, g + r * gs + ch * E);
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) dst[e] = czero<C>();
+    }
+  }
+}
+
+// rows x cv tile from shared memory (row stride ss) to global (row stride gs), 16-byte stores
+template <typename C>
+__device__ __forceinline__ void tile_store(C* g, int64_t gs, const C* s, int ss, int rows, int cv) {
+  constexpr int E = 16 / sizeof(C);
+  const int cvr = cv / E;
+  for (int q = threadIdx.x; q < rows * cvr; q += blockDim.x) {
+    const int r = q / cvr, ch = q - r * cvr;
+    *reinterpret_cast<int4*>(g + r * gs + ch * E) = *reinterpret_cast<const int4*>(s + r * ss + ch * E);
+  }
+}
+// columns per z-pass tile: even (16-byte chunks), blockDim = Z * tx <= 1024 (Z <= 512)
 static int z_lines_per_cta(int Z, int X) {
   int tx = 16;
-  while (tx > 1 && Z * tx > 512) tx /= 2;
-  return std::max(1, std::min(tx, X));
+  while (tx > 2 && Z * tx > 512) tx /= 2;
+  return std::max(2, std::min(tx, X));
 }
 
 // ------------------------------------------------------------------------------------------
@@ -83,27 +125,39 @@ __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int3
   C* b1 = b0 + X * nl;
   for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
   const int64_t l0 = (int64_t)blockIdx.x * nl;
-  for (int t = threadIdx.x; t < X * nl; t += blockDim.x) {
-    const int line = t / X, i = t % X;
-    const int64_t gl = l0 + line;
-    C v = czero<C>();
-    if (gl < nlines_total && i < L) {
-      const int64_t y = gl % M;
-      const int64_t z = (gl / M) % N;
-      const int64_t c = (gl / ((int64_t)M * N)) % 5;
-      const int64_t b = gl / ((int64_t)M * N * 5);
-      const int32_t vid = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
-      if (vid >= 0) v = to_c(xin[b * ldx + c * nv + vid], C());
+  const int tot = X * nl;
+  for (int t0 = threadIdx.x; t0 < tot; t0 += 4 * blockDim.x) {
+    int32_t vid[4];
+    int64_t off[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {     // independent voxel-map loads
+      const int t = t0 + u * blockDim.x;
+      const int line = t / X, i = t - (t / X) * X;
+      const int64_t gl = l0 + line;
+      vid[u] = -1;
+      off[u] = 0;
+      if (t < tot && gl < nlines_total && i < L) {
+        const int64_t y = gl % M;
+        const int64_t z = (gl / M) % N;
+        const int64_t c = (gl / ((int64_t)M * N)) % 5;
+        const int64_t b = gl / ((int64_t)M * N * 5);
+        vid[u] = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
+        off[u] = b * ldx + c * nv;
+      }
     }
-    b0[line * X + i] = v;
+    C v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = vid[u] >= 0 ? to_c(xin[off[u] + vid[u]], C()) : czero<C>();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int t = t0 + u * blockDim.x;
+      if (t < tot) b0[t] = v[u];
+    }
   }
   __syncthreads();
   C* r = fft_lines<-1>(b0, b1, tw, fd, 1, X, nl, true);
-  for (int t = threadIdx.x; t < X * nl; t += blockDim.x) {
-    const int line = t / X, i = t % X;
-    const int64_t gl = l0 + line;
-    if (gl < nlines_total) A[gl * X + i] = r[line * X + i];
-  }
+  const int rows = (nlines_total - l0 < nl) ? (int)(nlines_total - l0) : nl;
+  tile_store(A + l0 * X, X, r, X, rows, X);
 }
 
 // pass 2 / 4: FFT along y.  Rows of `nin` input (index < nin), `nout` output rows written.
@@ -122,20 +176,12 @@ __global__ void k_pass_y(const cplx<T>* __restrict__ src, int src_rows, int nin,
   const int64_t plane = blockIdx.y;
   const C* s = src + plane * src_rows * (int64_t)X;
   C* d = dst + plane * dst_rows * (int64_t)X;
-  for (int t = threadIdx.x; t < Y * tx; t += blockDim.x) {
-    const int line = t % tx, i = t / tx;
-    const int kx = kx0 + line;
-    C v = czero<C>();
-    if (i < nin && kx < X) v = s[(int64_t)i * X + kx];
-    b0[i * tx + line] = v;
-  }
+  const int cv = min(tx, X - kx0);
+  tile_load(b0, tx, s + kx0, X, Y, nin, tx, cv);
+  cp_async_wait_all();
   __syncthreads();
   C* r = fft_lines<DIR>(b0, b1, tw, fd, tx, 1, tx, false);
-  for (int t = threadIdx.x; t < nout * tx; t += blockDim.x) {
-    const int line = t % tx, i = t / tx;
-    const int kx = kx0 + line;
-    if (kx < X) d[(int64_t)i * X + kx] = r[i * tx + line];
-  }
+  tile_store(d + kx0, X, r, tx, nout, cv);
 }
 
 // pass 3: z-FFT, tensor product, inverse z-FFT.  B[b][c][z<N][ky][kx] in place.
@@ -168,14 +214,10 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
   const int64_t comp = (int64_t)N * plane;   // one component of one RHS
   for (int b = 0; b < nrhs; ++b) {
     C* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X;
-    for (int t = threadIdx.x; t < Z * nl; t += blockDim.x) {
-      const int line = t % nl, i = t / nl;
-      const int c = line / tx, tt = line % tx;
-      const int kx = kx0 + tt;
-      C v = czero<C>();
-      if (i < N && kx < X) v = base[c * comp + i * plane + kx];
-      b0[i * nl + line] = v;
-    }
+    const int cv = min(tx, X - kx0);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) tile_load(b0 + c * tx, nl, base + c * comp + kx0, plane, Z, N, tx, cv);
+    cp_async_wait_all();
     __syncthreads();
     C* f = fft_lines<-1>(b0, b1, tw, fd, nl, 1, nl, false);
     if (my_kz < Z) {
@@ -198,12 +240,8 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
     __syncthreads();
     C* other = (f == b0) ? b1 : b0;
     C* r = fft_lines<+1>(f, other, tw, fd, nl, 1, nl, false);
-    for (int t = threadIdx.x; t < N * nl; t += blockDim.x) {
-      const int line = t % nl, i = t / nl;
-      const int c = line / tx, tt = line % tx;
-      const int kx = kx0 + tt;
-      if (kx < X) base[c * comp + i * plane + kx] = r[i * nl + line];
-    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) tile_store(base + c * comp + kx0, plane, r + c * tx, nl, N, cv);
     __syncthreads();
   }
 }
@@ -223,11 +261,9 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
   C* b1 = b0 + X * nl;
   for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
   const int64_t l0 = (int64_t)blockIdx.x * nl;
-  for (int t = threadIdx.x; t < X * nl; t += blockDim.x) {
-    const int line = t / X, i = t % X;
-    const int64_t gl = l0 + line;
-    b0[line * X + i] = (gl < nlines_total) ? A[gl * X + i] : czero<C>();
-  }
+  const int rows_valid = (nlines_total - l0 < nl) ? (int)(nlines_total - l0) : nl;
+  tile_load(b0, X, A + l0 * X, X, nl, rows_valid, X, X);
+  cp_async_wait_all();
   __syncthreads();
   C* r = fft_lines<+1>(b0, b1, tw, fd, 1, X, nl, true);
   for (int t = threadIdx.x; t < L * nl; t += blockDim.x) {
@@ -272,7 +308,7 @@ void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2
   p.L = L; p.M = M; p.N = N; p.X = 2 * L; p.Y = 2 * M; p.Z = 2 * N; p.nv = nv; p.dx = dx;
   VH_REQUIRE(fft_factor(p.X, p.fx) && fft_factor(p.Y, p.fy) && fft_factor(p.Z, p.fz), ERR_UNSUPPORTED,
              "padded grid dimensions must factor into 2, 3, 5 and 7");
-  VH_REQUIRE(p.X <= 4096 && p.Y <= 4096 && p.Z <= 1024, ERR_UNSUPPORTED, "padded grid dimension too large");
+  VH_REQUIRE(p.X <= 4096 && p.Y <= 4096 && p.Z <= 512, ERR_UNSUPPORTED, "padded grid dimension too large");
   // voxel map
   const int64_t lmn = p.lmn();
   std::vector<int32_t> vm(lmn, -1);

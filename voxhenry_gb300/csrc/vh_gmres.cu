@@ -264,7 +264,7 @@ struct GmresOut {
 // (zero vector allowed).  scale/zslot: host arrays of B.  pcs: B preconditioners or nullptr.
 void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, const double2* scale_h,
                   const int* zslot_h, const double* tol, int m, int maxit, bool flexible, Prec prec, double2* x,
-                  GmresOut& out, bool true_relres = true) {
+                  GmresOut& out, bool true_relres = true, const double2* pre_Mb = nullptr) {
   cudaStream_t st = g->ctx->stream;
   const int64_t n = g->n;
   VH_REQUIRE(m >= 1 && maxit >= 1 && B >= 1, ERR_BAD_ARG, "restart and maxit must be positive");
@@ -339,8 +339,12 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
   }
   std::vector<double> bnorm(B);
   if (!flexible && pcs) {
-    apply_M(all, R.p, Zc.p);
-    VH_CUDA_TRY(cudaMemcpyAsync(R.p, Zc.p, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    if (pre_Mb && !any_x0) {   // M^-1 b supplied by the caller (the refinement driver already has it)
+      VH_CUDA_TRY(cudaMemcpyAsync(R.p, pre_Mb, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    } else {
+      apply_M(all, R.p, Zc.p);
+      VH_CUDA_TRY(cudaMemcpyAsync(R.p, Zc.p, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    }
     if (any_x0) {
       apply_M(all, b, Zc.p);
       bnorm = row_norms(Zc.p, n, all, n, d_rows, partr, nrm, st);
@@ -603,9 +607,14 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       tl[a] = std::max(inner_tol, 0.5 * tol[bb] * mb[bb] / std::max(sn[bb], 1e-300));
       ps[a] = pcs ? pcs[bb] : nullptr;
     }
+    // M^-1 r of the active rows (kept from the last check) seeds the inner solve
+    DevBuf<double2> Sc;
+    Sc.ensure((size_t)na * n);
+    k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(S.p, n, Sc.p, n, d_act.p, n);
+    count_launch();
     GmresOut inner;
     gmres_device(g, na, pcs ? ps.data() : nullptr, Rc.p, sc.data(), zs.data(), tl.data(), m, maxit, false, PREC_FP32,
-                 D.p, inner, false);
+                 D.p, inner, false, pcs ? Sc.p : nullptr);
     out.matvecs += inner.matvecs;
     out.precons += inner.precons;
     VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, active.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -637,10 +646,13 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       for (int a = 0; a < na; ++a) seq[a] = a;
       M(active, Ya.p, Sa.p);
       std::vector<double> snorm = row_norms(Sa.p, n, seq, n, d_rows, partr, nrm, st);
-      // scatter residuals back
-      for (int a = 0; a < na; ++a)
+      // scatter residuals (and their preconditioned form) back
+      for (int a = 0; a < na; ++a) {
         VH_CUDA_TRY(cudaMemcpyAsync(R.p + (int64_t)active[a] * n, Ya.p + (int64_t)a * n, n * sizeof(double2),
                                     cudaMemcpyDeviceToDevice, st));
+        VH_CUDA_TRY(cudaMemcpyAsync(S.p + (int64_t)active[a] * n, Sa.p + (int64_t)a * n, n * sizeof(double2),
+                                    cudaMemcpyDeviceToDevice, st));
+      }
       VH_CUDA_TRY(cudaStreamSynchronize(st));
       for (int a = 0; a < na; ++a) {
         const int bb = active[a];
@@ -689,7 +701,8 @@ void gmres_dispatch(vh_geom* g, int B, vh_precon* const* pcs, const double2* b_d
   GmresOut o;
   std::vector<int> steps;
   if (prec == VH_PREC_FP32)
-    solve_mixed_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, 1e-4, 20, x_dev, o, steps);
+    // inner tolerance 1e-5: above the complex64 floor, and two FP64 checks reach 1e-9..1e-10
+    solve_mixed_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, 1e-5, 20, x_dev, o, steps);
   else
     gmres_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, flexible != 0, PREC_FP64, x_dev, o);
   VH_CUDA_TRY(cudaStreamSynchronize(st));
