@@ -93,6 +93,27 @@ vh_status vh_matvec(vh_geom* g, int B, const double* x, double* y, const double*
 vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, const void* scale_dev,
                            const int* zslot, vh_prec prec);
 
+/* ---- allocation-free matvec (no counterpart in the reference) -----------------------------------
+ * The operator of vh_matvec_device, same arguments and results, enqueued on the context stream, but
+ * the call allocates no device memory (no cudaMalloc / cudaFree, no allocating library routine).
+ * For callers that cannot allocate at call time: a host whose device memory is all handed to its own
+ * pool allocator (a framework's caching allocator under a memory cap), and a host whose solve loop
+ * must not stall, since cudaMalloc / cudaFree synchronise the whole device and so serialise the work
+ * of its other streams.
+ *   - FFT scratch: one fixed device array of VH_MATVEC_NOALLOC_SCRATCH_BYTES per device, shared by
+ *     every context on that device.  The right-hand sides are processed in groups that fit it (at
+ *     most 64 per group); a grid whose single right-hand side needs more (30 L M N complex values of
+ *     the precision) is rejected with VH_ERR_UNSUPPORTED.  Nothing in it needs to start at zero.
+ *   - Calls whose GPU work overlaps (streams of different contexts on one device) race on that
+ *     scratch: order them on the device (one context, or events between the streams).
+ *   - The first call on a device does the set-up (it looks up the scratch array's device address and
+ *     fills a table of unit scales, then synchronises the context stream); make that first call
+ *     before any stream capture.
+ *   - zslot: as vh_matvec_device (NULL: slot 0); every slot named must already be set.           */
+#define VH_MATVEC_NOALLOC_SCRATCH_BYTES (16u << 20)
+vh_status vh_matvec_device_noalloc(vh_geom* g, int B, const void* x_dev, void* y_dev, const void* scale_dev,
+                                   const int* zslot, vh_prec prec);
+
 /* ---- preconditioner: lse_sparse_precon_prepare(dx, z_real, z_imag, idxS, st_sparse_precon, ..., Ae)
  *      (lse_sparse_precon_prepare.m:1).  A geometry created with fN_all == NULL serves a
  *      preconditioner-only caller.  st_sparse_precon: 3 complex self terms (already multiplied by

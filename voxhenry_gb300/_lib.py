@@ -38,6 +38,7 @@ SIGNATURES = {
     "vh_geom_set_z": (C.c_int, [_p, C.c_int, _dp, _dp]),
     "vh_matvec": (C.c_int, [_p, C.c_int, _dp, _dp, _dp, _ip, C.c_int]),
     "vh_matvec_device": (C.c_int, [_p, C.c_int, _p, _p, _p, _ip, C.c_int]),
+    "vh_matvec_device_noalloc": (C.c_int, [_p, C.c_int, _p, _p, _p, _ip, C.c_int]),
     "vh_precon_create": (C.c_int, [_p, C.c_int, _dp, C.c_int, C.POINTER(_p)]),
     "vh_precon_destroy": (None, [_p]),
     "vh_precon_create_batch": (C.c_int, [_p, C.c_int, C.c_int, _dp, _ip, C.POINTER(_p)]),

@@ -538,4 +538,27 @@ void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, do
     conv_apply_t<float>(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
 }
 
+void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t& b_per_rhs) {
+  const size_t cs = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
+  a_per_rhs = (size_t)5 * p.N * p.M * p.X * cs;
+  b_per_rhs = (size_t)5 * p.N * p.Y * p.X * cs;
+}
+
+void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
+                        const double2* scale, const double2* zdiag, int64_t zstride, void* scratchA, void* scratchB,
+                        cudaStream_t st) {
+  VH_REQUIRE(((uintptr_t)scratchA | (uintptr_t)scratchB) % 16 == 0, ERR_BAD_ARG, "FFT scratch must be 16-byte aligned");
+  size_t a1, b1;
+  conv_scratch_bytes(p, prec, a1, b1);
+  ConvPlan q = p;   // shallow view of the plan with the caller's scratch; owns nothing
+  q.scratchA = scratchA;
+  q.scratchB = scratchB;
+  q.scratch_bytes_A = a1 * B;
+  q.scratch_bytes_B = b1 * B;
+  if (prec == PREC_FP64)
+    conv_apply_t<double>(q, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
+  else
+    conv_apply_t<float>(q, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
+}
+
 }  // namespace vh

@@ -49,6 +49,18 @@ void conv_plan_reserve(ConvPlan& p, int B, Prec prec);
 void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
                 const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st);
 
+// Bytes of FFT scratch one right-hand side needs at precision `prec`: A (5 N M X complex values)
+// and Bf (5 N Y X complex values).
+void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t& b_per_rhs);
+
+// conv_apply with caller-provided scratch (scratchA: B * a_per_rhs bytes, scratchB: B * b_per_rhs
+// bytes, both 16-byte aligned), for callers that cannot allocate device memory: it reserves nothing
+// and allocates nothing.  Every scratch element a pass reads was written by an earlier pass, so the
+// scratch needs no clearing.
+void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
+                        const double2* scale, const double2* zdiag, int64_t zstride, void* scratchA, void* scratchB,
+                        cudaStream_t st);
+
 // In-place forward 3-D FFT of `batch` column-major X x Y x Z complex arrays (device).
 void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaStream_t st);
 
