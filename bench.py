@@ -40,6 +40,9 @@ UNIT = "freq-points/s"
 TOL = 1e-9
 RESTART = 50
 MAXIT = 10
+# the mixed path's Schur factor and triangular solves run in double-float (FP32 pairs, ~48 bits) on
+# GB300's FP32 pipes; its FP64 refinement residuals set the final accuracy
+MIXED_PRECON = "schur_invert_df"
 
 
 def dist_env():
@@ -59,7 +62,8 @@ def workload():
         "grid": [256, 256, 8],
         "voxels": int((w.sigma_e > 0).sum()),
         "rhs_per_step": len(w.freqs),
-        "gmres": {"tol": TOL, "restart": RESTART, "maxit": MAXIT, "preconditioner": "schur_invert (left)"},
+        "gmres": {"tol": TOL, "restart": RESTART, "maxit": MAXIT, "preconditioner": "schur_invert (left)",
+                  "schur_factor": {"mixed": "double-float (FP32 pairs)", "fp64": "fp64"}},
         "l2": "per-RHS vectors (~9.6 MB complex128 each) x 32 RHS and the 470 MB complex128 tensor exceed "
               "the 129 MB L2; no flush needed",
     }
@@ -150,6 +154,8 @@ def run_ours(args, rank, world):
 
     torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
     w, cfg = workload()
+    if args.mixed_precon != MIXED_PRECON:
+        cfg["gmres"]["schur_factor"]["mixed"] = "fp64"
     prob = structure.problem_from_workload(w)
     freqs = w.freqs
     sw = executer.Sweep(prob, freqs, want_fp32=True)
@@ -175,9 +181,12 @@ def run_ours(args, rank, world):
 
     st_all = (1j * 2 * np.pi * freqs * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
 
+    def precon_kind(prec):
+        return args.mixed_precon if prec == "fp32" else "schur_invert"
+
     def device_step(prec, tol=None, maxit=MAXIT):
         """One sweep with device-resident inputs: factors + batched solve + R, L."""
-        pcs = g.precons(st_all, sw.zslot)
+        pcs = g.precons(st_all, sw.zslot, kind=precon_kind(prec))
         parr = (C.c_void_p * B)(*[pcs[k // prob.num_ports].handle for k in range(B)])
         tv = tolv if tol is None else np.full(B, tol)
         st = lib.vh_gmres_device(g.handle, B, parr, C.c_void_p(b_dev.data_ptr()), _lib.cview(scale),
@@ -249,6 +258,7 @@ def run_ours(args, rank, world):
     t_fp64, out_fp64, _, _ = timed("fp64", args.steps, args.warmup)
     # e2e: the host-buffer C ABI call a user makes (Sweep -> vh_gmres), copies inside the region
     sw.pcs = None
+    sw.precon_kind = precon_kind("fp32")
     for _ in range(args.warmup):
         sw.prepare().solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
     torch.cuda.synchronize()
@@ -429,6 +439,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mixed-precon", default=MIXED_PRECON, choices=["schur_invert_df", "schur_invert"],
+                    help="Schur factor arithmetic of the mixed-precision path")
     args = ap.parse_args()
     if args.probe:
         run_probe(args)

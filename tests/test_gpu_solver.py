@@ -192,3 +192,59 @@ def test_numex1_matches_reference_results(lib):
     x = out["x"][2]
     idx = gold["numex1_x_sample_idx"]
     np.testing.assert_allclose(x[idx], gold["numex1_x_sample"], rtol=0, atol=1e-6 * np.abs(gold["numex1_x_sample"]).max())
+
+
+def test_precon_double_float_factor(lib, blob):
+    """VH_PRECON_SCHUR_INVERT_DF: factor and triangular solves in FP32 pairs (~48 bits): within
+    about cond(S) x 4e-15 of the FP64 preconditioner; 1e-10 on this geometry."""
+    vie, ex = lib
+    w, S, P = blob
+    om = 2 * np.pi * 1e9
+    jwmu = 1j * om * solver.MU0
+    z_real, _ = solver.z_arrays(w.sigma_e, None, om)
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, None, S.idxS, jwmu * P.st2, S.Ar)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS)
+    pcs = g.precons(np.stack([jwmu * P.st2] * 3), kind="schur_invert_df")
+    rng = np.random.default_rng(11)
+    X = rng.standard_normal((3, S.n)) + 1j * rng.standard_normal((3, S.n))
+    Y = vie.apply_precons(g, pcs, X)
+    for k in range(3):
+        assert np.all(np.isfinite(Y[k]))
+        assert rel(Y[k], ref.multiply(X[k])) < 1e-10
+
+
+def test_precon_double_float_spiral(lib):
+    """The double-float factor on a 2-turn spiral (partial blocks, empty separators, larger condition)."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.square_spiral(L=96, M=96, N=4, turns=2, thick=2)
+    S, P = problem_of(w)
+    om = 2 * np.pi * 3e9
+    jwmu = 1j * om * solver.MU0
+    z_real, _ = solver.z_arrays(w.sigma_e, None, om)
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, None, S.idxS, jwmu * P.st2, S.Ar)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS)
+    pcs = g.precons(np.stack([jwmu * P.st2] * 2), kind="schur_invert_df")
+    rng = np.random.default_rng(17)
+    X = rng.standard_normal((2, S.n)) + 1j * rng.standard_normal((2, S.n))
+    Y = vie.apply_precons(g, pcs, X)
+    for k in range(2):
+        assert np.all(np.isfinite(Y[k]))
+        assert rel(Y[k], ref.multiply(X[k])) < 1e-8
+
+
+def test_mixed_precision_double_float_factor_rl(lib):
+    """Mixed precision with the double-float Schur factor: R, L within 1e-6 of the oracle, every flag 0."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.two_bars(L=24, M=14, N=6, xr=(2, 22), zr=(1, 4), y1=(2, 5), y2=(9, 12))
+    S, P = problem_of(w)
+    freqs = np.array([1e3, 1e8, 1e10])
+    sw = ex.Sweep(P, freqs, precon="schur_invert_df").prepare()
+    out = sw.solve(restart=50, tol=1e-10, maxit=10, prec="fp32")
+    ref = solver.solve_frequencies(S, P.fN_all2, P.st2, freqs, restart=50, tol=1e-12)
+    assert np.all(out["flag"] == 0)
+    assert_port_matrix_close(out["R"], ref["R"], 1e-6)
+    assert_port_matrix_close(out["L"], ref["L"], 1e-6)

@@ -319,6 +319,7 @@ void vh_geom_destroy(vh_geom* g) {
   g->AeT.free_all();
   g->chol.free_all();
   cudaFree(g->pc_tmp);
+  cudaFree(g->pc_phi_df);
   cudaFree(g->pc_ptrs);
   for (auto* z : g->zslots) cudaFree(z);
   cudaFree(g->ones);

@@ -1,82 +1,95 @@
 // Multifrontal Cholesky of S = Ar D Ar^T on the device: numeric factorisation and solves.
 //
 // Factor storage W: one dense nf x nf column-major block per front.  After the factorisation
-// its first ns columns hold [L11; L21] and its trailing nb x nb block holds the update matrix
-// passed to the parent (extend-add).  All fronts of one tree height are processed by the same
-// launches; heights run from the leaves up.  Dense partial Cholesky of a front: blocks of 32
-// columns -- diagonal block (one CTA), panel triangular solve (row chunks), symmetric rank-32
-// update of the trailing lower triangle (64 x 64 tiles).
+// its first ns columns hold [L11; L21] (with each 32 x 32 diagonal block of L11 replaced by its
+// inverse) and its trailing nb x nb block holds the update matrix passed to the parent
+// (extend-add).  All fronts of one tree height are processed together; heights run from the
+// leaves up.  Fronts with nf <= kFusedMaxNf are factored whole in shared memory by one CTA
+// (k_chol_front); larger ones by blocks of 32 columns -- diagonal block (one CTA), panel
+// (row chunks), symmetric rank-32 update of the trailing lower triangle (64 x 64 tiles).
+//
+// The kernels are templates on the factor's element type T: double (the reference's arithmetic)
+// or dfloat, the FP32-pair format of the mixed-precision solver's factor (about 48 significant
+// bits on the FP32 pipes, which GB300 runs at 64 times its FP64 rate).  A plain single-precision
+// factor was measured and rejected: on the 256 x 256 x 8 spiral the Schur complement is too
+// ill-conditioned (FP32 Cholesky breaks down, and an FP32 LU preconditioner raises GMRES iterations
+// from 3-28 to 7-80+).
 #include <vector>
 
 #include "vh_chol.cuh"
+#include "vh_df.cuh"
 
 namespace vh {
 
 constexpr int kNB = 32;   // panel width
 constexpr int kTS = 64;   // update tile
 
+template <typename T> __device__ __forceinline__ T rsqrt_t(T p);
+template <> __device__ __forceinline__ double rsqrt_t<double>(double p) { return 1.0 / sqrt(p); }
+template <> __device__ __forceinline__ float rsqrt_t<float>(float p) { return 1.0f / sqrtf(p); }
+template <> __device__ __forceinline__ dfloat rsqrt_t<dfloat>(dfloat p) { return df_rsqrt(p); }
+
 // ---- assembly of the original entries of S: F(li, lj) = sum_t c_t D(q_t)
 // Every factorisation kernel handles gridDim.z factors at once (one per frequency): factor z
 // lives at Wp[z] and is built from the diagonal Dp[z].
+template <typename T>
 __global__ void k_chol_assemble(const FrontInfo* __restrict__ fr, const AsmEntry* __restrict__ ae,
                                 const int32_t* __restrict__ aq, const double* __restrict__ ac,
-                                const double* const* __restrict__ Dp, double* const* __restrict__ Wp) {
+                                const double* const* __restrict__ Dp, T* const* __restrict__ Wp) {
   const FrontInfo f = fr[blockIdx.x];
   const double* D = Dp[blockIdx.z];
-  double* W = Wp[blockIdx.z];
-  double* F = W + f.w_off;
+  T* F = Wp[blockIdx.z] + f.w_off;
   for (int e = threadIdx.x; e < f.asm_cnt; e += blockDim.x) {
     const AsmEntry a = ae[f.asm_off + e];
     double s = 0.0;
     for (int t = a.t0; t < a.t1; ++t) s = fma(ac[t], D[aq[t]], s);
-    F[a.li + (int64_t)a.lj * f.nf] = s;
+    F[a.li + (int64_t)a.lj * f.nf] = (T)s;
   }
 }
 
 // ---- extend-add of child `which` of every front in the level list
+template <typename T>
 __global__ void k_chol_extend_add(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                                  const int32_t* __restrict__ relmap, double* const* __restrict__ Wp, int which) {
+                                  const int32_t* __restrict__ relmap, T* const* __restrict__ Wp, int which) {
   const FrontInfo f = fr[lev[blockIdx.x]];
-  double* W = Wp[blockIdx.z];
+  T* W = Wp[blockIdx.z];
   const int ci = f.child[which];
   if (ci < 0) return;
   const FrontInfo c = fr[ci];
   const int nb = c.nb;
   const int32_t* rm = relmap + c.relmap_off;
-  const double* U = W + c.w_off + c.ns + (int64_t)c.ns * c.nf;   // U(a, b) = U[a + b * c.nf]
-  double* F = W + f.w_off;
+  const T* U = W + c.w_off + c.ns + (int64_t)c.ns * c.nf;   // U(a, b) = U[a + b * c.nf]
+  T* F = W + f.w_off;
   for (int b = blockIdx.y; b < nb; b += gridDim.y) {
     const int lj = rm[b];
-    for (int a = b + threadIdx.x; a < nb; a += blockDim.x) {
-      F[rm[a] + (int64_t)lj * f.nf] += U[a + (int64_t)b * c.nf];
-    }
+    for (int a = b + threadIdx.x; a < nb; a += blockDim.x) F[rm[a] + (int64_t)lj * f.nf] += U[a + (int64_t)b * c.nf];
   }
 }
 
-// ---- Cholesky of the diagonal block [k0, k0+w)
+// ---- Cholesky of the diagonal block [k0, k0+w); the block is replaced by the inverse of its factor
+template <typename T>
 __global__ void k_chol_diag(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                            double* const* __restrict__ Wp, int k0, int* __restrict__ err) {
+                            T* const* __restrict__ Wp, int k0, int* __restrict__ err) {
   const FrontInfo f = fr[lev[blockIdx.x]];
-  double* W = Wp[blockIdx.z];
+  T* W = Wp[blockIdx.z];
   if (f.ns <= k0) return;
   const int w = min(kNB, f.ns - k0);
-  __shared__ double A[kNB][kNB + 1];
-  double* F = W + f.w_off;
+  __shared__ T A[kNB][kNB + 1];
+  T* F = W + f.w_off;
   for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
     const int i = t % w, j = t / w;
-    A[i][j] = (i >= j) ? F[(k0 + i) + (int64_t)(k0 + j) * f.nf] : 0.0;
+    A[i][j] = (i >= j) ? F[(k0 + i) + (int64_t)(k0 + j) * f.nf] : T(0);
   }
   __syncthreads();
   for (int j = 0; j < w; ++j) {
-    const double piv = A[j][j];
-    if (!(piv > 0.0)) {
+    const T piv = A[j][j];
+    if (!(piv > T(0))) {
       if (threadIdx.x == 0) atomicExch(err, 1);
       return;                                   // uniform across the CTA: piv read after a barrier
     }
-    const double d = sqrt(piv);
-    const double inv = 1.0 / d;
+    const T inv = rsqrt_t(piv);
     __syncthreads();
-    if (threadIdx.x == 0) A[j][j] = d;
+    if (threadIdx.x == 0) A[j][j] = piv * inv;
     for (int i = j + 1 + threadIdx.x; i < w; i += blockDim.x) A[i][j] *= inv;
     __syncthreads();
     for (int t = threadIdx.x; t < (w - j - 1) * (w - j - 1); t += blockDim.x) {
@@ -86,15 +99,14 @@ __global__ void k_chol_diag(const int32_t* __restrict__ lev, const FrontInfo* __
     __syncthreads();
   }
   // Invert the factored block (lower triangular) and store the INVERSE in place of the block:
-  // the panel solve and both triangular solves then multiply by it (no divisions, no serial
-  // chain on the slow FP64 pipe).  Thread j computes column j: Linv(j,j) = 1/A(j,j),
-  // Linv(i,j) = -(sum_{k=j}^{i-1} A(i,k) Linv(k,j)) / A(i,i).
-  __shared__ double Iv[kNB][kNB + 1];
+  // the panel solve and both triangular solves then multiply by it.  Thread j computes column
+  // j: Linv(j,j) = 1/A(j,j), Linv(i,j) = -(sum_{k=j}^{i-1} A(i,k) Linv(k,j)) / A(i,i).
+  __shared__ T Iv[kNB][kNB + 1];
   if (threadIdx.x < w) {
     const int j = threadIdx.x;
-    Iv[j][j] = 1.0 / A[j][j];
+    Iv[j][j] = T(1) / A[j][j];
     for (int i = j + 1; i < w; ++i) {
-      double s = 0.0;
+      T s = T(0);
       for (int k = j; k < i; ++k) s = fma(A[i][k], Iv[k][j], s);
       Iv[i][j] = -s / A[i][i];
     }
@@ -107,28 +119,29 @@ __global__ void k_chol_diag(const int32_t* __restrict__ lev, const FrontInfo* __
 }
 
 // ---- panel rows [k0+w, nf): L(r, k0:k0+w) = F(r, k0:k0+w) L11^-T
+template <typename T>
 __global__ void k_chol_panel(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                             double* const* __restrict__ Wp, int k0) {
+                             T* const* __restrict__ Wp, int k0) {
   const FrontInfo f = fr[lev[blockIdx.x]];
-  double* W = Wp[blockIdx.z];
+  T* W = Wp[blockIdx.z];
   if (f.ns <= k0) return;
   const int w = min(kNB, f.ns - k0);
   const int r = k0 + w + blockIdx.y * blockDim.x + threadIdx.x;
-  __shared__ double A[kNB][kNB + 1];
-  double* F = W + f.w_off;
+  __shared__ T A[kNB][kNB + 1];
+  T* F = W + f.w_off;
   for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
     const int i = t % w, j = t / w;
-    A[i][j] = (i >= j) ? F[(k0 + i) + (int64_t)(k0 + j) * f.nf] : 0.0;
+    A[i][j] = (i >= j) ? F[(k0 + i) + (int64_t)(k0 + j) * f.nf] : T(0);
   }
   __syncthreads();
   if (r >= f.nf) return;
   // the diagonal block holds L11^-1 (k_chol_diag): L(r, k0+j) = sum_{k <= j} F(r, k0+k) Linv(j, k)
-  double a[kNB], x[kNB];
+  T a[kNB], x[kNB];
 #pragma unroll
-  for (int j = 0; j < kNB; ++j) a[j] = j < w ? F[r + (int64_t)(k0 + j) * f.nf] : 0.0;
+  for (int j = 0; j < kNB; ++j) a[j] = j < w ? F[r + (int64_t)(k0 + j) * f.nf] : T(0);
 #pragma unroll
   for (int j = 0; j < kNB; ++j) {
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int k = 0; k < kNB; ++k)
       if (k <= j) s = fma(a[k], A[j][k], s);
@@ -140,42 +153,43 @@ __global__ void k_chol_panel(const int32_t* __restrict__ lev, const FrontInfo* _
 }
 
 // ---- trailing update F(r, c) -= sum_k L(r, k) L(c, k) for t0 <= c <= r < nf, k in [k0, k0+w)
+template <typename T>
 __global__ void __launch_bounds__(256) k_chol_update(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr,
-                                                     double* const* __restrict__ Wp, int k0) {
+                                                     T* const* __restrict__ Wp, int k0) {
   const FrontInfo f = fr[lev[blockIdx.x]];
-  double* W = Wp[blockIdx.z];
+  T* W = Wp[blockIdx.z];
   if (f.ns <= k0) return;
   const int w = min(kNB, f.ns - k0);
   const int t0 = k0 + w;
   const int m = f.nf - t0;
   if (m <= 0) return;
-  const int T = (m + kTS - 1) / kTS;
+  const int nt = (m + kTS - 1) / kTS;
   const int tile = blockIdx.y;
-  if (tile >= T * (T + 1) / 2) return;
+  if (tile >= nt * (nt + 1) / 2) return;
   // tile -> (ti, tj), ti >= tj, row-major over the lower triangle
   int ti = (int)((sqrt(8.0 * tile + 1.0) - 1.0) * 0.5);
   while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
   while (ti * (ti + 1) / 2 > tile) --ti;
   const int tj = tile - ti * (ti + 1) / 2;
   const int r0 = t0 + ti * kTS, c0 = t0 + tj * kTS;
-  __shared__ double Pr[kNB][kTS + 1];
-  __shared__ double Pc[kNB][kTS + 1];
-  double* F = W + f.w_off;
+  __shared__ T Pr[kNB][kTS + 1];
+  __shared__ T Pc[kNB][kTS + 1];
+  T* F = W + f.w_off;
   for (int t = threadIdx.x; t < kNB * kTS; t += blockDim.x) {
     const int i = t % kTS, k = t / kTS;
     const int r = r0 + i, c = c0 + i;
-    Pr[k][i] = (k < w && r < f.nf) ? F[r + (int64_t)(k0 + k) * f.nf] : 0.0;
-    Pc[k][i] = (k < w && c < f.nf) ? F[c + (int64_t)(k0 + k) * f.nf] : 0.0;
+    Pr[k][i] = (k < w && r < f.nf) ? F[r + (int64_t)(k0 + k) * f.nf] : T(0);
+    Pc[k][i] = (k < w && c < f.nf) ? F[c + (int64_t)(k0 + k) * f.nf] : T(0);
   }
   __syncthreads();
   const int tr = threadIdx.x % 16, tc = threadIdx.x / 16;   // 4x4 register block per thread
-  double acc[4][4];
+  T acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
   for (int k = 0; k < w; ++k) {
-    double ra[4], cb[4];
+    T ra[4], cb[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) ra[a] = Pr[k][tr + 16 * a];
 #pragma unroll
@@ -194,49 +208,184 @@ __global__ void __launch_bounds__(256) k_chol_update(const int32_t* __restrict__
     }
 }
 
-void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, double* const* W, cudaStream_t st) {
+// ---- whole-front factorisation in shared memory (fronts with nf <= kFusedMaxNf), one CTA per
+// (front, factor).  The CTA loads the assembled front, adds the children's update matrices and
+// factors the first ns columns right-looking.  Per column j: scale column j (its pivot's square
+// root and reciprocal were taken by the one thread that finished the pivot), barrier, rank-1
+// update of the trailing lower triangle walked as one flat index range (every lane busy),
+// barrier.  It then writes [L11; L21], the update matrix and the inverses of the 32 x 32 diagonal
+// blocks of L11 (the form the triangular solves use) back to the factor storage.
+constexpr int kFusedThreads = 256;
+
+// offset of column c in the column-major lower triangle of order m (column c holds m - c entries)
+__host__ __device__ __forceinline__ int tri_off(int c, int m) { return c * m - (c * (c - 1)) / 2; }
+
+template <typename T>
+__global__ void __launch_bounds__(kFusedThreads, 1)
+    k_chol_front(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr, const int32_t* __restrict__ relmap,
+                 T* const* __restrict__ Wp, int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char fused_raw[];
+  T* S = reinterpret_cast<T*>(fused_raw);
+  const FrontInfo f = fr[lev[blockIdx.x]];
+  T* W = Wp[blockIdx.z];
+  const int nf = f.nf, ns = f.ns;
+  T* F = W + f.w_off;
+  T* piv_s = S + nf * nf;   // pivot j before its square root
+  T* inv_s = piv_s + ns;    // 1 / L(j, j)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int nwarps = kFusedThreads / 32;
+  for (int t = tid; t < nf * nf; t += kFusedThreads) S[t] = F[t];
+  __syncthreads();
+  for (int c = 0; c < 2; ++c) {
+    const int ci = f.child[c];
+    if (ci < 0) continue;
+    const FrontInfo ch = fr[ci];
+    const int nb = ch.nb;
+    const int32_t* rm = relmap + ch.relmap_off;
+    const T* U = W + ch.w_off + ch.ns + (int64_t)ch.ns * ch.nf;   // U(a, b) = U[a + b * ch.nf]
+    for (int t = tid; t < nb * nb; t += kFusedThreads) {
+      const int a = t % nb, b = t / nb;
+      if (a >= b) S[rm[a] + rm[b] * nf] += U[a + (int64_t)b * ch.nf];
+    }
+    __syncthreads();
+  }
+  if (ns > 0 && tid == 0) {
+    piv_s[0] = S[0];
+    inv_s[0] = rsqrt_t(S[0]);
+  }
+  __syncthreads();
+  for (int j = 0; j < ns; ++j) {
+    const T piv = piv_s[j];
+    if (!(piv > T(0))) {          // uniform: every thread reads the same value after a barrier
+      if (tid == 0) atomicExch(err, 1);
+      return;
+    }
+    const T inv = inv_s[j];
+    T* colj = S + j * nf;
+    for (int i = j + tid; i < nf; i += kFusedThreads) colj[i] = (i == j) ? piv * inv : colj[i] * inv;
+    __syncthreads();
+    // S(i, k) -= L(i, j) L(k, j) for j < k <= i < nf: trailing column c = k - j - 1 holds m - c entries
+    const int m = nf - j - 1;
+    const int total = (m * (m + 1)) / 2;
+    if (tid < total) {
+      const float mf = 2.0f * m + 1.0f;
+      int c = (int)((mf - sqrtf(fmaxf(mf * mf - 8.0f * tid, 0.0f))) * 0.5f);
+      c = max(0, min(c, m - 1));
+      while (c > 0 && tri_off(c, m) > tid) --c;
+      while (c + 1 < m && tri_off(c + 1, m) <= tid) ++c;
+      int p = tid - tri_off(c, m);   // position within column c: row k + p
+      T coef = colj[j + 1 + c];
+      T* colk = S + (j + 1 + c) * nf;
+      for (;;) {
+        const int i = j + 1 + c + p;
+        colk[i] = fma(-colj[i], coef, colk[i]);
+        p += kFusedThreads;
+        if (p >= m - c) {
+          do {
+            p -= m - c;
+            ++c;
+          } while (c < m && p >= m - c);
+          if (c >= m) break;
+          coef = colj[j + 1 + c];
+          colk = S + (j + 1 + c) * nf;
+        }
+      }
+      if (tid == 0 && j + 1 < ns) {   // thread 0 owns element (j+1, j+1): the next pivot
+        const T pn = S[(j + 1) + (j + 1) * nf];
+        piv_s[j + 1] = pn;
+        inv_s[j + 1] = rsqrt_t(pn);
+      }
+    }
+    __syncthreads();
+  }
+  // lower triangle back to the factor storage, except the diagonal blocks of L11 (inverted below)
+  for (int t = tid; t < nf * nf; t += kFusedThreads) {
+    const int i = t % nf, j = t / nf;
+    if (i < j) continue;
+    if (i < ns && (i >> 5) == (j >> 5)) continue;
+    F[t] = S[t];
+  }
+  // inverses of the diagonal blocks: lane j of a warp computes column j of L_blk^-1
+  const int nblk = (ns + 31) >> 5;
+  for (int bi = warp; bi < nblk; bi += nwarps) {
+    const int k0 = bi * 32, w = min(32, ns - k0);
+    if (lane < w) {
+      const int j = lane;
+      T iv[32];
+      iv[j] = inv_s[k0 + j];
+      F[(k0 + j) + (int64_t)(k0 + j) * nf] = iv[j];
+      for (int i = j + 1; i < w; ++i) {
+        T acc = T(0);
+        for (int k = j; k < i; ++k) acc = fma(S[(k0 + i) + (k0 + k) * nf], iv[k], acc);
+        iv[i] = -acc * inv_s[k0 + i];
+        F[(k0 + i) + (int64_t)(k0 + j) * nf] = iv[i];
+      }
+    }
+  }
+}
+
+template <typename T>
+static size_t fused_smem_bytes(int max_nf, int max_ns) {
+  return ((size_t)max_nf * max_nf + 2 * (size_t)max_ns) * sizeof(T);
+}
+
+template <typename T>
+void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* const* W, cudaStream_t st) {
   if (s.nfronts == 0 || nfac == 0) return;
   VH_REQUIRE(nfac <= 65535, ERR_BAD_ARG, "too many factors in one batch");
   int* d_err = s.d_err;
-  double** tab = nullptr;   // device: [D pointers | W pointers]
-  VH_CUDA_TRY(cudaMalloc(&tab, 2 * (size_t)nfac * sizeof(double*)));
-  std::vector<double*> h(2 * (size_t)nfac);
+  void** tab = nullptr;   // device: [D pointers | W pointers]
+  VH_CUDA_TRY(cudaMalloc(&tab, 2 * (size_t)nfac * sizeof(void*)));
+  std::vector<void*> h(2 * (size_t)nfac);
   for (int i = 0; i < nfac; ++i) {
     h[i] = const_cast<double*>(D[i]);
     h[nfac + i] = W[i];
   }
   try {
-    VH_CUDA_TRY(cudaMemcpyAsync(tab, h.data(), h.size() * sizeof(double*), cudaMemcpyHostToDevice, st));
-    const double* const* Dp = tab;
-    double* const* Wp = tab + nfac;
+    VH_CUDA_TRY(cudaMemcpyAsync(tab, h.data(), h.size() * sizeof(void*), cudaMemcpyHostToDevice, st));
+    const double* const* Dp = reinterpret_cast<const double* const*>(tab);
+    T* const* Wp = reinterpret_cast<T* const*>(tab + nfac);
     VH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-    for (int i = 0; i < nfac; ++i) VH_CUDA_TRY(cudaMemsetAsync(W[i], 0, s.w_total * sizeof(double), st));
+    for (int i = 0; i < nfac; ++i) VH_CUDA_TRY(cudaMemsetAsync(W[i], 0, s.w_total * sizeof(T), st));
     const unsigned nz = (unsigned)nfac;
-    k_chol_assemble<<<dim3(s.nfronts, 1, nz), 256, 0, st>>>(s.d_fronts, s.d_asm, s.d_asm_q, s.d_asm_c, Dp, Wp);
+    k_chol_assemble<T><<<dim3(s.nfronts, 1, nz), 256, 0, st>>>(s.d_fronts, s.d_asm, s.d_asm_q, s.d_asm_c, Dp, Wp);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
+    size_t fused_max = 0;
+    for (size_t hl = 0; hl < s.levels.size(); ++hl)
+      fused_max = std::max(fused_max, fused_smem_bytes<T>(s.fused_max_nf[hl], s.fused_max_ns[hl]));
+    if (fused_max > 0)
+      VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_front<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_max));
     for (size_t hl = 0; hl < s.levels.size(); ++hl) {
-      const unsigned nf = (unsigned)s.levels[hl].size();
-      const int32_t* lev = s.d_levels[hl];
+      if (!s.levels_fused[hl].empty()) {
+        const size_t sm = fused_smem_bytes<T>(s.fused_max_nf[hl], s.fused_max_ns[hl]);
+        k_chol_front<T><<<dim3((unsigned)s.levels_fused[hl].size(), 1, nz), kFusedThreads, sm, st>>>(
+            s.d_levels_fused[hl], s.d_fronts, s.d_relmap, Wp, d_err);
+        count_launch();
+        VH_CUDA_TRY(cudaGetLastError());
+      }
+      if (s.levels_blocked[hl].empty()) continue;
+      const unsigned nf = (unsigned)s.levels_blocked[hl].size();
+      const int32_t* lev = s.d_levels_blocked[hl];
       if (hl > 0) {
-        const unsigned cy = (unsigned)std::min(1024, std::max(1, s.level_max_nf[hl]));
+        const unsigned cy = (unsigned)std::min(1024, std::max(1, s.blocked_max_nf[hl]));
         for (int which = 0; which < 2; ++which) {
-          k_chol_extend_add<<<dim3(nf, cy, nz), 128, 0, st>>>(lev, s.d_fronts, s.d_relmap, Wp, which);
+          k_chol_extend_add<T><<<dim3(nf, cy, nz), 128, 0, st>>>(lev, s.d_fronts, s.d_relmap, Wp, which);
           count_launch();
           VH_CUDA_TRY(cudaGetLastError());
         }
       }
-      const int max_ns = s.level_max_ns[hl];
-      const int max_nf = s.level_max_nf[hl];
+      const int max_ns = s.blocked_max_ns[hl];
+      const int max_nf = s.blocked_max_nf[hl];
       for (int k0 = 0; k0 < max_ns; k0 += kNB) {
-        k_chol_diag<<<dim3(nf, 1, nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0, d_err);
+        k_chol_diag<T><<<dim3(nf, 1, nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0, d_err);
         count_launch();
         const int rows = max_nf - k0;
         if (rows > 0) {
-          k_chol_panel<<<dim3(nf, (unsigned)ceil_div(rows, 128), nz), 128, 0, st>>>(lev, s.d_fronts, Wp, k0);
+          k_chol_panel<T><<<dim3(nf, (unsigned)ceil_div(rows, 128), nz), 128, 0, st>>>(lev, s.d_fronts, Wp, k0);
           count_launch();
-          const int T = (int)ceil_div(rows, kTS);
-          k_chol_update<<<dim3(nf, (unsigned)(T * (T + 1) / 2), nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0);
+          const int nt = (int)ceil_div(rows, kTS);
+          k_chol_update<T><<<dim3(nf, (unsigned)(nt * (nt + 1) / 2), nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0);
           count_launch();
         }
         VH_CUDA_TRY(cudaGetLastError());
@@ -254,41 +403,41 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, double
 }
 
 // ---- triangular solves.  One warp per (front, RHS), kSolveWarps warps per CTA.  Each front's
-// dense triangle is processed in blocks of 32 columns: the 32 x 32 diagonal block is solved from
-// shared memory with warp shuffles (lane i owns row i of the block); the rest is coalesced
-// column-major GEMV / dot work whose loads are independent of one another.
+// dense triangle is processed in blocks of 32 columns: the 32 x 32 diagonal block is applied as
+// its stored inverse (lane i owns row i of the block); the rest is coalesced column-major GEMV /
+// dot work whose loads are independent of one another.
 constexpr int kSolveWarps = 4;
 constexpr int kBlk = 32;
 
+template <typename T>
 struct SolveSmem {
+  using C = cplx<T>;
+  static __host__ __device__ size_t vec_bytes(int max_nf) { return ((size_t)max_nf * sizeof(C) + 15) & ~(size_t)15; }
   static __host__ __device__ size_t per_warp(int max_nf) {
-    return (((size_t)max_nf * sizeof(double2) + 15) & ~(size_t)15) + kBlk * (kBlk + 1) * sizeof(double) +
-           kBlk * sizeof(double2);
+    return vec_bytes(max_nf) + kBlk * (kBlk + 1) * sizeof(T) + kBlk * sizeof(C);
   }
 };
 
-__device__ __forceinline__ double2 shfl_c(double2 v, int src) {
-  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
-}
-
+template <typename T>
 __global__ void __launch_bounds__(32 * kSolveWarps)
     k_chol_fsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
-                  const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, double* const* __restrict__ Wp,
-                  double2* __restrict__ x, int64_t ldx, int64_t xoff, double2* __restrict__ U, int64_t u_total,
+                  const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, T* const* __restrict__ Wp,
+                  cplx<T>* __restrict__ x, int64_t ldx, int64_t xoff, cplx<T>* __restrict__ U, int64_t u_total,
                   int max_nf) {
+  using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
   if (item >= (int64_t)nlev * B) return;
-  unsigned char* base = smem_raw + warp * SolveSmem::per_warp(max_nf);
-  double2* t = reinterpret_cast<double2*>(base);
-  double(*Lb)[kBlk + 1] = reinterpret_cast<double(*)[kBlk + 1]>(base + (((size_t)max_nf * sizeof(double2) + 15) & ~(size_t)15));
-  double2* yb = reinterpret_cast<double2*>(reinterpret_cast<unsigned char*>(Lb) + kBlk * (kBlk + 1) * sizeof(double));
+  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp(max_nf);
+  C* t = reinterpret_cast<C*>(base);
+  T(*Lb)[kBlk + 1] = reinterpret_cast<T(*)[kBlk + 1]>(base + SolveSmem<T>::vec_bytes(max_nf));
+  C* yb = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(Lb) + kBlk * (kBlk + 1) * sizeof(T));
   const FrontInfo f = fr[lev[item % nlev]];
   const int b = (int)(item / nlev);
-  const double* F = Wp[b] + f.w_off;
-  double2* xb = x + b * ldx + xoff;
-  double2* Ub = U + b * u_total;
+  const T* F = Wp[b] + f.w_off;
+  C* xb = x + b * ldx + xoff;
+  C* Ub = U + b * u_total;
   const int32_t* rw = rows + f.rows_off;
   const int nf = f.nf, ns = f.ns;
   // gathers: 4 independent index loads, then 4 independent value loads per lane
@@ -298,7 +447,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     for (int u = 0; u < 4; ++u) ix[u] = (r0 + 32 * u < ns) ? rw[r0 + 32 * u] : -1;
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      if (r0 + 32 * u < nf) t[r0 + 32 * u] = ix[u] >= 0 ? xb[ix[u]] : make_double2(0.0, 0.0);
+      if (r0 + 32 * u < nf) t[r0 + 32 * u] = ix[u] >= 0 ? xb[ix[u]] : czero<C>();
   }
   __syncwarp();
   for (int c = 0; c < 2; ++c) {
@@ -307,12 +456,12 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     const int32_t* rm = relmap + ch.relmap_off;
     for (int a0 = lane; a0 < ch.nb; a0 += 128) {
       int32_t ix[4];
-      double2 u[4];
+      C u[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int a = a0 + 32 * q;
         ix[q] = a < ch.nb ? rm[a] : -1;
-        u[q] = a < ch.nb ? Ub[ch.u_off + a] : make_double2(0.0, 0.0);
+        u[q] = a < ch.nb ? Ub[ch.u_off + a] : czero<C>();
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q)
@@ -325,17 +474,17 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   }
   for (int j0 = 0; j0 < ns; j0 += kBlk) {
     const int w = min(kBlk, ns - j0);
-    // the diagonal block holds L_blk^-1 (k_chol_diag): y_blk = L_blk^-1 t_blk, lane i owns row i
+    // the diagonal block holds L_blk^-1: y_blk = L_blk^-1 t_blk, lane i owns row i
 #pragma unroll
     for (int k = 0; k < kBlk; ++k)
-      Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
-    yb[lane] = lane < w ? t[j0 + lane] : make_double2(0.0, 0.0);   // every lane: yb is read for all 32 k
+      Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
+    yb[lane] = lane < w ? t[j0 + lane] : czero<C>();   // every lane: yb is read for all 32 k
     __syncwarp();
-    double2 tv = make_double2(0.0, 0.0);
+    C tv = czero<C>();
 #pragma unroll
     for (int k = 0; k < kBlk; ++k) {
       if (k < w) {
-        const double l = Lb[lane][k];
+        const T l = Lb[lane][k];
         tv.x = fma(l, yb[k].x, tv.x);
         tv.y = fma(l, yb[k].y, tv.y);
       }
@@ -345,11 +494,11 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     yb[lane] = tv;   // zero for lanes >= w (their Lb rows are zero); the GEMV below reads all 32
     __syncwarp();
     for (int r = j0 + w + lane; r < nf; r += 32) {
-      double ax = 0.0, ay = 0.0;
-      const double* Lr = F + r + (int64_t)j0 * nf;
-      double lv[kBlk];
+      T ax = T(0), ay = T(0);
+      const T* Lr = F + r + (int64_t)j0 * nf;
+      T lv[kBlk];
 #pragma unroll
-      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : 0.0;   // independent loads
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : T(0);   // independent loads
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) {
         ax = fma(lv[k], yb[k].x, ax);
@@ -362,26 +511,31 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   }
   for (int j = lane; j < ns; j += 32) xb[rw[j]] = t[j];
   for (int a = lane; a < f.nb; a += 32) {
-    const double2 v = t[ns + a];
-    Ub[f.u_off + a] = make_double2(-v.x, -v.y);
+    const C v = t[ns + a];
+    C nv;
+    nv.x = -v.x;
+    nv.y = -v.y;
+    Ub[f.u_off + a] = nv;
   }
 }
 
+template <typename T>
 __global__ void __launch_bounds__(32 * kSolveWarps)
     k_chol_bsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
-                  const int32_t* __restrict__ rows, double* const* __restrict__ Wp, double2* __restrict__ x,
-                  int64_t ldx, int64_t xoff, int max_nf) {
+                  const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x, int64_t ldx,
+                  int64_t xoff, int max_nf) {
+  using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
   if (item >= (int64_t)nlev * B) return;
-  unsigned char* base = smem_raw + warp * SolveSmem::per_warp(max_nf);
-  double2* t = reinterpret_cast<double2*>(base);
-  double(*Lb)[kBlk + 1] = reinterpret_cast<double(*)[kBlk + 1]>(base + (((size_t)max_nf * sizeof(double2) + 15) & ~(size_t)15));
+  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp(max_nf);
+  C* t = reinterpret_cast<C*>(base);
+  T(*Lb)[kBlk + 1] = reinterpret_cast<T(*)[kBlk + 1]>(base + SolveSmem<T>::vec_bytes(max_nf));
   const FrontInfo f = fr[lev[item % nlev]];
   const int b = (int)(item / nlev);
-  const double* F = Wp[b] + f.w_off;
-  double2* xb = x + b * ldx + xoff;
+  const T* F = Wp[b] + f.w_off;
+  C* xb = x + b * ldx + xoff;
   const int32_t* rw = rows + f.rows_off;
   const int nf = f.nf, ns = f.ns;
   // own rows: y; boundary rows: final x (4 independent index loads, then value loads, per lane)
@@ -397,11 +551,11 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   // z_own -= L21^T x_bnd, column-oriented: lane j walks its own column (contiguous rows, no
   // cross-lane reductions)
   for (int j = lane; j < ns; j += 32) {
-    const double* col = F + (int64_t)j * nf;
-    double sx = 0.0, sy = 0.0;
+    const T* col = F + (int64_t)j * nf;
+    T sx = T(0), sy = T(0);
     int r = ns;
     for (; r + 4 <= nf; r += 4) {
-      double lv[4];
+      T lv[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) lv[u] = col[r + u];
 #pragma unroll
@@ -411,7 +565,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
       }
     }
     for (; r < nf; ++r) {
-      const double l = col[r];
+      const T l = col[r];
       sx = fma(l, t[r].x, sx);
       sy = fma(l, t[r].y, sy);
     }
@@ -426,14 +580,14 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     // x_blk = L_blk^-T z_blk with the stored inverse (lower): lane i: x_i = sum_{k >= i} Linv(k, i) z_k
 #pragma unroll
     for (int k = 0; k < kBlk; ++k)
-      Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : 0.0;
+      Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
     __syncwarp();
-    double2 xv = make_double2(0.0, 0.0);
+    C xv = czero<C>();
 #pragma unroll
     for (int k = 0; k < kBlk; ++k) {
       if (k < w) {
-        const double l = Lb[k][lane];
-        const double2 zk = t[j0 + k];
+        const T l = Lb[k][lane];
+        const C zk = t[j0 + k];
         xv.x = fma(l, zk.x, xv.x);
         xv.y = fma(l, zk.y, xv.y);
       }
@@ -443,11 +597,11 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     __syncwarp();
     // z_j -= sum_{r in block} L(r, j) x_r for the own columns j < j0 (lane per column)
     for (int j = lane; j < j0; j += 32) {
-      const double* col = F + (int64_t)j * nf + j0;
-      double lv[kBlk];
+      const T* col = F + (int64_t)j * nf + j0;
+      T lv[kBlk];
 #pragma unroll
-      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? col[k] : 0.0;
-      double sx = 0.0, sy = 0.0;
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? col[k] : T(0);
+      T sx = T(0), sy = T(0);
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) {
         if (k < w) {
@@ -463,33 +617,41 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   for (int j = lane; j < ns; j += 32) xb[rw[j]] = t[j];
 }
 
-void chol_solve(const CholSymbolic& s, int B, double* const* Wp, double2* x, int64_t ldx, int64_t xoff, double2* U,
+template <typename T>
+void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t ldx, int64_t xoff, cplx<T>* U,
                 cudaStream_t st) {
   if (s.nfronts == 0 || B == 0) return;
-  const size_t sm_max = kSolveWarps * SolveSmem::per_warp(s.max_nf);
+  const size_t sm_max = kSolveWarps * SolveSmem<T>::per_warp(s.max_nf);
   VH_REQUIRE(sm_max <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();
     const int mnf = s.level_max_nf[h];
-    const size_t smh = kSolveWarps * SolveSmem::per_warp(mnf);
+    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
-    k_chol_fsolve<<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows, s.d_relmap, Wp, x,
-                                                        ldx, xoff, U, s.u_total, mnf);
+    k_chol_fsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows, s.d_relmap,
+                                                           Wp, x, ldx, xoff, U, s.u_total, mnf);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   for (size_t hh = s.levels.size(); hh-- > 0;) {
     const int nlev = (int)s.levels[hh].size();
     const int mnf = s.level_max_nf[hh];
-    const size_t smh = kSolveWarps * SolveSmem::per_warp(mnf);
+    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
-    k_chol_bsolve<<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp, x, ldx,
-                                                        xoff, mnf);
+    k_chol_bsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp, x, ldx,
+                                                           xoff, mnf);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
 }
+
+template void chol_factor<double>(const CholSymbolic&, int, const double* const*, double* const*, cudaStream_t);
+template void chol_solve<double>(const CholSymbolic&, int, double* const*, double2*, int64_t, int64_t, double2*,
+                                 cudaStream_t);
+template void chol_factor<dfloat>(const CholSymbolic&, int, const double* const*, dfloat* const*, cudaStream_t);
+template void chol_solve<dfloat>(const CholSymbolic&, int, dfloat* const*, dcomplex*, int64_t, int64_t, dcomplex*,
+                                 cudaStream_t);
 
 }  // namespace vh

@@ -13,6 +13,9 @@
 
 namespace vh {
 
+// Fronts of at most this order are factored by one CTA with the whole front in shared memory.
+constexpr int kFusedMaxNf = 160;
+
 struct FrontInfo {
   int32_t ns;          // pivots (own panels)
   int32_t nb;          // boundary rows
@@ -44,6 +47,9 @@ struct CholSymbolic {
   std::vector<FrontInfo> fronts;
   std::vector<std::vector<int32_t>> levels;  // fronts per height (leaves first)
   std::vector<int32_t> level_max_ns, level_max_nf;
+  // per height, the fronts factored whole in shared memory (nf <= kFusedMaxNf) and the others
+  std::vector<std::vector<int32_t>> levels_fused, levels_blocked;
+  std::vector<int32_t> fused_max_ns, fused_max_nf, blocked_max_ns, blocked_max_nf;
   // device copies
   FrontInfo* d_fronts = nullptr;
   int32_t* d_rows = nullptr;
@@ -52,6 +58,7 @@ struct CholSymbolic {
   int32_t* d_asm_q = nullptr;
   double* d_asm_c = nullptr;
   std::vector<int32_t*> d_levels;   // per height: front ids
+  std::vector<int32_t*> d_levels_fused, d_levels_blocked;
   int* d_err = nullptr;             // factorisation status flag
   int64_t n_asm = 0;
   void free_all();
@@ -66,13 +73,16 @@ void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64
                    int leaf_size, cudaStream_t st, bool to_device = true);
 
 // Numeric factorisation of `nfac` factors at once (one per frequency): factor i goes to W[i]
-// (sym.w_total doubles, device) from the diagonal D[i] = A_inv (nc reals, device).  The pointer
-// arrays are host arrays.
-void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, double* const* W, cudaStream_t st);
+// (sym.w_total values of T, device) from the diagonal D[i] = A_inv (nc doubles, device).  The
+// pointer arrays are host arrays.  T = double, or dfloat (FP32 pairs) for the mixed-precision solver.
+template <typename T>
+void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* const* W, cudaStream_t st);
 
-// Solves S x = b in place for B right-hand sides.  x: device, complex, RHS b at x + b*ldx + xoff
-// (panel indexing); Wp: device array of B factor pointers; U: device scratch of B * u_total complex.
-void chol_solve(const CholSymbolic& s, int B, double* const* Wp, double2* x, int64_t ldx, int64_t xoff, double2* U,
+// Solves S x = b in place for B right-hand sides in the factor's precision.  x: device, complex of
+// T, RHS b at x + b*ldx + xoff (panel indexing); Wp: device array of B factor pointers; U: device
+// scratch of B * u_total complex values of T.
+template <typename T>
+void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t ldx, int64_t xoff, cplx<T>* U,
                 cudaStream_t st);
 
 }  // namespace vh

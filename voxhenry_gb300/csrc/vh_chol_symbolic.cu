@@ -24,6 +24,10 @@ void CholSymbolic::free_all() {
   cudaFree(d_asm_q);
   cudaFree(d_asm_c);
   for (auto* p : d_levels) cudaFree(p);
+  for (auto* p : d_levels_fused) cudaFree(p);
+  for (auto* p : d_levels_blocked) cudaFree(p);
+  d_levels_fused.clear();
+  d_levels_blocked.clear();
   cudaFree(d_err);
   d_err = nullptr;
   d_levels.clear();
@@ -307,6 +311,23 @@ void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64
       s.level_max_ns[h] = std::max(s.level_max_ns[h], s.fronts[f].ns);
       s.level_max_nf[h] = std::max(s.level_max_nf[h], s.fronts[f].nf);
     }
+  const size_t nh = s.levels.size();
+  s.levels_fused.assign(nh, {});
+  s.levels_blocked.assign(nh, {});
+  s.fused_max_ns.assign(nh, 0);
+  s.fused_max_nf.assign(nh, 0);
+  s.blocked_max_ns.assign(nh, 0);
+  s.blocked_max_nf.assign(nh, 0);
+  for (size_t h = 0; h < nh; ++h)
+    for (int f : s.levels[h]) {
+      const FrontInfo& fi = s.fronts[f];
+      const bool fused = fi.nf <= kFusedMaxNf;
+      (fused ? s.levels_fused : s.levels_blocked)[h].push_back(f);
+      int32_t& mns = (fused ? s.fused_max_ns : s.blocked_max_ns)[h];
+      int32_t& mnf = (fused ? s.fused_max_nf : s.blocked_max_nf)[h];
+      mns = std::max(mns, fi.ns);
+      mnf = std::max(mnf, fi.nf);
+    }
   s.nfronts = nfr;
   s.w_total = w_off;
   s.u_total = u_off;
@@ -334,6 +355,12 @@ void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64
   upload(s.d_asm_c, asm_c, st);
   s.d_levels.assign(s.levels.size(), nullptr);
   for (size_t h = 0; h < s.levels.size(); ++h) upload(s.d_levels[h], s.levels[h], st);
+  s.d_levels_fused.assign(nh, nullptr);
+  s.d_levels_blocked.assign(nh, nullptr);
+  for (size_t h = 0; h < nh; ++h) {
+    if (!s.levels_fused[h].empty()) upload(s.d_levels_fused[h], s.levels_fused[h], st);
+    if (!s.levels_blocked[h].empty()) upload(s.d_levels_blocked[h], s.levels_blocked[h], st);
+  }
   VH_CUDA_TRY(cudaMalloc(&s.d_err, sizeof(int)));
   VH_CUDA_TRY(cudaStreamSynchronize(st));
 }

@@ -1,0 +1,104 @@
+// Double-float ("float-float") arithmetic: a value is the unevaluated sum hi + lo of two floats
+// with |lo| <= ulp(hi) / 2, about 48 significant bits (unit roundoff ~ 2^-47).  GB300 issues FP32
+// at 64 times its FP64 rate, so a double-float multiply-add (about 14 FP32 instructions) costs a
+// quarter of the FP64 pipe time of one DFMA; the mixed-precision solver uses it for the Schur
+// factor and its triangular solves, where FP32 alone is far too inaccurate for the condition of S.
+//
+// Algorithms (published, restated here): Knuth's TwoSum and Dekker's Fast2Sum for exact sums,
+// the FMA form of Dekker's TwoProduct for exact products (Dekker 1971, "A floating-point technique
+// for extending the available precision"); the pair operations follow the "sloppy" double-double
+// add and the standard product of Hida, Li and Bailey's double-double arithmetic.  Every elementary
+// step uses the _rn intrinsics so that the compiler cannot contract or reassociate it.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "vh_common.cuh"
+
+namespace vh {
+
+using ::fma;   // keep the FP64 / FP32 overloads visible next to the pair overload below
+
+struct dfloat {
+  float hi, lo;
+  dfloat() = default;
+  __host__ __device__ constexpr dfloat(float h) : hi(h), lo(0.0f) {}
+  __host__ __device__ constexpr dfloat(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr dfloat(int v) : hi((float)v), lo(0.0f) {}
+  // nearest pair to a double: hi = rn(d), lo = rn(d - hi) (d - hi is exact in double)
+  __host__ __device__ explicit dfloat(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  __host__ __device__ double to_double() const { return (double)hi + (double)lo; }
+};
+
+struct dcomplex {
+  dfloat x, y;
+};
+template <> struct cplx_t<dfloat> { using type = dcomplex; };
+
+__device__ __forceinline__ dcomplex to_c(double2 a, dcomplex) { return dcomplex{dfloat(a.x), dfloat(a.y)}; }
+__device__ __forceinline__ double2 to_d(dcomplex a) { return make_double2(a.x.to_double(), a.y.to_double()); }
+
+// s + e = a + b exactly (Knuth)
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// s + e = a + b exactly when |a| >= |b| or a == 0 (Dekker)
+__device__ __forceinline__ void df_fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
+  float s, e;
+  df_two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  dfloat r;
+  df_fast_two_sum(s, e, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
+__device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);                       // exact error of a.hi * b.hi
+  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+  dfloat r;
+  df_fast_two_sum(p, e, r.hi, r.lo);
+  return r;
+}
+// a * b + c with one rounding to the pair format
+__device__ __forceinline__ dfloat fma(dfloat a, dfloat b, dfloat c) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+  float s, t;
+  df_two_sum(p, c.hi, s, t);
+  t = __fadd_rn(t, __fadd_rn(e, c.lo));
+  dfloat r;
+  df_fast_two_sum(s, t, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ dfloat& operator+=(dfloat& a, dfloat b) { return a = a + b; }
+__device__ __forceinline__ dfloat& operator-=(dfloat& a, dfloat b) { return a = a - b; }
+__device__ __forceinline__ dfloat& operator*=(dfloat& a, dfloat b) { return a = a * b; }
+__device__ __forceinline__ bool operator>(dfloat a, dfloat b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+
+// 1 / b: single-precision seed, then two Newton steps y <- y + y (1 - b y), each in pair arithmetic
+__device__ __forceinline__ dfloat df_recip(dfloat b) {
+  dfloat y(__frcp_rn(b.hi));
+  const dfloat one(1.0f);
+  for (int it = 0; it < 2; ++it) y = fma(y, one - b * y, y);
+  return y;
+}
+__device__ __forceinline__ dfloat operator/(dfloat a, dfloat b) { return a * df_recip(b); }
+
+// 1 / sqrt(p): single-precision seed, then two Newton steps y <- y + y (1 - p y^2) / 2
+__device__ __forceinline__ dfloat df_rsqrt(dfloat p) {
+  dfloat y(rsqrtf(p.hi));
+  const dfloat one(1.0f), half(0.5f);
+  for (int it = 0; it < 2; ++it) y = fma(y * half, one - p * y * y, y);
+  return y;
+}
+
+}  // namespace vh

@@ -581,9 +581,11 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
   // |M^-1 b|
   M(all, b, S.p);
   std::vector<double> mb = row_norms(S.p, n, all, n, d_rows, partr, nrm, st);
+  const std::vector<double> bnorm = row_norms(b, n, all, n, d_rows, partr, nrm, st);
   std::vector<int> active = all;
   VH_CUDA_TRY(cudaMemcpyAsync(R.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-  std::vector<double> sn = mb;   // |M^-1 r| with x = 0
+  std::vector<double> sn = mb;      // |M^-1 r| with x = 0
+  std::vector<double> rn = bnorm;   // |r| with x = 0
   for (int i = 0; i < B; ++i) out.resvec[i].push_back(1.0);
   for (int step = 0; step < max_refine && !active.empty(); ++step) {
     const int na = (int)active.size();
@@ -604,7 +606,8 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       sc[a] = scale_h ? scale_h[bb] : make_double2(1.0, 0.0);
       zs[a] = zslot_h ? zslot_h[bb] : 0;
       // ask the inner solve for what is still missing, but not below its precision floor
-      tl[a] = std::max(inner_tol, 0.5 * tol[bb] * mb[bb] / std::max(sn[bb], 1e-300));
+      tl[a] = std::max(inner_tol, 0.5 * std::min(tol[bb] * mb[bb] / std::max(sn[bb], 1e-300),
+                                                 tol[bb] * bnorm[bb] / std::max(rn[bb], 1e-300)));
       ps[a] = pcs ? pcs[bb] : nullptr;
     }
     // M^-1 r of the active rows (kept from the last check) seeds the inner solve
@@ -646,6 +649,7 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       for (int a = 0; a < na; ++a) seq[a] = a;
       M(active, Ya.p, Sa.p);
       std::vector<double> snorm = row_norms(Sa.p, n, seq, n, d_rows, partr, nrm, st);
+      const std::vector<double> rnorm = row_norms(Ya.p, n, seq, n, d_rows, partr, nrm, st);
       // scatter residuals (and their preconditioned form) back
       for (int a = 0; a < na; ++a) {
         VH_CUDA_TRY(cudaMemcpyAsync(R.p + (int64_t)active[a] * n, Ya.p + (int64_t)a * n, n * sizeof(double2),
@@ -657,8 +661,12 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       for (int a = 0; a < na; ++a) {
         const int bb = active[a];
         sn[bb] = snorm[a];
+        rn[bb] = rnorm[a];
         out.resvec[bb].push_back(snorm[a] / mb[bb]);
-        if (snorm[a] > tol[bb] * mb[bb]) still.push_back(bb);
+        // refine until both the preconditioned and the true FP64 residual meet tol: a single-precision
+        // Schur factor weighs the residual differently from the exact one, and the true residual is
+        // what the flag (pgmres.m:182-186) and the result's accuracy depend on
+        if (snorm[a] > tol[bb] * mb[bb] || rnorm[a] > tol[bb] * bnorm[bb]) still.push_back(bb);
       }
     }
     active.swap(still);

@@ -64,7 +64,9 @@ struct vh_geom {
   bool has_conv = false;           // false for a preconditioner-only geometry (no tensor)
   vh::CholSymbolic chol;           // built on the first 'schur_invert' preconditioner
   bool chol_ready = false;
-  double2* pc_tmp = nullptr;       // chol_solve update vectors, B * u_total
+  double2* pc_tmp = nullptr;       // chol_solve update vectors, B * u_total (16-byte complex values)
+  void* pc_phi_df = nullptr;       // double-float factor: B * nphi pair-complex panel values being solved
+  size_t pc_phi_df_cap = 0;
   size_t pc_tmp_cap = 0;
   double** pc_ptrs = nullptr;      // device pointer tables (A_inv, W) for batched applies
   int pc_ptrs_cap = 0;

@@ -8,13 +8,15 @@
 #include <vector>
 
 #include "../../include/voxhenry_gpu.h"
+#include "vh_df.cuh"
 #include "vh_internal.cuh"
 
 struct vh_precon {
   vh_geom* g = nullptr;
   int kind = 0;
+  bool df = false;           // factor and triangular solves in double-float (VH_PRECON_SCHUR_INVERT_DF)
   double* A_inv = nullptr;   // nc reals
-  double* W = nullptr;       // factor storage
+  void* W = nullptr;         // factor storage: w_total doubles, or w_total FP32 pairs when `df`
 };
 
 namespace vh {
@@ -40,10 +42,13 @@ __global__ void k_a_inv(const double2* __restrict__ z, int64_t nv, double dx, do
   }
 }
 
-// y_phi[b] = x_phi[b] - Ar (A_inv_b .* x_J[b])
+// phi[b] = x_phi[b] - Ar (A_inv_b .* x_J[b]), stored as C: complex128 in place in y, or the
+// pair-complex vector of a double-float factor; RHS b at phi + b * ldphi
+template <typename C>
 __global__ void k_precon_rhs(int64_t nphi, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
                              const double* __restrict__ val, double* const* __restrict__ ainv,
-                             const double2* __restrict__ x, double2* __restrict__ y, int64_t ld, int64_t nc) {
+                             const double2* __restrict__ x, int64_t ld, int64_t nc, C* __restrict__ phi,
+                             int64_t ldphi) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
   if (r >= nphi) return;
@@ -56,26 +61,32 @@ __global__ void k_precon_rhs(int64_t nphi, const int32_t* __restrict__ rp, const
     acc.x -= a * xb[q].x;
     acc.y -= a * xb[q].y;
   }
-  y[b * ld + nc + r] = acc;
+  phi[b * ldphi + r] = to_c(acc, C());
 }
 
-// y_J[b] = (x_J[b] + Ar^T y_phi[b]) .* A_inv_b
-__global__ void k_precon_finish(int64_t nc, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
-                                const double* __restrict__ val, double* const* __restrict__ ainv,
-                                const double2* __restrict__ x, double2* __restrict__ y, int64_t ld) {
+// y_J[b] = (x_J[b] + Ar^T phi[b]) .* A_inv_b;  y_phi[b] = phi[b] when phi is not y's own storage
+template <typename C>
+__global__ void k_precon_finish(int64_t nc, int64_t nphi, const int32_t* __restrict__ rp,
+                                const int32_t* __restrict__ col, const double* __restrict__ val,
+                                double* const* __restrict__ ainv, const double2* __restrict__ x,
+                                double2* __restrict__ y, int64_t ld, const C* __restrict__ phi, int64_t ldphi,
+                                bool copy_phi) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
-  if (q >= nc) return;
-  const double2* yb = y + b * ld + nc;
-  double2 acc = x[b * ld + q];
-  for (int32_t k = rp[q]; k < rp[q + 1]; ++k) {
-    const double a = val[k];
-    const double2 v = yb[col[k]];
-    acc.x = fma(a, v.x, acc.x);
-    acc.y = fma(a, v.y, acc.y);
+  const C* pb = phi + b * ldphi;
+  if (q < nc) {
+    double2 acc = x[b * ld + q];
+    for (int32_t k = rp[q]; k < rp[q + 1]; ++k) {
+      const double a = val[k];
+      const double2 v = to_d(pb[col[k]]);
+      acc.x = fma(a, v.x, acc.x);
+      acc.y = fma(a, v.y, acc.y);
+    }
+    const double s = ainv[b][q];
+    y[b * ld + q] = make_double2(acc.x * s, acc.y * s);
+  } else if (copy_phi && q < nc + nphi) {
+    y[b * ld + q] = to_d(pb[q - nc]);
   }
-  const double s = ainv[b][q];
-  y[b * ld + q] = make_double2(acc.x * s, acc.y * s);
 }
 
 void ensure_symbolic(vh_geom* g) {
@@ -106,15 +117,17 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
     VH_CUDA_TRY(cudaMalloc(&g->pc_ptrs, 2 * (size_t)B * sizeof(double*)));
     g->pc_ptrs_cap = B;
   }
-  std::vector<double*> h(2 * (size_t)B);
+  const bool df = pcs[0]->df;
+  for (int b = 0; b < B; ++b)
+    VH_REQUIRE(pcs[b]->df == df, ERR_BAD_ARG, "mixed factor precisions in one batch");
+  std::vector<void*> h(2 * (size_t)B);
   for (int b = 0; b < B; ++b) {
     h[b] = pcs[b]->A_inv;
     h[B + b] = pcs[b]->W;
   }
   double** d_ainv = g->pc_ptrs;
-  double** d_w = g->pc_ptrs + B;
-  VH_CUDA_TRY(cudaMemcpyAsync(g->pc_ptrs, h.data(), 2 * (size_t)B * sizeof(double*), cudaMemcpyHostToDevice, st));
-  const size_t need = (size_t)B * std::max<int64_t>(1, g->chol.u_total);
+  VH_CUDA_TRY(cudaMemcpyAsync(g->pc_ptrs, h.data(), 2 * (size_t)B * sizeof(void*), cudaMemcpyHostToDevice, st));
+  const size_t need = (size_t)B * std::max<int64_t>(1, g->chol.u_total);   // 16-byte complex values
   if (need > g->pc_tmp_cap) {
     cudaFree(g->pc_tmp);
     g->pc_tmp = nullptr;
@@ -122,16 +135,44 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
     VH_CUDA_TRY(cudaMalloc(&g->pc_tmp, need * sizeof(double2)));
     g->pc_tmp_cap = need;
   }
-  if (g->nphi > 0) {
-    k_precon_rhs<<<dim3((unsigned)ceil_div(g->nphi, 256), B), 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val,
-                                                                           d_ainv, x, y, g->n, g->nc);
-    count_launch();
-    VH_CUDA_TRY(cudaGetLastError());
-    chol_solve(g->chol, B, d_w, y, g->n, g->nc, g->pc_tmp, st);
+  dcomplex* phi_df = nullptr;
+  if (df) {
+    const size_t nall = (size_t)B * std::max<int64_t>(1, g->nphi);
+    if (nall > g->pc_phi_df_cap) {
+      cudaFree(g->pc_phi_df);
+      g->pc_phi_df = nullptr;
+      g->pc_phi_df_cap = 0;
+      VH_CUDA_TRY(cudaMalloc(&g->pc_phi_df, nall * sizeof(dcomplex)));
+      g->pc_phi_df_cap = nall;
+    }
+    phi_df = static_cast<dcomplex*>(g->pc_phi_df);
   }
-  if (g->nc > 0) {
-    k_precon_finish<<<dim3((unsigned)ceil_div(g->nc, 256), B), 256, 0, st>>>(g->nc, g->AeT.rowptr, g->AeT.col,
-                                                                            g->AeT.val, d_ainv, x, y, g->n);
+  if (g->nphi > 0) {
+    const dim3 grid((unsigned)ceil_div(g->nphi, 256), B);
+    if (df) {
+      k_precon_rhs<dcomplex><<<grid, 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val, d_ainv, x, g->n,
+                                                   g->nc, phi_df, g->nphi);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+      chol_solve<dfloat>(g->chol, B, reinterpret_cast<dfloat* const*>(g->pc_ptrs + B), phi_df, g->nphi, 0,
+                         reinterpret_cast<dcomplex*>(g->pc_tmp), st);
+    } else {
+      k_precon_rhs<double2><<<grid, 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val, d_ainv, x, g->n,
+                                                  g->nc, y + g->nc, g->n);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+      chol_solve<double>(g->chol, B, g->pc_ptrs + B, y, g->n, g->nc, g->pc_tmp, st);
+    }
+  }
+  if (g->nc > 0 || (df && g->nphi > 0)) {
+    const int64_t rows = df ? g->nc + g->nphi : g->nc;
+    const dim3 grid((unsigned)ceil_div(rows, 256), B);
+    if (df)
+      k_precon_finish<dcomplex><<<grid, 256, 0, st>>>(g->nc, g->nphi, g->AeT.rowptr, g->AeT.col, g->AeT.val, d_ainv,
+                                                      x, y, g->n, phi_df, g->nphi, true);
+    else
+      k_precon_finish<double2><<<grid, 256, 0, st>>>(g->nc, g->nphi, g->AeT.rowptr, g->AeT.col, g->AeT.val, d_ainv,
+                                                     x, y, g->n, y + g->nc, g->n, false);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -172,20 +213,23 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
     ps[i]->kind = kind;
   }
   vh_status s = guarded_pc(g->ctx, [&] {
-    VH_REQUIRE(kind == VH_PRECON_NONE || kind == VH_PRECON_SCHUR_INVERT, ERR_UNSUPPORTED,
-               "preconditioner kind not supported (schur_approx / schur_gmres / schur_invert_original)");
+    VH_REQUIRE(kind == VH_PRECON_NONE || kind == VH_PRECON_SCHUR_INVERT || kind == VH_PRECON_SCHUR_INVERT_DF,
+               ERR_UNSUPPORTED, "preconditioner kind not supported (schur_approx / schur_gmres / schur_invert_original)");
+    const bool df = kind == VH_PRECON_SCHUR_INVERT_DF;
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     if (kind == VH_PRECON_NONE) return;
     VH_REQUIRE(st_sparse_precon, ERR_BAD_ARG, "st_sparse_precon is required");
     cudaStream_t st = g->ctx->stream;
     ensure_symbolic(g);
     std::vector<const double*> D(nfreq);
-    std::vector<double*> W(nfreq);
+    std::vector<void*> W(nfreq);
     for (int i = 0; i < nfreq; ++i) {
       const int zs = zslot ? zslot[i] : 0;
       VH_REQUIRE(zs >= 0 && zs < (int)g->zslots.size() && g->zslots[zs], ERR_BAD_ARG, "z slot not set");
       vh_precon* p = ps[i];
       VH_CUDA_TRY(cudaMalloc(&p->A_inv, std::max<int64_t>(1, g->nc) * sizeof(double)));
+      p->df = df;
+      static_assert(sizeof(dfloat) == sizeof(double), "pair factor entries take a double's storage");
       VH_CUDA_TRY(cudaMalloc(&p->W, std::max<int64_t>(1, g->chol.w_total) * sizeof(double)));
       const double* sp = st_sparse_precon + 6 * i;
       const double2 s1 = make_double2(sp[0], sp[1]), s2 = make_double2(sp[2], sp[3]), s3 = make_double2(sp[4], sp[5]);
@@ -198,7 +242,10 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
       W[i] = p->W;
     }
     ProfScope prof(&g->ctx->prof, SEC_FACTOR, st, nfreq);
-    chol_factor(g->chol, nfreq, D.data(), W.data(), st);
+    if (df)
+      chol_factor<dfloat>(g->chol, nfreq, D.data(), reinterpret_cast<dfloat* const*>(W.data()), st);
+    else
+      chol_factor<double>(g->chol, nfreq, D.data(), reinterpret_cast<double* const*>(W.data()), st);
   });
   if (s != VH_OK) {
     for (auto* p : ps) vh_precon_destroy(p);
