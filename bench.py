@@ -417,7 +417,7 @@ def run_probe(args):
                                             None, prec), g.ctx.handle)
     else:
         st = (1j * 2 * np.pi * w.freqs[:B] * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
-        pcs = g.precons(st, np.zeros(B, dtype=np.int32))
+        pcs = g.precons(st, np.zeros(B, dtype=np.int32), kind=args.probe_kind)
         parr = (C.c_void_p * B)(*[p.handle for p in pcs])
         for _ in range(args.probe_iters):
             _lib.check(lib.vh_precon_apply_device(g.handle, B, parr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr())),
@@ -434,6 +434,7 @@ def main():
                     help="profiling aid: run only the warm-up and timed mixed-precision sweeps, print nothing")
     ap.add_argument("--probe-rhs", type=int, default=4)
     ap.add_argument("--probe-iters", type=int, default=3)
+    ap.add_argument("--probe-kind", default="schur_invert", choices=["schur_invert", "schur_invert_df"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)

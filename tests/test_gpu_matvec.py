@@ -134,3 +134,21 @@ def test_matvec_linearity_large(vie):
     assert rel(lhs, rhs) < 1e-13
     ref = solver.lse_matvect_mult(x, s * fN, S.Ar, z_real, None, S.dx, S.idxS5)
     assert rel(g.matvec(x, scale=s), ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL)])
+def test_matvec_voxel_box_inside_grid(vie, prec, tol):
+    """Voxels in y 3..12 and z 2..5 of a 20 x 16 x 9 grid: the transform visits only that box."""
+    from voxhenry_gb300 import geometry
+
+    w = geometry.two_bars(L=20, M=16, N=9, xr=(1, 19), zr=(2, 6), y1=(3, 6), y2=(9, 13))
+    S, fN, st = system_of(w)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)
+    s = 1j * 2 * np.pi * 3e9 * solver.MU0
+    rng = np.random.default_rng(12)
+    X = np.stack([rand_c(rng, S.n) for _ in range(3)])
+    Y = g.matvec(X, scale=np.full(3, s), prec=prec)
+    for b in range(3):
+        ref = solver.lse_matvect_mult(X[b], s * fN, S.Ar, z_real, None, S.dx, S.idxS5)
+        assert rel(Y[b], ref) < tol

@@ -357,10 +357,10 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* con
     if (fused_max > 0)
       VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_front<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_max));
     for (size_t hl = 0; hl < s.levels.size(); ++hl) {
-      if (!s.levels_fused[hl].empty()) {
-        const size_t sm = fused_smem_bytes<T>(s.fused_max_nf[hl], s.fused_max_ns[hl]);
-        k_chol_front<T><<<dim3((unsigned)s.levels_fused[hl].size(), 1, nz), kFusedThreads, sm, st>>>(
-            s.d_levels_fused[hl], s.d_fronts, s.d_relmap, Wp, d_err);
+      for (const auto& fc : s.fused_classes[hl]) {
+        const size_t sm = fused_smem_bytes<T>(fc.max_nf, fc.max_ns);
+        k_chol_front<T><<<dim3((unsigned)fc.count, 1, nz), kFusedThreads, sm, st>>>(
+            s.d_levels_fused[hl] + fc.offset, s.d_fronts, s.d_relmap, Wp, d_err);
         count_launch();
         VH_CUDA_TRY(cudaGetLastError());
       }

@@ -47,8 +47,14 @@ struct CholSymbolic {
   std::vector<FrontInfo> fronts;
   std::vector<std::vector<int32_t>> levels;  // fronts per height (leaves first)
   std::vector<int32_t> level_max_ns, level_max_nf;
-  // per height, the fronts factored whole in shared memory (nf <= kFusedMaxNf) and the others
+  // per height, the fronts factored whole in shared memory (nf <= kFusedMaxNf) and the others.
+  // levels_fused[h] is sorted by decreasing order; fused_classes[h] cuts it into runs whose shared
+  // memory lets the same number of CTAs share an SM, so that small fronts run at high occupancy.
+  struct FusedClass {
+    int32_t offset, count, max_nf, max_ns;
+  };
   std::vector<std::vector<int32_t>> levels_fused, levels_blocked;
+  std::vector<std::vector<FusedClass>> fused_classes;
   std::vector<int32_t> fused_max_ns, fused_max_nf, blocked_max_ns, blocked_max_nf;
   // device copies
   FrontInfo* d_fronts = nullptr;

@@ -328,6 +328,30 @@ void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64
       mns = std::max(mns, fi.ns);
       mnf = std::max(mnf, fi.nf);
     }
+  // occupancy classes of the fused fronts: CTAs per SM that the shared memory of a front allows
+  // (the kernel holds nf^2 + 2 ns values of 8 bytes; 228 KB per SM, 1 KB reserved per CTA, <= 8)
+  auto ctas_per_sm = [](int nf, int ns) {
+    const size_t bytes = ((size_t)nf * nf + 2 * (size_t)ns) * 8 + 1024;
+    return (int)std::min<size_t>(8, std::max<size_t>(1, (228 * 1024) / bytes));
+  };
+  s.fused_classes.assign(nh, {});
+  for (size_t h = 0; h < nh; ++h) {
+    auto& L = s.levels_fused[h];
+    std::stable_sort(L.begin(), L.end(), [&](int a, int b) { return s.fronts[a].nf > s.fronts[b].nf; });
+    for (size_t i = 0; i < L.size();) {
+      const int cls = ctas_per_sm(s.fronts[L[i]].nf, s.fronts[L[i]].ns);
+      CholSymbolic::FusedClass fc{(int32_t)i, 0, 0, 0};
+      size_t j = i;
+      while (j < L.size() && ctas_per_sm(s.fronts[L[j]].nf, s.fronts[L[j]].ns) == cls) {
+        fc.max_nf = std::max(fc.max_nf, s.fronts[L[j]].nf);
+        fc.max_ns = std::max(fc.max_ns, s.fronts[L[j]].ns);
+        ++j;
+      }
+      fc.count = (int32_t)(j - i);
+      s.fused_classes[h].push_back(fc);
+      i = j;
+    }
+  }
   s.nfronts = nfr;
   s.w_total = w_off;
   s.u_total = u_off;
@@ -343,6 +367,8 @@ void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64
       }
       fprintf(stderr, "height %zu: %zu fronts, max ns %d, max nb %d, max nf %d, sum ns %ld, sum nb %ld\n", h,
               s.levels[h].size(), s.level_max_ns[h], max_nb, s.level_max_nf[h], (long)sum_ns, (long)sum_nb);
+      for (const auto& fc : s.fused_classes[h])
+        fprintf(stderr, "    fused class: %d fronts, max nf %d, max ns %d\n", fc.count, fc.max_nf, fc.max_ns);
     }
   }
   if (!to_device) return;

@@ -5,13 +5,16 @@
 // five inverse FFTs, crop, diagonal z/dx {1,1,1,1/6,1/2} term, gather) as five
 // passes over HBM:
 //   1. fwd-x : gather x_J through the voxel map, FFT along x (input half zero)
-//              -> A[b][c][z<N][y<M][kx<2L]
-//   2. fwd-y : FFT along y (input half zero)          -> B[b][c][z<N][ky<2M][kx]
+//              -> A[b][c][z][y][kx<2L]
+//   2. fwd-y : FFT along y (input half zero)          -> B[b][c][z][ky<2M][kx]
 //   3. z     : FFT along z, multiply by the tensor spectrum, inverse FFT along z,
-//              keep z<N (in place in B).  The 7 tensor values of a point stay in
-//              registers while the CTA walks the RHS batch.
-//   4. inv-y : inverse FFT along y, keep y<M          -> A
+//              keep the voxel rows (in place in B).  The 7 tensor values of a point stay
+//              in registers while the CTA walks the RHS batch.
+//   4. inv-y : inverse FFT along y, keep the voxel rows -> A
 //   5. inv-x : inverse FFT along x, keep x<L, add the diagonal term, scatter to y_J.
+// Only the bounding box of the voxels in y and z is visited: y in [y0, y0+ny), z in
+// [z0, z0+nz) (A and B hold those rows, compact).  Lines outside it are zero on input and
+// unused on output, so the result is the same as that of the full padded transform.
 // The 1/(8LMN) normalisation of ifftn is folded into the stored tensor; the
 // frequency factor j*omega*mu is a per-RHS scalar applied in pass 5.
 #include <cmath>
@@ -115,8 +118,8 @@ static int z_lines_per_cta(int Z, int X) {
 // pass 1: fwd-x.  CTA handles `nl` consecutive lines (y fastest, then z, c, b), line-major smem.
 template <typename T>
 __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int32_t* __restrict__ vmap, int L, int M,
-                        int N, int64_t nv, int64_t nlines_total, cplx<T>* __restrict__ A, FftDesc fd,
-                        const cplx<T>* __restrict__ twg, int nl) {
+                        int y0, int ny, int z0, int nz, int64_t nv, int64_t nlines_total, cplx<T>* __restrict__ A,
+                        FftDesc fd, const cplx<T>* __restrict__ twg, int nl) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int X = fd.n;
@@ -137,10 +140,10 @@ __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int3
       vid[u] = -1;
       off[u] = 0;
       if (t < tot && gl < nlines_total && i < L) {
-        const int64_t y = gl % M;
-        const int64_t z = (gl / M) % N;
-        const int64_t c = (gl / ((int64_t)M * N)) % 5;
-        const int64_t b = gl / ((int64_t)M * N * 5);
+        const int64_t y = y0 + gl % ny;
+        const int64_t z = z0 + (gl / ny) % nz;
+        const int64_t c = (gl / ((int64_t)ny * nz)) % 5;
+        const int64_t b = gl / ((int64_t)ny * nz * 5);
         vid[u] = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
         off[u] = b * ldx + c * nv;
       }
@@ -162,9 +165,11 @@ __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int3
 
 // pass 2 / 4: FFT along y.  Rows of `nin` input (index < nin), `nout` output rows written.
 // src: [plane][nin_rows_stride][X], dst: [plane][nout_stride][X]; CTA: `tx` consecutive kx of one plane.
+// The nin source rows enter the transform at rows in_off..; result rows out_off.. are stored.
 template <typename T, int DIR>
 __global__ void k_pass_y(const cplx<T>* __restrict__ src, int src_rows, int nin, cplx<T>* __restrict__ dst,
-                         int dst_rows, int nout, int X, FftDesc fd, const cplx<T>* __restrict__ twg, int tx) {
+                         int dst_rows, int nout, int X, FftDesc fd, const cplx<T>* __restrict__ twg, int tx,
+                         int in_off, int out_off) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Y = fd.n;
@@ -177,18 +182,19 @@ __global__ void k_pass_y(const cplx<T>* __restrict__ src, int src_rows, int nin,
   const C* s = src + plane * src_rows * (int64_t)X;
   C* d = dst + plane * dst_rows * (int64_t)X;
   const int cv = min(tx, X - kx0);
-  tile_load(b0, tx, s + kx0, X, Y, nin, tx, cv);
+  for (int q = threadIdx.x; q < in_off * tx; q += blockDim.x) b0[q] = czero<C>();
+  tile_load(b0 + in_off * tx, tx, s + kx0, X, Y - in_off, nin, tx, cv);
   cp_async_wait_all();
   __syncthreads();
   C* r = fft_lines<DIR>(b0, b1, tw, fd, tx, 1, tx, false);
-  tile_store(d + kx0, X, r, tx, nout, cv);
+  tile_store(d + kx0, X, r + out_off * tx, tx, nout, cv);
 }
 
 // pass 3: z-FFT, tensor product, inverse z-FFT.  B[b][c][z<N][ky][kx] in place.
 // blockDim = Z * tx; thread (kz, tx) keeps the 7 tensor values of its point in registers.
 template <typename T>
-__global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ tens, int N, int Y, int X, int nrhs,
-                        FftDesc fd, const cplx<T>* __restrict__ twg, int tx) {
+__global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ tens, int z0, int nz, int Y, int X,
+                        int nrhs, FftDesc fd, const cplx<T>* __restrict__ twg, int tx) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Z = fd.n;
@@ -210,13 +216,15 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
 #pragma unroll
     for (int k = 0; k < 7; ++k) g[k] = czero<C>();
   }
-  const int64_t plane = (int64_t)Y * X;      // one z row of one component
-  const int64_t comp = (int64_t)N * plane;   // one component of one RHS
+  const int64_t plane = (int64_t)Y * X;       // one z row of one component
+  const int64_t comp = (int64_t)nz * plane;   // one component of one RHS
   for (int b = 0; b < nrhs; ++b) {
     C* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X;
     const int cv = min(tx, X - kx0);
+    for (int q = threadIdx.x; q < z0 * nl; q += blockDim.x) b0[q] = czero<C>();   // rows below the voxels
 #pragma unroll
-    for (int c = 0; c < 5; ++c) tile_load(b0 + c * tx, nl, base + c * comp + kx0, plane, Z, N, tx, cv);
+    for (int c = 0; c < 5; ++c)
+      tile_load(b0 + c * tx + z0 * nl, nl, base + c * comp + kx0, plane, Z - z0, nz, tx, cv);
     cp_async_wait_all();
     __syncthreads();
     C* f = fft_lines<-1>(b0, b1, tw, fd, nl, 1, nl, false);
@@ -241,15 +249,16 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
     C* other = (f == b0) ? b1 : b0;
     C* r = fft_lines<+1>(f, other, tw, fd, nl, 1, nl, false);
 #pragma unroll
-    for (int c = 0; c < 5; ++c) tile_store(base + c * comp + kx0, plane, r + c * tx, nl, N, cv);
+    for (int c = 0; c < 5; ++c) tile_store(base + c * comp + kx0, plane, r + c * tx + z0 * nl, nl, nz, cv);
     __syncthreads();
   }
 }
 
 // pass 5: inverse x-FFT, crop, diagonal term, scatter.
 template <typename T>
-__global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict__ vmap, int L, int M, int N,
-                        int64_t nv, int64_t nlines_total, const double2* __restrict__ xin, int64_t ldx,
+__global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict__ vmap, int L, int M, int y0,
+                        int ny, int z0, int nz, int64_t nv, int64_t nlines_total, const double2* __restrict__ xin,
+                        int64_t ldx,
                         double2* __restrict__ yout, int64_t ldy, const double2* __restrict__ scale,
                         const double2* __restrict__ zdiag, int64_t zstride, double inv_dx, FftDesc fd,
                         const cplx<T>* __restrict__ twg, int nl) {
@@ -270,10 +279,10 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
     const int line = t / L, i = t % L;
     const int64_t gl = l0 + line;
     if (gl >= nlines_total) continue;
-    const int64_t y = gl % M;
-    const int64_t z = (gl / M) % N;
-    const int64_t c = (gl / ((int64_t)M * N)) % 5;
-    const int64_t b = gl / ((int64_t)M * N * 5);
+    const int64_t y = y0 + gl % ny;
+    const int64_t z = z0 + (gl / ny) % nz;
+    const int64_t c = (gl / ((int64_t)ny * nz)) % 5;
+    const int64_t b = gl / ((int64_t)ny * nz * 5);
     const int32_t vid = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
     if (vid < 0) continue;
     const double2 conv = to_d(r[line * X + i]);
@@ -318,6 +327,15 @@ void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2
     VH_REQUIRE(v == 0 || idxS_host[v] > idxS_host[v - 1], ERR_BAD_ARG, "idxS must be strictly increasing");
     vm[li] = (int32_t)v;
   }
+  int ylo = M, yhi = -1, zlo = N, zhi = -1;
+  for (int64_t v = 0; v < nv; ++v) {
+    const int64_t li = idxS_host[v] - 1;
+    const int y = (int)((li / L) % M), z = (int)(li / ((int64_t)L * M));
+    ylo = std::min(ylo, y); yhi = std::max(yhi, y);
+    zlo = std::min(zlo, z); zhi = std::max(zhi, z);
+  }
+  p.y0 = nv ? ylo : 0; p.ny = nv ? yhi - ylo + 1 : 0;
+  p.z0 = nv ? zlo : 0; p.nz = nv ? zhi - zlo + 1 : 0;
   VH_CUDA_TRY(cudaMalloc(&p.vmap, lmn * sizeof(int32_t)));
   VH_CUDA_TRY(cudaMemcpyAsync(p.vmap, vm.data(), lmn * sizeof(int32_t), cudaMemcpyHostToDevice, st));
   // twiddles
@@ -359,8 +377,8 @@ void conv_plan_destroy(ConvPlan& p) {
 
 void conv_plan_reserve(ConvPlan& p, int B, Prec prec) {
   const size_t cs = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
-  const size_t needA = (size_t)B * 5 * p.N * p.M * p.X * cs;
-  const size_t needB = (size_t)B * 5 * p.N * p.Y * p.X * cs;
+  const size_t needA = (size_t)B * 5 * p.nz * p.ny * p.X * cs;
+  const size_t needB = (size_t)B * 5 * p.nz * p.Y * p.X * cs;
   if (needA > p.scratch_bytes_A) {
     cudaFree(p.scratchA);
     p.scratchA = nullptr;
@@ -387,15 +405,17 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   const C* tens = dbl ? reinterpret_cast<const C*>(p.tens64) : reinterpret_cast<const C*>(p.tens32);
   C* const* twp = dbl ? reinterpret_cast<C* const*>(p.tw64) : reinterpret_cast<C* const*>(p.tw32);
   VH_REQUIRE(tens != nullptr, ERR_BAD_ARG, "tensor for this precision was not built");
-  const int X = p.X, Y = p.Y, Z = p.Z, L = p.L, M = p.M, N = p.N;
+  const int X = p.X, Y = p.Y, Z = p.Z, L = p.L, M = p.M;
+  const int y0 = p.y0, ny = p.ny, z0 = p.z0, nz = p.nz;
+  VH_REQUIRE(ny > 0 && nz > 0, ERR_BAD_ARG, "FFT convolution of a geometry without voxels");
   // pass 1
   {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
-    const int64_t lines = (int64_t)M * N * 5 * B;
+    const int64_t lines = (int64_t)ny * nz * 5 * B;
     const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C);
     const unsigned grid = (unsigned)ceil_div(lines, nl);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_fwd_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_fwd_x<T><<<grid, 256, sm, st>>>(x, ldx, p.vmap, L, M, N, p.nv, lines, A, p.fx, twp[0], nl);
+    k_fwd_x<T><<<grid, 256, sm, st>>>(x, ldx, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, A, p.fx, twp[0], nl);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -403,9 +423,9 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   {
     const int tx = y_lines_per_cta(Y, X, dbl);
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
-    dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * N * B));
+    dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
     VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_pass_y<T, -1><<<grid, 256, sm, st>>>(A, M, M, Bf, Y, Y, X, p.fy, twp[1], tx);
+    k_pass_y<T, -1><<<grid, 256, sm, st>>>(A, ny, ny, Bf, Y, Y, X, p.fy, twp[1], tx, y0, 0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -415,7 +435,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const size_t sm = (size_t)(Z + 2 * Z * 5 * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)Y);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_zpass<T><<<grid, Z * tx, sm, st>>>(Bf, tens, N, Y, X, B, p.fz, twp[2], tx);
+    k_zpass<T><<<grid, Z * tx, sm, st>>>(Bf, tens, z0, nz, Y, X, B, p.fz, twp[2], tx);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -423,21 +443,21 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   {
     const int tx = y_lines_per_cta(Y, X, dbl);
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
-    dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * N * B));
+    dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
     VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_pass_y<T, +1><<<grid, 256, sm, st>>>(Bf, Y, Y, A, M, M, X, p.fy, twp[1], tx);
+    k_pass_y<T, +1><<<grid, 256, sm, st>>>(Bf, Y, Y, A, ny, ny, X, p.fy, twp[1], tx, 0, y0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 5
   {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
-    const int64_t lines = (int64_t)M * N * 5 * B;
+    const int64_t lines = (int64_t)ny * nz * 5 * B;
     const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C);
     const unsigned grid = (unsigned)ceil_div(lines, nl);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_inv_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_inv_x<T><<<grid, 256, sm, st>>>(A, p.vmap, L, M, N, p.nv, lines, x, ldx, y, ldy, scale, zdiag, zstride,
-                                      1.0 / p.dx, p.fx, twp[0], nl);
+    k_inv_x<T><<<grid, 256, sm, st>>>(A, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, x, ldx, y, ldy, scale, zdiag,
+                                      zstride, 1.0 / p.dx, p.fx, twp[0], nl);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -540,8 +560,8 @@ void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, do
 
 void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t& b_per_rhs) {
   const size_t cs = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
-  a_per_rhs = (size_t)5 * p.N * p.M * p.X * cs;
-  b_per_rhs = (size_t)5 * p.N * p.Y * p.X * cs;
+  a_per_rhs = (size_t)5 * p.nz * p.ny * p.X * cs;
+  b_per_rhs = (size_t)5 * p.nz * p.Y * p.X * cs;
 }
 
 void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,

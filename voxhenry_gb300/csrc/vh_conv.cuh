@@ -17,6 +17,10 @@ struct ConvPlan {
   int L = 0, M = 0, N = 0;   // voxel grid
   int X = 0, Y = 0, Z = 0;   // padded grid (2L, 2M, 2N)
   int64_t nv = 0;            // non-empty voxels
+  // bounding box of the voxels in y and z: the x-passes run over lines y0 <= y < y0+ny,
+  // z0 <= z < z0+nz only, and the y- and z-FFTs load and keep only those rows (every other line
+  // of the zero-padded operands is zero, and only voxel rows of the result are used)
+  int y0 = 0, ny = 0, z0 = 0, nz = 0;
   double dx = 0;
   FftDesc fx{}, fy{}, fz{};
   int32_t* vmap = nullptr;   // (L*M*N) voxel -> compact index or -1, column-major
@@ -25,7 +29,7 @@ struct ConvPlan {
   float2* tens32 = nullptr;
   double2* tw64[3] = {nullptr, nullptr, nullptr};
   float2* tw32[3] = {nullptr, nullptr, nullptr};
-  // scratch: A (5 * N * M * X per RHS) and Bf (5 * N * Y * X per RHS), in bytes
+  // scratch: A (5 * nz * ny * X per RHS) and Bf (5 * nz * Y * X per RHS), in bytes
   void* scratchA = nullptr;
   void* scratchB = nullptr;
   size_t scratch_bytes_A = 0, scratch_bytes_B = 0;
@@ -49,8 +53,8 @@ void conv_plan_reserve(ConvPlan& p, int B, Prec prec);
 void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
                 const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st);
 
-// Bytes of FFT scratch one right-hand side needs at precision `prec`: A (5 N M X complex values)
-// and Bf (5 N Y X complex values).
+// Bytes of FFT scratch one right-hand side needs at precision `prec`: A (5 nz ny X complex values)
+// and Bf (5 nz Y X complex values), at most 30 L M N values in all.
 void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t& b_per_rhs);
 
 // conv_apply with caller-provided scratch (scratchA: B * a_per_rhs bytes, scratchB: B * b_per_rhs
