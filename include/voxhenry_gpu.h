@@ -14,6 +14,8 @@
  * Every call returns a vh_status; vh_last_error() gives the text of the last failure
  * on a context.  Host pointers are borrowed for the duration of the call.
  * A context owns one CUDA stream; calls on one context must not overlap.
+ * Handles may be destroyed in any order: a geometry keeps its context, and a preconditioner its
+ * geometry, until it is destroyed itself.
  */
 #ifndef VOXHENRY_GPU_H
 #define VOXHENRY_GPU_H

@@ -211,12 +211,7 @@ vh_status vh_ctx_create(int device, vh_ctx** out) {
   return VH_OK;
 }
 
-void vh_ctx_destroy(vh_ctx* ctx) {
-  if (!ctx) return;
-  cudaSetDevice(ctx->device);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
-  delete ctx;
-}
+void vh_ctx_destroy(vh_ctx* ctx) { vh::ctx_release(ctx); }
 
 const char* vh_last_error(const vh_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
@@ -232,6 +227,8 @@ vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const doub
   if (!ctx || !out) return VH_ERR_BAD_ARG;
   *out = nullptr;
   auto* g = new vh_geom();
+  g->ctx = ctx;
+  ctx->refs.fetch_add(1);
   vh_status s = guarded(ctx, [&] {
     VH_REQUIRE(L >= 2 && M >= 2 && N >= 2, ERR_UNSUPPORTED, "grids thinner than 2 voxels are not supported");
     VH_REQUIRE(dx > 0 && nv >= 0 && num_node >= 0, ERR_BAD_ARG, "bad sizes");
@@ -311,8 +308,20 @@ vh_status vh_geom_create_generated(vh_ctx* ctx, int L, int M, int N, double dx, 
   return VH_OK;
 }
 
-void vh_geom_destroy(vh_geom* g) {
-  if (!g) return;
+void vh_geom_destroy(vh_geom* g) { vh::geom_release(g); }
+
+}  // extern "C"
+
+namespace vh {
+void ctx_release(vh_ctx* c) {
+  if (!c || c->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+void geom_release(vh_geom* g) {
+  if (!g || g->refs.fetch_sub(1) != 1) return;
   if (g->ctx) cudaSetDevice(g->ctx->device);
   conv_plan_destroy(g->conv);
   g->Ae.free_all();
@@ -327,8 +336,13 @@ void vh_geom_destroy(vh_geom* g) {
   cudaFree(g->io_y);
   cudaFree(g->io_s);
   cudaFree(g->zgather);
+  vh_ctx* c = g->ctx;
   delete g;
+  ctx_release(c);
 }
+}  // namespace vh
+
+extern "C" {
 
 vh_status vh_geom_sizes(const vh_geom* g, int64_t* n_curr, int64_t* n_node, int64_t* n) {
   if (!g) return VH_ERR_BAD_ARG;

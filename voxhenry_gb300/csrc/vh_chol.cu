@@ -334,14 +334,20 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* con
   if (s.nfronts == 0 || nfac == 0) return;
   VH_REQUIRE(nfac <= 65535, ERR_BAD_ARG, "too many factors in one batch");
   int* d_err = s.d_err;
-  void** tab = nullptr;   // device: [D pointers | W pointers]
-  VH_CUDA_TRY(cudaMalloc(&tab, 2 * (size_t)nfac * sizeof(void*)));
+  if (nfac > s.tab_cap) {   // device: [D pointers | W pointers], kept with the symbolic structure
+    cudaFree(s.d_tab);
+    s.d_tab = nullptr;
+    s.tab_cap = 0;
+    VH_CUDA_TRY(cudaMalloc(&s.d_tab, 2 * (size_t)nfac * sizeof(void*)));
+    s.tab_cap = nfac;
+  }
+  void** tab = s.d_tab;
   std::vector<void*> h(2 * (size_t)nfac);
   for (int i = 0; i < nfac; ++i) {
     h[i] = const_cast<double*>(D[i]);
     h[nfac + i] = W[i];
   }
-  try {
+  {
     VH_CUDA_TRY(cudaMemcpyAsync(tab, h.data(), h.size() * sizeof(void*), cudaMemcpyHostToDevice, st));
     const double* const* Dp = reinterpret_cast<const double* const*>(tab);
     T* const* Wp = reinterpret_cast<T* const*>(tab + nfac);
@@ -395,11 +401,7 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* con
     VH_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     VH_CUDA_TRY(cudaStreamSynchronize(st));
     VH_REQUIRE(herr == 0, ERR_BAD_ARG, "Schur complement is not positive definite (check the port/ground nodes)");
-  } catch (...) {
-    cudaFree(tab);
-    throw;
   }
-  cudaFree(tab);
 }
 
 // ---- triangular solves.  One warp per (front, RHS), kSolveWarps warps per CTA.  Each front's

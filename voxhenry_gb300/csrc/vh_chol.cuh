@@ -66,6 +66,8 @@ struct CholSymbolic {
   std::vector<int32_t*> d_levels;   // per height: front ids
   std::vector<int32_t*> d_levels_fused, d_levels_blocked;
   int* d_err = nullptr;             // factorisation status flag
+  mutable void** d_tab = nullptr;   // device pointer table of the batched factorisation
+  mutable int tab_cap = 0;
   int64_t n_asm = 0;
   void free_all();
 };

@@ -30,6 +30,9 @@ void CholSymbolic::free_all() {
   d_levels_blocked.clear();
   cudaFree(d_err);
   d_err = nullptr;
+  cudaFree(d_tab);
+  d_tab = nullptr;
+  tab_cap = 0;
   d_levels.clear();
   d_fronts = nullptr; d_rows = nullptr; d_relmap = nullptr; d_asm = nullptr; d_asm_q = nullptr; d_asm_c = nullptr;
 }

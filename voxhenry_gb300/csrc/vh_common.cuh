@@ -2,7 +2,12 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -88,6 +93,67 @@ struct Error {
   } while (0)
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------- device memory pool
+// Per-context cache of device blocks.  The solver needs large transient buffers on every call
+// (the Krylov basis of a 32-RHS batch is B (m+1) n complex values, ~16 GB on a 256 x 256 x 8 grid;
+// a Schur factor ~0.25 GB per frequency), and cudaMalloc / cudaFree of that size cost milliseconds
+// and synchronise the device.  get() takes the smallest cached block of at least the size asked
+// (and at most twice it), else allocates; put() returns a block to the cache.  An allocation that
+// fails for lack of memory frees the cache and retries.  Blocks are freed when the pool is destroyed.
+class DevicePool {
+ public:
+  void* get(size_t bytes) {
+    bytes = (std::max<size_t>(bytes, 1) + 511) & ~(size_t)511;
+    std::lock_guard<std::mutex> lock(mu_);
+    auto it = free_.lower_bound(bytes);
+    if (it != free_.end() && it->first <= 2 * bytes) {
+      void* p = it->second;
+      used_[p] = it->first;
+      free_.erase(it);
+      return p;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+      (void)cudaGetLastError();
+      trim_locked();
+      e = cudaMalloc(&p, bytes);
+    }
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      throw Error{e == cudaErrorMemoryAllocation ? ERR_OOM : ERR_CUDA,
+                  std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    }
+    used_[p] = bytes;
+    return p;
+  }
+  void put(void* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(mu_);
+    auto it = used_.find(p);
+    if (it == used_.end()) return;
+    free_.emplace(it->second, p);
+    used_.erase(it);
+  }
+  void trim() {
+    std::lock_guard<std::mutex> lock(mu_);
+    trim_locked();
+  }
+  ~DevicePool() {
+    trim_locked();
+    for (auto& kv : used_) cudaFree(kv.first);
+  }
+
+ private:
+  void trim_locked() {
+    for (auto& kv : free_) cudaFree(kv.second);
+    free_.clear();
+  }
+  std::mutex mu_;
+  std::multimap<size_t, void*> free_;
+  std::unordered_map<void*, size_t> used_;
+};
 
 // ---------------------------------------------------------------- instrumentation
 // Kernels launched by this library (every launch site calls count_launch()).

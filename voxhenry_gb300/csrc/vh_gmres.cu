@@ -210,19 +210,41 @@ __global__ void k_axpy_rows(double2* __restrict__ x, const double2* __restrict__
   }
 }
 
+// The context pool that solver buffers come from while a C ABI call runs on this thread (set by
+// PoolScope at the call's entry); without one, DevBuf allocates and frees directly.
+thread_local DevicePool* tl_pool = nullptr;
+struct PoolScope {
+  DevicePool* prev;
+  explicit PoolScope(DevicePool* p) : prev(tl_pool) { tl_pool = p; }
+  ~PoolScope() { tl_pool = prev; }
+};
+
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t cap = 0;
-  void ensure(size_t n) {
-    if (n <= cap) return;
-    cudaFree(p);
+  DevicePool* pool = nullptr;
+  void release() {
+    if (pool)
+      pool->put(p);
+    else
+      cudaFree(p);
     p = nullptr;
     cap = 0;
-    VH_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)));
+    pool = nullptr;
+  }
+  void ensure(size_t n) {
+    if (n <= cap) return;
+    release();
+    const size_t bytes = std::max<size_t>(1, n) * sizeof(T);
+    pool = tl_pool;
+    if (pool)
+      p = static_cast<T*>(pool->get(bytes));
+    else
+      VH_CUDA_TRY(cudaMalloc(&p, bytes));
     cap = n;
   }
-  ~DevBuf() { cudaFree(p); }
+  ~DevBuf() { release(); }
 };
 
 unsigned grid1(int64_t n) { return (unsigned)std::min<int64_t>(4096, std::max<int64_t>(1, ceil_div(n, 256))); }
@@ -704,6 +726,7 @@ void gmres_dispatch(vh_geom* g, int B, vh_precon* const* pcs, const double2* b_d
                     double2* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
   VH_REQUIRE(B >= 1 && b_dev && x_dev && tol, ERR_BAD_ARG, "bad gmres arguments");
   VH_REQUIRE(!(flexible && prec == VH_PREC_FP32), ERR_UNSUPPORTED, "mixed precision uses the left-preconditioned form");
+  PoolScope pool_scope(&g->ctx->pool);
   cudaStream_t st = g->ctx->stream;
   VH_CUDA_TRY(cudaMemsetAsync(x_dev, 0, (size_t)B * g->n * sizeof(double2), st));
   GmresOut o;

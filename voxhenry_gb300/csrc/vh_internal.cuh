@@ -1,5 +1,6 @@
 // Internal state behind the C ABI handles.
 #pragma once
+#include <atomic>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -9,11 +10,15 @@
 #include "vh_chol.cuh"
 #include "vh_conv.cuh"
 
+// Handles are reference counted: a geometry holds its context and a preconditioner its geometry,
+// so the owner may destroy them in any order; a parent is released with its last child.
 struct vh_ctx {
+  std::atomic<int> refs{1};
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string last_error;
   vh::Profiler prof;
+  vh::DevicePool pool;   // solver buffers and factors; all their work is ordered on `stream`
 };
 
 namespace vh {
@@ -53,6 +58,7 @@ void csc_upload(int64_t nrow, int64_t ncol, const int64_t* jc, const int64_t* ir
 }  // namespace vh
 
 struct vh_geom {
+  std::atomic<int> refs{1};
   vh_ctx* ctx = nullptr;
   int L = 0, M = 0, N = 0;
   double dx = 0;
@@ -80,3 +86,9 @@ struct vh_geom {
   double2* zgather = nullptr;      // B x nv gathered z for mixed slots
   size_t zgather_cap = 0;
 };
+
+namespace vh {
+// Drop one reference; the last one frees the handle (and releases its parent).
+void ctx_release(vh_ctx* c);
+void geom_release(vh_geom* g);
+}  // namespace vh

@@ -210,6 +210,7 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
   for (int i = 0; i < nfreq; ++i) {
     ps[i] = new vh_precon();
     ps[i]->g = g;
+    g->refs.fetch_add(1);   // the handle keeps its geometry (and context) alive
     ps[i]->kind = kind;
   }
   vh_status s = guarded_pc(g->ctx, [&] {
@@ -227,10 +228,10 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
       const int zs = zslot ? zslot[i] : 0;
       VH_REQUIRE(zs >= 0 && zs < (int)g->zslots.size() && g->zslots[zs], ERR_BAD_ARG, "z slot not set");
       vh_precon* p = ps[i];
-      VH_CUDA_TRY(cudaMalloc(&p->A_inv, std::max<int64_t>(1, g->nc) * sizeof(double)));
+      p->A_inv = static_cast<double*>(g->ctx->pool.get(std::max<int64_t>(1, g->nc) * sizeof(double)));
       p->df = df;
       static_assert(sizeof(dfloat) == sizeof(double), "pair factor entries take a double's storage");
-      VH_CUDA_TRY(cudaMalloc(&p->W, std::max<int64_t>(1, g->chol.w_total) * sizeof(double)));
+      p->W = g->ctx->pool.get(std::max<int64_t>(1, g->chol.w_total) * sizeof(double));
       const double* sp = st_sparse_precon + 6 * i;
       const double2 s1 = make_double2(sp[0], sp[1]), s2 = make_double2(sp[2], sp[3]), s3 = make_double2(sp[4], sp[5]);
       if (g->nv) {
@@ -263,10 +264,14 @@ vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_spa
 
 void vh_precon_destroy(vh_precon* p) {
   if (!p) return;
-  if (p->g) cudaSetDevice(p->g->ctx->device);
-  cudaFree(p->A_inv);
-  cudaFree(p->W);
+  vh_geom* g = p->g;
+  if (g) {   // storage goes back to the context pool; the handle's reference keeps both alive until here
+    cudaSetDevice(g->ctx->device);
+    g->ctx->pool.put(p->A_inv);
+    g->ctx->pool.put(p->W);
+  }
   delete p;
+  geom_release(g);
 }
 
 vh_status vh_precon_stats(const vh_precon* p, int64_t* nnz_factor, double* flops, int* nfronts, int* max_front) {
