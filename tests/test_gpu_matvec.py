@@ -136,12 +136,23 @@ def test_matvec_linearity_large(vie):
     assert rel(g.matvec(x, scale=s), ref) < FP64_TOL
 
 
+BOXES = [  # (grid, z range): padded z lengths 18 (shared-memory z-pass) and 8, 16, 32 (register z-pass)
+    ((20, 16, 9), (2, 6)),
+    ((16, 10, 4), (1, 2)),
+    ((20, 16, 8), (2, 5)),
+    ((12, 10, 16), (3, 8)),
+    ((12, 10, 16), (0, 16)),
+]
+
+
 @pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL)])
-def test_matvec_voxel_box_inside_grid(vie, prec, tol):
-    """Voxels in y 3..12 and z 2..5 of a 20 x 16 x 9 grid: the transform visits only that box."""
+@pytest.mark.parametrize("shape,zr", BOXES)
+def test_matvec_voxel_box_inside_grid(vie, prec, tol, shape, zr):
+    """Voxels in a y and z sub-range of the grid: the transform visits only that box."""
     from voxhenry_gb300 import geometry
 
-    w = geometry.two_bars(L=20, M=16, N=9, xr=(1, 19), zr=(2, 6), y1=(3, 6), y2=(9, 13))
+    L, M, N = shape
+    w = geometry.two_bars(L=L, M=M, N=N, xr=(1, L - 1), zr=zr, y1=(1, 3), y2=(M - 4, M - 1))
     S, fN, st = system_of(w)
     z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
     g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)

@@ -190,6 +190,24 @@ __global__ void k_pass_y(const cplx<T>* __restrict__ src, int src_rows, int nin,
   tile_store(d + kx0, X, r + out_off * tx, tx, nout, cv);
 }
 
+// The 13 distinct products of the 5 current spectra with the 7 tensor components at one point
+// (lse_matvect_mult.m:57-86), in place: (Jx, Jy, Jz, J2D, J3D) -> their operator images.
+template <typename C>
+__device__ __forceinline__ void tensor_apply(const C* g, C& jx, C& jy, C& jz, C& j2, C& j3) {
+  const C a = cmul(g[1], jx);             // G2 Jx
+  const C bb = cmul(g[2], jy);            // G3 Jy
+  const C o1 = cadd(cmul(g[0], jx), cmul(g[1], cadd(j2, j3)));
+  const C o2 = cadd(cmul(g[0], jy), cmul(g[2], csub(j2, j3)));
+  const C o3 = cadd(cmul(g[0], jz), cmul(g[4], j3));
+  const C o4 = cadd(csub(cneg(a), bb), cadd(cmul(g[3], j2), cmul(g[5], j3)));
+  const C o5 = cadd(cadd(csub(bb, a), cneg(cmul(g[4], jz))), cadd(cmul(g[5], j2), cmul(g[6], j3)));
+  jx = o1;
+  jy = o2;
+  jz = o3;
+  j2 = o4;
+  j3 = o5;
+}
+
 // pass 3: z-FFT, tensor product, inverse z-FFT.  B[b][c][z<N][ky][kx] in place.
 // blockDim = Z * tx; thread (kz, tx) keeps the 7 tensor values of its point in registers.
 template <typename T>
@@ -230,20 +248,7 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
     C* f = fft_lines<-1>(b0, b1, tw, fd, nl, 1, nl, false);
     if (my_kz < Z) {
       C* p = f + my_kz * nl + my_t;
-      const C jx = p[0], jy = p[tx], jz = p[2 * tx], j2 = p[3 * tx], j3 = p[4 * tx];
-      // lse_matvect_mult.m:57-86
-      const C a = cmul(g[1], jx);             // G2 Jx
-      const C bb = cmul(g[2], jy);            // G3 Jy
-      const C o1 = cadd(cmul(g[0], jx), cmul(g[1], cadd(j2, j3)));
-      const C o2 = cadd(cmul(g[0], jy), cmul(g[2], csub(j2, j3)));
-      const C o3 = cadd(cmul(g[0], jz), cmul(g[4], j3));
-      const C o4 = cadd(csub(cneg(a), bb), cadd(cmul(g[3], j2), cmul(g[5], j3)));
-      const C o5 = cadd(cadd(csub(bb, a), cneg(cmul(g[4], jz))), cadd(cmul(g[5], j2), cmul(g[6], j3)));
-      p[0] = o1;
-      p[tx] = o2;
-      p[2 * tx] = o3;
-      p[3 * tx] = o4;
-      p[4 * tx] = o5;
+      tensor_apply(g, p[0], p[tx], p[2 * tx], p[3 * tx], p[4 * tx]);
     }
     __syncthreads();
     C* other = (f == b0) ? b1 : b0;
@@ -251,6 +256,99 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
 #pragma unroll
     for (int c = 0; c < 5; ++c) tile_store(base + c * comp + kx0, plane, r + c * tx + z0 * nl, nl, nz, cv);
     __syncthreads();
+  }
+}
+
+// pass 3 for Z = 8, 16, 32: one thread transforms one column of one component in registers.  The
+// nz voxel rows enter the transform at rows 0.. (circular convolution is shift invariant), so the
+// forward transform reads only NZ >= nz leading rows and the inverse forms only the first NZ rows
+// (pruned at compile time).  Block: 5 warps (warp = component, lane = kx column) over 32 columns of
+// one ky row; the five spectra of a point meet in shared memory for the tensor product.
+constexpr int kZregCols = 32;
+
+template <typename T, int Z, int NZ>
+__global__ void __launch_bounds__(5 * kZregCols)
+    k_zpass_reg(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ tens, int nz, int Y, int X, int nrhs,
+                const cplx<T>* __restrict__ twg) {
+  using C = cplx<T>;
+  constexpr int BITS = Z == 8 ? 3 : (Z == 16 ? 4 : 5);
+  static_assert(Z == 8 || Z == 16 || Z == 32, "register z-pass lengths");
+  extern __shared__ __align__(16) unsigned char zr_raw[];
+  C* tw = reinterpret_cast<C*>(zr_raw);
+  C* S = tw + Z;   // S[(c * Z + p) * 32 + lane]: component c, transform position p
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < Z; i += blockDim.x) tw[i] = twg[i];
+  const int ky = blockIdx.y;
+  const int kx = blockIdx.x * kZregCols + lane;
+  const bool col_ok = kx < X;
+  const int64_t plane = (int64_t)Y * X;       // one z row of one component
+  const int64_t comp = (int64_t)nz * plane;   // one component of one RHS
+  __syncthreads();
+  for (int b = 0; b < nrhs; ++b) {
+    C* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X + kx;
+    {
+      C v[Z];
+#pragma unroll
+      for (int i = 0; i < Z; ++i) v[i] = czero<C>();
+#pragma unroll
+      for (int i = 0; i < NZ; ++i)
+        if (i < nz && col_ok) v[i] = base[warp * comp + i * plane];
+      dif_pruned<Z, Z, NZ, -1>(v, tw);
+#pragma unroll
+      for (int p = 0; p < Z; ++p) S[(warp * Z + p) * kZregCols + lane] = v[p];
+    }
+    __syncthreads();
+    for (int p = warp; p < Z; p += 5) {   // position p holds kz = bitrev(p)
+      const int kz = bit_reverse<BITS>(p);
+      C g[7];
+#pragma unroll
+      for (int k = 0; k < 7; ++k) g[k] = col_ok ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : czero<C>();
+      C* q = S + p * kZregCols + lane;
+      constexpr int cs = Z * kZregCols;
+      tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+    }
+    __syncthreads();
+    {
+      C v[Z];
+#pragma unroll
+      for (int p = 0; p < Z; ++p) v[p] = S[(warp * Z + p) * kZregCols + lane];
+      dit_pruned<Z, Z, NZ, +1>(v, tw);
+#pragma unroll
+      for (int i = 0; i < NZ; ++i)
+        if (i < nz && col_ok) base[warp * comp + i * plane] = v[i];
+    }
+    __syncthreads();   // S is rewritten by the next RHS
+  }
+}
+
+template <typename T, int Z, int NZ>
+static void launch_zpass_reg(cplx<T>* Bf, const cplx<T>* tens, int nz, int Y, int X, int B, const cplx<T>* tw,
+                             cudaStream_t st) {
+  const size_t sm = (size_t)(Z + 5 * Z * kZregCols) * sizeof(cplx<T>);
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass_reg<T, Z, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  dim3 grid((unsigned)ceil_div(X, kZregCols), (unsigned)Y);
+  k_zpass_reg<T, Z, NZ><<<grid, 5 * kZregCols, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
+  count_launch();
+  VH_CUDA_TRY(cudaGetLastError());
+}
+
+// true when the register z-pass handles this length (Z = 8, 16, 32; nz <= Z / 2 always holds)
+template <typename T>
+static bool zpass_reg(int Z, int nz, cplx<T>* Bf, const cplx<T>* tens, int Y, int X, int B, const cplx<T>* tw,
+                      cudaStream_t st) {
+  int nzb = 2;
+  while (nzb < nz) nzb *= 2;
+  switch (Z * 100 + nzb) {
+    case 802: launch_zpass_reg<T, 8, 2>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 804: launch_zpass_reg<T, 8, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 1602: launch_zpass_reg<T, 16, 2>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 1604: launch_zpass_reg<T, 16, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 1608: launch_zpass_reg<T, 16, 8>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3202: launch_zpass_reg<T, 32, 2>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3204: launch_zpass_reg<T, 32, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3208: launch_zpass_reg<T, 32, 8>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3216: launch_zpass_reg<T, 32, 16>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    default: return false;
   }
 }
 
@@ -430,7 +528,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 3
-  {
+  if (!zpass_reg<T>(Z, nz, Bf, tens, Y, X, B, twp[2], st)) {
     const int tx = z_lines_per_cta(Z, X);
     const size_t sm = (size_t)(Z + 2 * Z * 5 * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)Y);

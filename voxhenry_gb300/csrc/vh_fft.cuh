@@ -205,4 +205,72 @@ __device__ C* fft_lines(C* buf0, C* buf1, const C* tw, const FftDesc& d, int es,
   return src;
 }
 
+// ---- register-resident pruned transforms of a compile-time power-of-two length (one line per
+// thread).  tw[j] = exp(-2 pi i j / Z) for the top-level length Z; DIR = -1 forward, +1 inverse
+// (unnormalised).  Multiplications by 1, -+i and exp(-+i pi/4) are resolved at compile time.
+template <int Z, int N, int DIR, typename C>
+__host__ __device__ __forceinline__ C tw_mul(C x, int n, const C* tw) {
+  if (n == 0) return x;
+  if (4 * n == N) return cmul_i<DIR>(x);
+  const C w = tw[n * (Z / N)];
+  if (8 * n == N) {   // w = (c, -+c), c = cos(pi/4)
+    const auto c = w.x;
+    C r;
+    if (DIR < 0) { r.x = (x.x + x.y) * c; r.y = (x.y - x.x) * c; }
+    else { r.x = (x.x - x.y) * c; r.y = (x.x + x.y) * c; }
+    return r;
+  }
+  return DIR < 0 ? cmul(x, w) : cmulc(x, w);
+}
+
+// Decimation in frequency, natural-order input whose entries at or beyond NZ are zero (they are
+// not read), bit-reversed output.  A half whose upper part is zero costs only its twiddles.
+template <int Z, int N, int NZ, int DIR, typename C>
+__host__ __device__ __forceinline__ void dif_pruned(C* v, const C* tw) {
+  if constexpr (N > 1) {
+    constexpr int H = N / 2;
+#pragma unroll
+    for (int n = 0; n < H; ++n) {
+      if (n >= NZ) continue;                       // both zero
+      if (n + H >= NZ) {                           // upper zero
+        v[n + H] = tw_mul<Z, N, DIR>(v[n], n, tw);
+      } else {
+        const C a = v[n], b = v[n + H];
+        v[n] = cadd(a, b);
+        v[n + H] = tw_mul<Z, N, DIR>(csub(a, b), n, tw);
+      }
+    }
+    constexpr int NZ2 = NZ < H ? NZ : H;
+    dif_pruned<Z, H, NZ2, DIR>(v, tw);
+    dif_pruned<Z, H, NZ2, DIR>(v + H, tw);
+  }
+}
+
+// Decimation in time, bit-reversed input, natural-order output of which only entries below NZ
+// are formed.
+template <int Z, int N, int NZ, int DIR, typename C>
+__host__ __device__ __forceinline__ void dit_pruned(C* v, const C* tw) {
+  if constexpr (N > 1) {
+    constexpr int H = N / 2;
+    constexpr int NZ2 = NZ < H ? NZ : H;
+    dit_pruned<Z, H, NZ2, DIR>(v, tw);
+    dit_pruned<Z, H, NZ2, DIR>(v + H, tw);
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+      const bool lo = k < NZ, hi = k + H < NZ;
+      if (!lo && !hi) continue;
+      const C t = tw_mul<Z, N, DIR>(v[k + H], k, tw);
+      if (hi) v[k + H] = csub(v[k], t);
+      if (lo) v[k] = cadd(v[k], t);
+    }
+  }
+}
+
+template <int BITS>
+__host__ __device__ constexpr int bit_reverse(int x) {
+  int r = 0;
+  for (int b = 0; b < BITS; ++b) r |= ((x >> b) & 1) << (BITS - 1 - b);
+  return r;
+}
+
 }  // namespace vh
