@@ -154,8 +154,9 @@ vh_status vh_precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const
  *      relres = |b - A x| / |b|, iter = [inner iterations of the last cycle, outer cycles] (2 ints),
  *      resvec (first resvec_len entries, row b at b*resvec_len), nres = its full length.
  *      prec = VH_PREC_FP32: mixed precision -- FP64 iterative refinement around left-preconditioned
- *      GMRES whose FFT matvec runs in complex64; iter then counts inner iterations / cycles summed
- *      over refinement steps and resvec holds the preconditioned residual after each step.     */
+ *      GMRES whose FFT matvec runs in complex64, refined until the true residual meets tol; iter then
+ *      counts inner iterations / cycles summed over refinement steps and resvec holds the true relative
+ *      residual |b - A x| / |b| after each step.                                                 */
 vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
                    int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
                    double* relres, int* iter, double* resvec, int resvec_len, int* nres);

@@ -669,27 +669,43 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       count_launch();
       std::vector<int> seq(na);
       for (int a = 0; a < na; ++a) seq[a] = a;
-      M(active, Ya.p, Sa.p);
-      std::vector<double> snorm = row_norms(Sa.p, n, seq, n, d_rows, partr, nrm, st);
       const std::vector<double> rnorm = row_norms(Ya.p, n, seq, n, d_rows, partr, nrm, st);
-      // scatter residuals (and their preconditioned form) back
-      for (int a = 0; a < na; ++a) {
+      for (int a = 0; a < na; ++a)
         VH_CUDA_TRY(cudaMemcpyAsync(R.p + (int64_t)active[a] * n, Ya.p + (int64_t)a * n, n * sizeof(double2),
                                     cudaMemcpyDeviceToDevice, st));
-        VH_CUDA_TRY(cudaMemcpyAsync(S.p + (int64_t)active[a] * n, Sa.p + (int64_t)a * n, n * sizeof(double2),
-                                    cudaMemcpyDeviceToDevice, st));
-      }
-      VH_CUDA_TRY(cudaStreamSynchronize(st));
+      // refine until the true FP64 residual meets tol: it is what the flag (pgmres.m:182-186) and the
+      // accuracy of the result depend on (the preconditioner, whatever its arithmetic, sets only the
+      // iteration count).  Only the RHS that go on need M^-1 r, the seed of their next inner solve.
+      std::vector<int> go;   // positions in the compact arrays
       for (int a = 0; a < na; ++a) {
         const int bb = active[a];
-        sn[bb] = snorm[a];
         rn[bb] = rnorm[a];
-        out.resvec[bb].push_back(snorm[a] / mb[bb]);
-        // refine until both the preconditioned and the true FP64 residual meet tol: a single-precision
-        // Schur factor weighs the residual differently from the exact one, and the true residual is
-        // what the flag (pgmres.m:182-186) and the result's accuracy depend on
-        if (snorm[a] > tol[bb] * mb[bb] || rnorm[a] > tol[bb] * bnorm[bb]) still.push_back(bb);
+        out.resvec[bb].push_back(rnorm[a] / bnorm[bb]);
+        if (rnorm[a] > tol[bb] * bnorm[bb]) {
+          go.push_back(a);
+          still.push_back(bb);
+        }
       }
+      if (!go.empty()) {
+        const int ng = (int)go.size();
+        DevBuf<double2> Yg;
+        DevBuf<int> d_go;
+        Yg.ensure((size_t)ng * n);
+        d_go.ensure(ng);
+        VH_CUDA_TRY(cudaMemcpyAsync(d_go.p, go.data(), ng * sizeof(int), cudaMemcpyHostToDevice, st));
+        k_gather<<<dim3(grid1(n), ng), 256, 0, st>>>(Ya.p, n, Yg.p, n, d_go.p, n);
+        count_launch();
+        M(still, Yg.p, Sa.p);
+        std::vector<int> gseq(ng);
+        for (int a = 0; a < ng; ++a) gseq[a] = a;
+        const std::vector<double> snorm = row_norms(Sa.p, n, gseq, n, d_rows, partr, nrm, st);
+        for (int a = 0; a < ng; ++a) {
+          sn[still[a]] = snorm[a];
+          VH_CUDA_TRY(cudaMemcpyAsync(S.p + (int64_t)still[a] * n, Sa.p + (int64_t)a * n, n * sizeof(double2),
+                                      cudaMemcpyDeviceToDevice, st));
+        }
+      }
+      VH_CUDA_TRY(cudaStreamSynchronize(st));
     }
     active.swap(still);
   }
