@@ -154,9 +154,11 @@ vh_status vh_precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const
  *      relres = |b - A x| / |b|, iter = [inner iterations of the last cycle, outer cycles] (2 ints),
  *      resvec (first resvec_len entries, row b at b*resvec_len), nres = its full length.
  *      prec = VH_PREC_FP32: mixed precision -- FP64 iterative refinement around left-preconditioned
- *      GMRES whose FFT matvec runs in complex64, refined until the true residual meets tol; iter then
- *      counts inner iterations / cycles summed over refinement steps and resvec holds the true relative
- *      residual |b - A x| / |b| after each step.                                                 */
+ *      GMRES whose FFT matvec runs in complex64, refined until the residual |b - A x| meets tol: it is
+ *      formed in FP64 after the first refinement step and then updated, r <- r - A d, with the complex64
+ *      product of each (small) correction d, which keeps it within ~1e-6 |A d| (~1e-11 |b| at tol 1e-9)
+ *      of the FP64 residual.  iter then counts inner iterations / cycles summed over refinement steps;
+ *      resvec holds that relative residual after each step, relres its last value.              */
 vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
                    int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
                    double* relres, int* iter, double* resvec, int resvec_len, int* nres);

@@ -248,3 +248,25 @@ def test_mixed_precision_double_float_factor_rl(lib):
     assert np.all(out["flag"] == 0)
     assert_port_matrix_close(out["R"], ref["R"], 1e-6)
     assert_port_matrix_close(out["L"], ref["L"], 1e-6)
+
+
+def test_mixed_precision_relres_is_the_fp64_residual(lib):
+    """Mixed precision updates the residual after the first refinement step with the complex64 product
+    of the correction; the reported relres must still be the FP64 residual |b - A x| / |b| to ~1e-11."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.two_bars(L=24, M=14, N=6, xr=(2, 22), zr=(1, 4), y1=(2, 5), y2=(9, 12))
+    S, P = problem_of(w)
+    freqs = np.array([1e3, 1e8, 1e10])
+    sw = ex.Sweep(P, freqs, precon="schur_invert_df").prepare()
+    out = sw.solve(restart=50, tol=1e-10, maxit=10, prec="fp32")
+    g = sw.geom
+    for k in range(len(out["x"])):
+        f = freqs[k // P.num_ports]
+        s = 1j * 2 * np.pi * f * solver.MU0
+        b = P.rhs[:, k % P.num_ports].astype(complex)
+        r = b - g.matvec(out["x"][k], scale=s)
+        true_rel = np.linalg.norm(r) / np.linalg.norm(b)
+        assert abs(true_rel - out["relres"][k]) < 1e-11
+        assert true_rel < 1e-10 + 2e-11 and out["flag"][k] == 0
