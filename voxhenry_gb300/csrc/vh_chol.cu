@@ -208,20 +208,30 @@ __global__ void __launch_bounds__(256) k_chol_update(const int32_t* __restrict__
     }
 }
 
-// ---- whole-front factorisation in shared memory (fronts with nf <= kFusedMaxNf), one CTA per
-// (front, factor).  The CTA loads the assembled front, adds the children's update matrices and
-// factors the first ns columns right-looking.  Per column j: scale column j (its pivot's square
-// root and reciprocal were taken by the one thread that finished the pivot), barrier, rank-1
-// update of the trailing lower triangle walked as one flat index range (every lane busy),
-// barrier.  It then writes [L11; L21], the update matrix and the inverses of the 32 x 32 diagonal
-// blocks of L11 (the form the triangular solves use) back to the factor storage.
-constexpr int kFusedThreads = 256;
+// ---- whole-front factorisation in shared memory (fronts with nf <= kFusedMaxNf), one CTA of NT
+// threads per (front, factor); NT grows with the front (a single warp up to nf = 64, so that small
+// fronts are not dominated by per-column overhead).  The front's lower triangle is held packed:
+// column k at tri_off(k, nf) - k, rows k..nf-1.  The CTA adds the children's update matrices and
+// factors the first ns columns right-looking with one barrier per column: every thread takes the
+// square root and reciprocal of the pivot itself, updates the trailing triangle with the unscaled
+// column times 1/pivot (walked as one flat index range, every thread busy), and scales the
+// previous column, which no thread reads any more, in the same step.  It then writes [L11; L21],
+// the update matrix and the inverses of the 32 x 32 diagonal blocks of L11 (the form the
+// triangular solves use) back to the factor storage.
 
 // offset of column c in the column-major lower triangle of order m (column c holds m - c entries)
 __host__ __device__ __forceinline__ int tri_off(int c, int m) { return c * m - (c * (c - 1)) / 2; }
 
-template <typename T>
-__global__ void __launch_bounds__(kFusedThreads, 1)
+template <int NT>
+__device__ __forceinline__ void front_bar() {
+  if constexpr (NT == 32)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT)
     k_chol_front(const int32_t* __restrict__ lev, const FrontInfo* __restrict__ fr, const int32_t* __restrict__ relmap,
                  T* const* __restrict__ Wp, int* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char fused_raw[];
@@ -230,12 +240,16 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   T* W = Wp[blockIdx.z];
   const int nf = f.nf, ns = f.ns;
   T* F = W + f.w_off;
-  T* piv_s = S + nf * nf;   // pivot j before its square root
-  T* inv_s = piv_s + ns;    // 1 / L(j, j)
+  T* inv_s = S + nf * (nf + 1) / 2;   // 1 / L(j, j)
+  auto col = [&](int k) { return S + tri_off(k, nf) - k; };   // col(k)[i] = (i, k), i >= k
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int nwarps = kFusedThreads / 32;
-  for (int t = tid; t < nf * nf; t += kFusedThreads) S[t] = F[t];
-  __syncthreads();
+  constexpr int nwarps = NT / 32;
+  for (int k = 0; k < nf; ++k) {
+    T* sk = col(k);
+    const T* fk = F + (int64_t)k * nf;
+    for (int i = k + tid; i < nf; i += NT) sk[i] = fk[i];
+  }
+  front_bar<NT>();
   for (int c = 0; c < 2; ++c) {
     const int ci = f.child[c];
     if (ci < 0) continue;
@@ -243,28 +257,28 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     const int nb = ch.nb;
     const int32_t* rm = relmap + ch.relmap_off;
     const T* U = W + ch.w_off + ch.ns + (int64_t)ch.ns * ch.nf;   // U(a, b) = U[a + b * ch.nf]
-    for (int t = tid; t < nb * nb; t += kFusedThreads) {
+    for (int t = tid; t < nb * nb; t += NT) {
       const int a = t % nb, b = t / nb;
-      if (a >= b) S[rm[a] + rm[b] * nf] += U[a + (int64_t)b * ch.nf];
+      if (a >= b) col(rm[b])[rm[a]] += U[a + (int64_t)b * ch.nf];
     }
-    __syncthreads();
+    front_bar<NT>();
   }
-  if (ns > 0 && tid == 0) {
-    piv_s[0] = S[0];
-    inv_s[0] = rsqrt_t(S[0]);
-  }
-  __syncthreads();
+  T prev_piv = T(0), prev_inv = T(0);
   for (int j = 0; j < ns; ++j) {
-    const T piv = piv_s[j];
-    if (!(piv > T(0))) {          // uniform: every thread reads the same value after a barrier
+    T* colj = col(j);
+    const T piv = colj[j];        // final: updated last in step j-1, before its barrier
+    if (!(piv > T(0))) {          // uniform: every thread reads the same value
       if (tid == 0) atomicExch(err, 1);
       return;
     }
-    const T inv = inv_s[j];
-    T* colj = S + j * nf;
-    for (int i = j + tid; i < nf; i += kFusedThreads) colj[i] = (i == j) ? piv * inv : colj[i] * inv;
-    __syncthreads();
-    // S(i, k) -= L(i, j) L(k, j) for j < k <= i < nf: trailing column c = k - j - 1 holds m - c entries
+    const T inv = rsqrt_t(piv);
+    const T inv2 = inv * inv;
+    if (tid == 0) inv_s[j] = inv;
+    if (j > 0) {                  // deferred scaling of column j-1
+      T* colp = col(j - 1);
+      for (int i = j - 1 + tid; i < nf; i += NT) colp[i] = (i == j - 1) ? prev_piv * prev_inv : colp[i] * prev_inv;
+    }
+    // S(i, k) -= S(i, j) S(k, j) / piv for j < k <= i < nf: trailing column c = k - j - 1 holds m - c entries
     const int m = nf - j - 1;
     const int total = (m * (m + 1)) / 2;
     if (tid < total) {
@@ -274,36 +288,40 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       while (c > 0 && tri_off(c, m) > tid) --c;
       while (c + 1 < m && tri_off(c + 1, m) <= tid) ++c;
       int p = tid - tri_off(c, m);   // position within column c: row k + p
-      T coef = colj[j + 1 + c];
-      T* colk = S + (j + 1 + c) * nf;
+      T coef = colj[j + 1 + c] * inv2;
+      T* colk = col(j + 1 + c);
       for (;;) {
         const int i = j + 1 + c + p;
         colk[i] = fma(-colj[i], coef, colk[i]);
-        p += kFusedThreads;
+        p += NT;
         if (p >= m - c) {
           do {
             p -= m - c;
             ++c;
           } while (c < m && p >= m - c);
           if (c >= m) break;
-          coef = colj[j + 1 + c];
-          colk = S + (j + 1 + c) * nf;
+          coef = colj[j + 1 + c] * inv2;
+          colk = col(j + 1 + c);
         }
       }
-      if (tid == 0 && j + 1 < ns) {   // thread 0 owns element (j+1, j+1): the next pivot
-        const T pn = S[(j + 1) + (j + 1) * nf];
-        piv_s[j + 1] = pn;
-        inv_s[j + 1] = rsqrt_t(pn);
-      }
     }
-    __syncthreads();
+    prev_piv = piv;
+    prev_inv = inv;
+    front_bar<NT>();
   }
+  if (ns > 0) {
+    T* colp = col(ns - 1);
+    for (int i = ns - 1 + tid; i < nf; i += NT) colp[i] = (i == ns - 1) ? prev_piv * prev_inv : colp[i] * prev_inv;
+  }
+  front_bar<NT>();
   // lower triangle back to the factor storage, except the diagonal blocks of L11 (inverted below)
-  for (int t = tid; t < nf * nf; t += kFusedThreads) {
-    const int i = t % nf, j = t / nf;
-    if (i < j) continue;
-    if (i < ns && (i >> 5) == (j >> 5)) continue;
-    F[t] = S[t];
+  for (int k = 0; k < nf; ++k) {
+    const T* sk = col(k);
+    T* fk = F + (int64_t)k * nf;
+    for (int i = k + tid; i < nf; i += NT) {
+      if (i < ns && (i >> 5) == (k >> 5)) continue;
+      fk[i] = sk[i];
+    }
   }
   // inverses of the diagonal blocks: lane j of a warp computes column j of L_blk^-1
   const int nblk = (ns + 31) >> 5;
@@ -316,7 +334,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       F[(k0 + j) + (int64_t)(k0 + j) * nf] = iv[j];
       for (int i = j + 1; i < w; ++i) {
         T acc = T(0);
-        for (int k = j; k < i; ++k) acc = fma(S[(k0 + i) + (k0 + k) * nf], iv[k], acc);
+        for (int k = j; k < i; ++k) acc = fma(col(k0 + k)[k0 + i], iv[k], acc);
         iv[i] = -acc * inv_s[k0 + i];
         F[(k0 + i) + (int64_t)(k0 + j) * nf] = iv[i];
       }
@@ -324,9 +342,33 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   }
 }
 
+// packed lower triangle plus the reciprocal pivots
 template <typename T>
 static size_t fused_smem_bytes(int max_nf, int max_ns) {
-  return ((size_t)max_nf * max_nf + 2 * (size_t)max_ns) * sizeof(T);
+  return ((size_t)max_nf * (max_nf + 1) / 2 + (size_t)max_ns) * sizeof(T);
+}
+
+// CTA size for fronts up to order max_nf: one warp up to 64, then 2, 4, 8 warps
+static int fused_threads(int max_nf) { return max_nf <= 64 ? 32 : (max_nf <= 96 ? 64 : (max_nf <= 128 ? 128 : 256)); }
+
+template <typename T, int NT>
+static void launch_front_nt(const int32_t* lev, unsigned count, unsigned nz, size_t sm, const CholSymbolic& s,
+                            T* const* Wp, int* d_err, cudaStream_t st) {
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_front<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_chol_front<T, NT><<<dim3(count, 1, nz), NT, sm, st>>>(lev, s.d_fronts, s.d_relmap, Wp, d_err);
+  count_launch();
+  VH_CUDA_TRY(cudaGetLastError());
+}
+
+template <typename T>
+static void launch_front(int max_nf, const int32_t* lev, unsigned count, unsigned nz, size_t sm, const CholSymbolic& s,
+                         T* const* Wp, int* d_err, cudaStream_t st) {
+  switch (fused_threads(max_nf)) {
+    case 32: launch_front_nt<T, 32>(lev, count, nz, sm, s, Wp, d_err, st); break;
+    case 64: launch_front_nt<T, 64>(lev, count, nz, sm, s, Wp, d_err, st); break;
+    case 128: launch_front_nt<T, 128>(lev, count, nz, sm, s, Wp, d_err, st); break;
+    default: launch_front_nt<T, 256>(lev, count, nz, sm, s, Wp, d_err, st); break;
+  }
 }
 
 template <typename T>
@@ -357,19 +399,10 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* con
     k_chol_assemble<T><<<dim3(s.nfronts, 1, nz), 256, 0, st>>>(s.d_fronts, s.d_asm, s.d_asm_q, s.d_asm_c, Dp, Wp);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
-    size_t fused_max = 0;
-    for (size_t hl = 0; hl < s.levels.size(); ++hl)
-      fused_max = std::max(fused_max, fused_smem_bytes<T>(s.fused_max_nf[hl], s.fused_max_ns[hl]));
-    if (fused_max > 0)
-      VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_front<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_max));
     for (size_t hl = 0; hl < s.levels.size(); ++hl) {
-      for (const auto& fc : s.fused_classes[hl]) {
-        const size_t sm = fused_smem_bytes<T>(fc.max_nf, fc.max_ns);
-        k_chol_front<T><<<dim3((unsigned)fc.count, 1, nz), kFusedThreads, sm, st>>>(
-            s.d_levels_fused[hl] + fc.offset, s.d_fronts, s.d_relmap, Wp, d_err);
-        count_launch();
-        VH_CUDA_TRY(cudaGetLastError());
-      }
+      for (const auto& fc : s.fused_classes[hl])
+        launch_front<T>(fc.max_nf, s.d_levels_fused[hl] + fc.offset, (unsigned)fc.count, nz,
+                        fused_smem_bytes<T>(fc.max_nf, fc.max_ns), s, Wp, d_err, st);
       if (s.levels_blocked[hl].empty()) continue;
       const unsigned nf = (unsigned)s.levels_blocked[hl].size();
       const int32_t* lev = s.d_levels_blocked[hl];
