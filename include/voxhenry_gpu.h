@@ -40,14 +40,16 @@ typedef enum vh_status {
 /* arithmetic of the FFT convolution: complex128, or complex64 with fp32 accumulation */
 typedef enum vh_prec { VH_PREC_FP64 = 0, VH_PREC_FP32 = 1 } vh_prec;
 
-/* preconditioner kinds of lse_sparse_precon_prepare.m:5,71,83,90 */
+/* preconditioner kinds of lse_sparse_precon_prepare.m:5,71,83,90 ('schur_gmres' is not provided) */
 typedef enum vh_precon_kind {
   VH_PRECON_NONE = 0,            /* 'no_precond' */
   VH_PRECON_SCHUR_INVERT = 1,    /* 'schur_invert' : exact Schur complement, sparse Cholesky in FP64 */
-  VH_PRECON_SCHUR_INVERT_DF = 2  /* 'schur_invert' with the factor and its triangular solves in double-float
+  VH_PRECON_SCHUR_INVERT_DF = 2, /* 'schur_invert' with the factor and its triangular solves in double-float
                                     (FP32 pairs, ~48 significant bits, on GB300's FP32 pipes); no counterpart
                                     in the reference.  For the mixed-precision solver (VH_PREC_FP32), whose FP64
                                     residuals set the accuracy; FP64 solves to 1e-12 want VH_PRECON_SCHUR_INVERT */
+  VH_PRECON_SCHUR_APPROX = 3     /* 'schur_approx' (lse_sparse_precon_prepare.m:71-81, multiply.m:48-58): S^-1
+                                    replaced by W Ae diag(A_inv)^-1 Ae^T W, W = diag(1 / sum_k |Ae(:,k)|); no factor */
 } vh_precon_kind;
 
 typedef struct vh_ctx vh_ctx;

@@ -270,3 +270,44 @@ def test_mixed_precision_relres_is_the_fp64_residual(lib):
         true_rel = np.linalg.norm(r) / np.linalg.norm(b)
         assert abs(true_rel - out["relres"][k]) < 1e-11
         assert true_rel < 1e-10 + 2e-11 and out["flag"][k] == 0
+
+
+def test_precon_schur_approx_matches_oracle(lib, blob):
+    """'schur_approx' (lse_sparse_precon_prepare.m:71-81, lse_sparse_precon_multiply.m:48-58)."""
+    vie, ex = lib
+    w, S, P = blob
+    om = 2 * np.pi * 3e8
+    jwmu = 1j * om * solver.MU0
+    z_real, _ = solver.z_arrays(w.sigma_e, None, om)
+    ref = solver.SparsePrecon("schur_approx").prepare(S.dx, z_real, None, S.idxS, jwmu * P.st2, S.Ar)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS)
+    pcs = g.precons(np.stack([jwmu * P.st2] * 3), kind="schur_approx")
+    rng = np.random.default_rng(23)
+    X = rng.standard_normal((3, S.n)) + 1j * rng.standard_normal((3, S.n))
+    Y = vie.apply_precons(g, pcs, X)
+    for k in range(3):
+        assert rel(Y[k], ref.multiply(X[k])) < 1e-12
+
+
+def test_pgmres_schur_approx_matches_oracle(lib, blob):
+    """pgmres with the 'schur_approx' preconditioner through the drop-in calls: the same iterations as
+    the oracle (this weak preconditioner does not reach tol here in either; both report flag 1)."""
+    vie, ex = lib
+    w, S, P = blob
+    om = 2 * np.pi * 1e9
+    jwmu = 1j * om * solver.MU0
+    fN = jwmu * P.fN_all2
+    st = jwmu * P.st2
+    z_real, _ = solver.z_arrays(w.sigma_e, None, om)
+    vie.lse_sparse_precon_prepare(S.dx, z_real, None, S.idxS, st, None, None, S.Ar, kind="schur_approx")
+    A = vie.matvec_handle(fN, S.Ar, z_real, None, S.dx, S.idxS5)
+    b = S.rhs[:, 0].astype(complex)
+    xg, flag, relres, it, resvec = vie.pgmres(A, b, 20, 1e-10, 2, vie.precon_handle())
+    ref = solver.SparsePrecon("schur_approx").prepare(S.dx, z_real, None, S.idxS, st, S.Ar)
+    Aref = lambda J: solver.lse_matvect_mult(J, fN, S.Ar, z_real, None, S.dx, S.idxS5)
+    xo, flag_o, relres_o, it_o, resvec_o = solver.pgmres(Aref, b, 20, 1e-10, 2, ref.multiply)
+    assert flag == flag_o
+    assert tuple(it) == tuple(it_o) and len(resvec) == len(resvec_o)
+    np.testing.assert_allclose(resvec, resvec_o, rtol=1e-6)
+    assert abs(relres - relres_o) <= 1e-6 * relres_o
+    assert rel(xg, xo) < 1e-8

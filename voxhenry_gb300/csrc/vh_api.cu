@@ -329,6 +329,7 @@ void geom_release(vh_geom* g) {
   g->chol.free_all();
   cudaFree(g->pc_tmp);
   cudaFree(g->pc_phi_df);
+  cudaFree(g->approx_w);
   cudaFree(g->pc_ptrs);
   for (auto* z : g->zslots) cudaFree(z);
   cudaFree(g->ones);

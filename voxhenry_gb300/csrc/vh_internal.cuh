@@ -72,6 +72,7 @@ struct vh_geom {
   bool chol_ready = false;
   double2* pc_tmp = nullptr;       // chol_solve update vectors, B * u_total (16-byte complex values)
   void* pc_phi_df = nullptr;       // double-float factor: B * nphi pair-complex panel values being solved
+  double* approx_w = nullptr;      // 'schur_approx': 1 / sum_k |Ae(r, k)| per panel row r (device)
   size_t pc_phi_df_cap = 0;
   size_t pc_tmp_cap = 0;
   double** pc_ptrs = nullptr;      // device pointer tables (A_inv, W) for batched applies

@@ -5,6 +5,7 @@
 //   S = Ar A_inv Ar^T, factored (sparse Cholesky; the reference uses CHOLMOD LDL^T or LU).
 // multiply (lse_sparse_precon_multiply.m:61-88):
 //   bb = x_phi - Ar (A_inv x_J);  phi = S^-1 bb;  y_J = (x_J + Ar^T phi) A_inv;  y_phi = phi.
+#include <cmath>
 #include <vector>
 
 #include "../../include/voxhenry_gpu.h"
@@ -89,6 +90,43 @@ __global__ void k_precon_finish(int64_t nc, int64_t nphi, const int32_t* __restr
   }
 }
 
+// y[b][r] = x[b][r] * w[r]  (x, y may alias)
+__global__ void k_row_scale(const double2* x, int64_t ldx, const double* __restrict__ w, double2* y, int64_t ldy,
+                            int64_t rows) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (r >= rows) return;
+  const double2 v = x[b * ldx + r];
+  y[b * ldy + r] = make_double2(v.x * w[r], v.y * w[r]);
+}
+
+// x[b][q] /= A_inv_b[q]  (the diagonal A_noninv of lse_sparse_precon_prepare.m:76)
+__global__ void k_div_ainv(double2* x, int64_t ldx, double* const* __restrict__ ainv, int64_t rows) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (q >= rows) return;
+  const double a = ainv[b][q];
+  double2 v = x[b * ldx + q];
+  v.x /= a;
+  v.y /= a;
+  x[b * ldx + q] = v;
+}
+
+// W = diag(1 / sum_k |Ae(r, k)|) of lse_sparse_precon_prepare.m:78, once per geometry
+void ensure_approx_w(vh_geom* g) {
+  if (g->approx_w || g->nphi == 0) return;
+  std::vector<double> w(g->nphi);
+  for (int64_t r = 0; r < g->nphi; ++r) {
+    double s = 0.0;
+    for (int32_t k = g->hAe.rp[r]; k < g->hAe.rp[r + 1]; ++k) s += std::fabs(g->hAe.val[k]);
+    VH_REQUIRE(s > 0.0, ERR_BAD_ARG, "panel node without incident currents");
+    w[r] = 1.0 / s;
+  }
+  VH_CUDA_TRY(cudaMalloc(&g->approx_w, g->nphi * sizeof(double)));
+  VH_CUDA_TRY(cudaMemcpyAsync(g->approx_w, w.data(), g->nphi * sizeof(double), cudaMemcpyHostToDevice, g->ctx->stream));
+  VH_CUDA_TRY(cudaStreamSynchronize(g->ctx->stream));
+}
+
 void ensure_symbolic(vh_geom* g) {
   if (g->chol_ready) return;
   chol_symbolic(g->chol, g->L, g->M, g->N, g->nv, g->idxS.data(), g->nphi, g->hAe.rp, g->hAe.col, g->hAe.val,
@@ -134,6 +172,38 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
     g->pc_tmp_cap = 0;
     VH_CUDA_TRY(cudaMalloc(&g->pc_tmp, need * sizeof(double2)));
     g->pc_tmp_cap = need;
+  }
+  if (kind == VH_PRECON_SCHUR_APPROX) {   // lse_sparse_precon_multiply.m:48-58
+    const int64_t nc = g->nc, nphi = g->nphi;
+    double2* tmp = static_cast<double2*>(g->ctx->pool.get((size_t)B * std::max<int64_t>(1, g->n) * sizeof(double2)));
+    double2* t1 = tmp;                      // B x nphi
+    double2* t2 = tmp + (size_t)B * nphi;   // B x nc
+    if (nphi > 0) {
+      const dim3 gp((unsigned)ceil_div(nphi, 256), B), gc((unsigned)std::max<int64_t>(1, ceil_div(nc, 256)), B);
+      k_precon_rhs<double2><<<gp, 256, 0, st>>>(nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val, d_ainv, x, g->n, nc,
+                                                y + nc, g->n);   // bb
+      count_launch();
+      k_row_scale<<<gp, 256, 0, st>>>(y + nc, g->n, g->approx_w, t1, nphi, nphi);   // W bb
+      count_launch();
+      spmv_batched(g->AeT, B, t1, nphi, 0, t2, nc, 0, 0, st);                        // Ae^T W bb
+      if (nc > 0) {
+        k_div_ainv<<<gc, 256, 0, st>>>(t2, nc, d_ainv, nc);                          // A_noninv (...)
+        count_launch();
+      }
+      spmv_batched(g->Ae, B, t2, nc, 0, y, g->n, nc, 0, st);                          // Ae (...)
+      k_row_scale<<<gp, 256, 0, st>>>(y + nc, g->n, g->approx_w, y + nc, g->n, nphi);   // W (...)
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+    }
+    if (nc > 0) {
+      k_precon_finish<double2><<<dim3((unsigned)ceil_div(nc, 256), B), 256, 0, st>>>(
+          nc, nphi, g->AeT.rowptr, g->AeT.col, g->AeT.val, d_ainv, x, y, g->n, y + nc, g->n, false);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+    }
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    g->ctx->pool.put(tmp);
+    return;
   }
   dcomplex* phi_df = nullptr;
   if (df) {
@@ -214,14 +284,19 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
     ps[i]->kind = kind;
   }
   vh_status s = guarded_pc(g->ctx, [&] {
-    VH_REQUIRE(kind == VH_PRECON_NONE || kind == VH_PRECON_SCHUR_INVERT || kind == VH_PRECON_SCHUR_INVERT_DF,
-               ERR_UNSUPPORTED, "preconditioner kind not supported (schur_approx / schur_gmres / schur_invert_original)");
+    VH_REQUIRE(kind == VH_PRECON_NONE || kind == VH_PRECON_SCHUR_INVERT || kind == VH_PRECON_SCHUR_INVERT_DF ||
+                   kind == VH_PRECON_SCHUR_APPROX,
+               ERR_UNSUPPORTED, "preconditioner kind not supported (schur_gmres / schur_invert_original)");
     const bool df = kind == VH_PRECON_SCHUR_INVERT_DF;
+    const bool approx = kind == VH_PRECON_SCHUR_APPROX;
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     if (kind == VH_PRECON_NONE) return;
     VH_REQUIRE(st_sparse_precon, ERR_BAD_ARG, "st_sparse_precon is required");
     cudaStream_t st = g->ctx->stream;
-    ensure_symbolic(g);
+    if (approx)
+      ensure_approx_w(g);
+    else
+      ensure_symbolic(g);
     std::vector<const double*> D(nfreq);
     std::vector<void*> W(nfreq);
     for (int i = 0; i < nfreq; ++i) {
@@ -231,7 +306,7 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
       p->A_inv = static_cast<double*>(g->ctx->pool.get(std::max<int64_t>(1, g->nc) * sizeof(double)));
       p->df = df;
       static_assert(sizeof(dfloat) == sizeof(double), "pair factor entries take a double's storage");
-      p->W = g->ctx->pool.get(std::max<int64_t>(1, g->chol.w_total) * sizeof(double));
+      if (!approx) p->W = g->ctx->pool.get(std::max<int64_t>(1, g->chol.w_total) * sizeof(double));
       const double* sp = st_sparse_precon + 6 * i;
       const double2 s1 = make_double2(sp[0], sp[1]), s2 = make_double2(sp[2], sp[3]), s3 = make_double2(sp[4], sp[5]);
       if (g->nv) {
@@ -241,6 +316,10 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
       VH_CUDA_TRY(cudaGetLastError());
       D[i] = p->A_inv;
       W[i] = p->W;
+    }
+    if (approx) {
+      VH_CUDA_TRY(cudaStreamSynchronize(st));
+      return;
     }
     ProfScope prof(&g->ctx->prof, SEC_FACTOR, st, nfreq);
     if (df)

@@ -201,7 +201,7 @@ class Geometry:
             pass
 
 
-PRECON_KIND = {"no_precond": 0, "schur_invert": 1, "schur_invert_df": 2}
+PRECON_KIND = {"no_precond": 0, "schur_invert": 1, "schur_invert_df": 2, "schur_approx": 3}
 
 
 class Precon:
