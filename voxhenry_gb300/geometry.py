@@ -161,3 +161,14 @@ CONFIGS = {
     "C3": two_bars,
     "C4": ring,
 }
+
+
+def from_vhr(path_or_model, name: str | None = None) -> Workload:
+    """A workload from a .vhr file (or a parsed vhr.VhrModel): the inputs of VoxHenry_executer.m."""
+    from . import vhr
+
+    m = vhr.read(path_or_model) if isinstance(path_or_model, str) else path_or_model
+    lam = m.lambdaL if m.lambdaL is not None and np.any(m.lambdaL) else None
+    return Workload(name or (path_or_model if isinstance(path_or_model, str) else "vhr"), m.sigma_e, m.dx,
+                    list(m.pnt_lft), list(m.pnt_rght), np.asarray(m.freq, dtype=np.float64), lambdaL=lam,
+                    meta={"pnt_well_cond": m.pnt_well_cond, "portnames": m.portnames})
