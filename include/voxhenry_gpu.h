@@ -194,6 +194,19 @@ vh_status vh_incidence(int64_t nv, const int64_t* all_panels_ids, int64_t* Ae_jc
  *   complex (2L, 2M, 2N, 7) column-major; st_sparse_precon (HOST, may be NULL): 3 complex.       */
 vh_status vh_circulant_tensor(vh_ctx* ctx, int L, int M, int N, double dx, double* fN_all, double* st_sparse_precon);
 
+/* ---- post-processing of the currents (src_post_process) -----------------------------------------
+ * [Jx,Jy,Jz,J2d,J3d] grids of post_obtain_curr_coefs_on_grid(x, Mc) (post_obtain_curr_coefs_on_grid.m:1):
+ *   x: HOST, B solutions (complex, leading dimension ldx >= 5 nv, current coefficients first);
+ *   grids: HOST, B x 5 x (L M N) complex, column-major grids, zero outside the voxels; scattered on
+ *   the device.  idxS: the nv 1-based voxel indices (pre_define_structure_params.m:6-14).        */
+vh_status vh_currents_on_grid(vh_ctx* ctx, int L, int M, int N, int64_t nv, const int64_t* idxS, int B,
+                              const double* x, int64_t ldx, double* grids);
+/* y = A x for a real CSC matrix A (nrows x ncols, 0-based ir) and B complex HOST vectors (leading
+ * dimensions ldx, ldy), on the device: the node currents -Ae_only_leaving x + Ae_only_entering_bndry x
+ * of post_obtain_currs_on_nodes.m:7-9 (one product with the difference matrix).                */
+vh_status vh_sparse_matvec(vh_ctx* ctx, int64_t nrows, int64_t ncols, const int64_t* jc, const int64_t* ir,
+                           const double* pr, int B, const double* x, int64_t ldx, double* y, int64_t ldy);
+
 #ifdef __cplusplus
 }
 #endif

@@ -311,3 +311,30 @@ def test_pgmres_schur_approx_matches_oracle(lib, blob):
     np.testing.assert_allclose(resvec, resvec_o, rtol=1e-6)
     assert abs(relres - relres_o) <= 1e-6 * relres_o
     assert rel(xg, xo) < 1e-8
+
+
+def test_sharded_sweep_with_gpu_solver(lib):
+    """sharding.sweep_distributed with the GPU Sweep solver (one gloo rank on this process) gives the
+    same R, L as a direct Sweep over all frequencies."""
+    import socket
+
+    import torch.distributed as dist
+
+    vie, ex = lib
+    from voxhenry_gb300 import geometry, sharding
+
+    w = geometry.two_bars(L=24, M=14, N=6, xr=(2, 22), zr=(1, 4), y1=(2, 5), y2=(9, 12))
+    S, P = problem_of(w)
+    freqs = np.array([1e3, 1e7, 5e9])
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    try:
+        out = sharding.sweep_distributed(freqs, sharding.gpu_sweep_solver(P, tol=1e-12))
+    finally:
+        dist.destroy_process_group()
+    ref = ex.Sweep(P, freqs).prepare().solve(restart=50, tol=1e-12, maxit=10)
+    np.testing.assert_array_equal(out["R"], ref["R"])
+    np.testing.assert_array_equal(out["L"], ref["L"])
+    assert np.all(out["flag"] == 0)
