@@ -40,7 +40,7 @@ typedef enum vh_status {
 /* arithmetic of the FFT convolution: complex128, or complex64 with fp32 accumulation */
 typedef enum vh_prec { VH_PREC_FP64 = 0, VH_PREC_FP32 = 1 } vh_prec;
 
-/* preconditioner kinds of lse_sparse_precon_prepare.m:5,71,83,90 ('schur_gmres' is not provided) */
+/* preconditioner kinds of lse_sparse_precon_prepare.m:5,71,83,90 ('schur_invert_original' is not provided) */
 typedef enum vh_precon_kind {
   VH_PRECON_NONE = 0,            /* 'no_precond' */
   VH_PRECON_SCHUR_INVERT = 1,    /* 'schur_invert' : exact Schur complement, sparse Cholesky in FP64 */
@@ -48,8 +48,14 @@ typedef enum vh_precon_kind {
                                     (FP32 pairs, ~48 significant bits, on GB300's FP32 pipes); no counterpart
                                     in the reference.  For the mixed-precision solver (VH_PREC_FP32), whose FP64
                                     residuals set the accuracy; FP64 solves to 1e-12 want VH_PRECON_SCHUR_INVERT */
-  VH_PRECON_SCHUR_APPROX = 3     /* 'schur_approx' (lse_sparse_precon_prepare.m:71-81, multiply.m:48-58): S^-1
+  VH_PRECON_SCHUR_APPROX = 3,    /* 'schur_approx' (lse_sparse_precon_prepare.m:71-81, multiply.m:48-58): S^-1
                                     replaced by W Ae diag(A_inv)^-1 Ae^T W, W = diag(1 / sum_k |Ae(:,k)|); no factor */
+  VH_PRECON_SCHUR_GMRES = 4      /* 'schur_gmres' (prepare.m:83-88, multiply.m:26-46): S^-1 applied by an inner
+                                    restarted GMRES on S = Ae diag(A_inv) Ae^T with the Jacobi preconditioner
+                                    diag(S), restart min(100, num_curr - 1), at most 10 cycles, tolerance prectol
+                                    (vh_precon_set_prectol; 0.1 as VoxHenry_executer.m:38).  The apply is not a
+                                    fixed linear operator: use it with flexible GMRES (VoxHenry_executer.m:294-297);
+                                    the mixed-precision solver rejects it. */
 } vh_precon_kind;
 
 typedef struct vh_ctx vh_ctx;
@@ -135,6 +141,10 @@ vh_status vh_precon_create(vh_geom* g, vh_precon_kind kind, const double* st_spa
 vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, const double* st_sparse_precon,
                                  const int* zslot, vh_precon** out);
 void vh_precon_destroy(vh_precon* p);
+/* 'schur_gmres': the `prectol` argument of lse_sparse_precon_multiply.m:1 (default 0.1), and the inner GMRES
+ * iterations summed over every apply of this handle so far (the reference prints them, multiply.m:44). */
+vh_status vh_precon_set_prectol(vh_precon* p, double prectol);
+vh_status vh_precon_inner_iterations(const vh_precon* p, int64_t* total);
 /* factor statistics: entries of L, factorisation flops, fronts, largest front order */
 vh_status vh_precon_stats(const vh_precon* p, int64_t* nnz_factor, double* flops, int* nfronts, int* max_front);
 /* host-only symbolic analysis of S = Ae diag Ae^T (no device needed): same statistics plus the bytes of

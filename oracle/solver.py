@@ -119,9 +119,32 @@ class SparsePrecon:
             self.A_noninv = 1.0 / self.A_inv
             w = np.asarray(abs(self.Ae).sum(axis=1)).ravel()
             self.Wd = 1.0 / w
+        elif self.kind == "schur_gmres":
+            # prepare.m:83-88: S = Ae A_inv Ae', precond = diag(S); S v by lse_sparse_schur_compl_multiply.m:3
+            self.S = (self.Ae @ sp.diags(self.A_inv) @ self.AeT).tocsr()
+            self.Sd = self.S.diagonal()
+            self.prectol = 0.1            # VoxHenry_executer.m:38
+            self.inner_iters = 0
         else:
             raise NotImplementedError(self.kind)
         return self
+
+    def schur_gmres_solve(self, bb):
+        """multiply.m:43: gmres(fPSchur, bb, min(100, num_curr - 1), prectol, 10, precond).
+
+        The inner solver is MATLAB's built-in gmres (not part of the reference's sources).  Restated from
+        its published algorithm: restarted GMRES (Saad & Schultz 1986) with x0 = 0 and the left
+        preconditioner M = precond = diag(S), stopping when the preconditioned relative residual
+        |M^-1 (bb - S x)| / |M^-1 bb| <= prectol; a zero right-hand side gives x = 0.  The restatement
+        orthogonalises by classical Gram-Schmidt (the oracle's pgmres) where MATLAB uses Householder
+        reflections: the same Krylov minimiser in exact arithmetic."""
+        if not np.any(bb):
+            return np.zeros_like(bb)
+        nc = self.Ae.shape[1]
+        x, _, _, _, resvec = pgmres(lambda v: self.S @ v, bb, restart=min(100, nc - 1), tol=self.prectol,
+                                    maxit=10, L1=lambda v: v / self.Sd)
+        self.inner_iters += len(resvec) - 1
+        return x
 
     def solve_S(self, b):
         # the factor is real; apply it to the real and imaginary parts
@@ -130,7 +153,7 @@ class SparsePrecon:
         return self.lu.solve(b)
 
     def multiply(self, x):
-        """lse_sparse_precon_multiply.m:61-117 (schur_invert), :48-58 (schur_approx)."""
+        """lse_sparse_precon_multiply.m:61-117 (schur_invert), :48-58 (schur_approx), :26-46 (schur_gmres)."""
         if self.kind == "no_precond":
             return x.copy()
         nc = self.Ae.shape[1]
@@ -140,6 +163,8 @@ class SparsePrecon:
         bb = b - self.Ae @ (self.A_inv * a)
         if self.kind == "schur_invert":
             out[nc:] = self.solve_S(bb)
+        elif self.kind == "schur_gmres":
+            out[nc:] = self.schur_gmres_solve(bb)
         else:
             t = self.AeT @ (self.Wd * bb)
             out[nc:] = self.Wd * (self.Ae @ (self.A_noninv * t))
@@ -280,7 +305,10 @@ def solve_frequencies(sysm, fN_all2, st2, freqs, restart=100, maxit=10, tol=None
         A = lambda J: lse_matvect_mult(J, fN, sysm.Ar, z_real, z_imag, sysm.dx, sysm.idxS5)
         for p in range(P):
             b = sysm.rhs[:, p].astype(np.complex128)
-            x, flag, relres, it, resvec = pgmres(A, b, restart, t, maxit, pc.multiply)
+            if precon == "schur_gmres":   # VoxHenry_executer.m:294-297: the flexible solver
+                x, flag, relres, it, resvec = fpgmres(A, b, restart, t, maxit, pc.multiply)
+            else:
+                x, flag, relres, it, resvec = pgmres(A, b, restart, t, maxit, pc.multiply)
             Y[fi, :, p] = sysm.rhs.T @ x                  # sum(rhs(:,kk).*x), no conjugate
             iters.append((f, p, len(resvec) - 1, relres))
             if keep_x:

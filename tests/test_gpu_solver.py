@@ -338,3 +338,60 @@ def test_sharded_sweep_with_gpu_solver(lib):
     np.testing.assert_array_equal(out["R"], ref["R"])
     np.testing.assert_array_equal(out["L"], ref["L"])
     assert np.all(out["flag"] == 0)
+
+
+@pytest.mark.parametrize("f", [1e6, 3e9])
+def test_precon_schur_gmres_matches_oracle(lib, blob, f):
+    """'schur_gmres' (lse_sparse_precon_prepare.m:83-88, lse_sparse_precon_multiply.m:26-46): the inner
+    Jacobi-preconditioned GMRES on S takes the oracle's iteration counts and returns its result, for a
+    batch mixing frequencies, a zero right-hand side and two inner tolerances."""
+    vie, ex = lib
+    w, S, P = blob
+    fs = [f, 10 * f]
+    st = np.stack([1j * 2 * np.pi * fq * solver.MU0 * P.st2 for fq in fs])
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 2 * np.pi * f)   # conductors only: z does not depend on f
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS)
+    pcs = g.precons(st, kind="schur_gmres")
+    pcs[1].set_prectol(1e-3)
+    refs = [solver.SparsePrecon("schur_gmres").prepare(S.dx, z_real, None, S.idxS, st[i], S.Ar) for i in range(2)]
+    refs[1].prectol = 1e-3
+    rng = np.random.default_rng(29)
+    X = rng.standard_normal((3, S.n)) + 1j * rng.standard_normal((3, S.n))
+    X[2] = 0.0
+    batch = [pcs[0], pcs[1], pcs[0]]
+    Y = vie.apply_precons(g, batch, X)
+    for k, i in enumerate([0, 1, 0]):
+        ref = refs[i].multiply(X[k])
+        if k == 2:
+            assert not np.any(Y[k]) and not np.any(ref)
+        else:
+            assert rel(Y[k], ref) < 1e-10, k
+    assert pcs[0].inner_iterations() == refs[0].inner_iters > 0
+    assert pcs[1].inner_iterations() == refs[1].inner_iters > refs[0].inner_iters / 2
+
+
+def test_fpgmres_schur_gmres_sweep_matches_oracle(lib):
+    """The executer's 'schur_gmres' path (flexible outer GMRES, VoxHenry_executer.m:294-297) on two
+    bars: converged, with the oracle's outer iterations and R, L."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.two_bars(L=16, M=10, N=5, xr=(1, 15), zr=(1, 3), y1=(1, 3), y2=(6, 8))
+    S, P = problem_of(w)
+    freqs = np.array([1e6, 1e9, 2e10])
+    sw = ex.Sweep(P, freqs, precon="schur_gmres").prepare()
+    out = sw.solve(restart=50, tol=1e-10, maxit=10)
+    fN, st = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
+    ref = solver.solve_frequencies(S, fN, st, freqs, restart=50, tol=1e-10, precon="schur_gmres")
+    assert np.all(out["flag"] == 0)
+    assert [len(r) - 1 for r in out["resvec"]] == [i[2] for i in ref["iters"]]
+    assert_port_matrix_close(out["R"], ref["R"], 1e-8)
+    assert_port_matrix_close(out["L"], ref["L"], 1e-8)
+
+
+def test_mixed_precision_rejects_schur_gmres(lib, blob):
+    vie, ex = lib
+    w, S, P = blob
+    sw = ex.Sweep(P, np.array([1e9]), precon="schur_gmres").prepare()
+    with pytest.raises(Exception, match="schur_gmres"):
+        sw.solve(restart=20, tol=1e-8, maxit=2, prec="fp32")

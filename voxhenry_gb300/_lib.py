@@ -45,6 +45,8 @@ SIGNATURES = {
     "vh_precon_destroy": (None, [_p]),
     "vh_precon_create_batch": (C.c_int, [_p, C.c_int, C.c_int, _dp, _ip, C.POINTER(_p)]),
     "vh_precon_stats": (C.c_int, [_p, _i64p, _dp, _ip, _ip]),
+    "vh_precon_set_prectol": (C.c_int, [_p, C.c_double]),
+    "vh_precon_inner_iterations": (C.c_int, [_p, _i64p]),
     "vh_schur_analyze": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, _i64p, C.c_int64, _i64p, _i64p, _dp,
                                    _i64p, _dp, _ip, _ip, _i64p]),
     "vh_precon_apply": (C.c_int, [_p, C.c_int, C.POINTER(_p), _dp, _dp]),

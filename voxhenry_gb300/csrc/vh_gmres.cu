@@ -274,21 +274,13 @@ std::vector<double> row_norms(const double2* x, int64_t ldx, const std::vector<i
 
 namespace vh {
 
-struct GmresOut {
-  std::vector<int> flag, inner, outer;
-  std::vector<double> relres;
-  std::vector<std::vector<double>> resvec;
-  int64_t matvecs = 0;   // RHS-matvecs performed
-  int64_t precons = 0;
-};
-
-// Restarted (F)GMRES for B right-hand sides.  b, x: device, B x n (ld n).  x holds x0 on entry
-// (zero vector allowed).  scale/zslot: host arrays of B.  pcs: B preconditioners or nullptr.
-void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, const double2* scale_h,
-                  const int* zslot_h, const double* tol, int m, int maxit, bool flexible, Prec prec, double2* x,
-                  GmresOut& out, bool true_relres = true, const double2* pre_Mb = nullptr) {
-  cudaStream_t st = g->ctx->stream;
-  const int64_t n = g->n;
+// Restarted (F)GMRES for B right-hand sides of the operator `op` (length op.n).  b, x: device,
+// B x n (ld n).  x holds x0 on entry (zero vector allowed).  op.M empty: no preconditioner.
+void gmres_core(const KrylovOps& op, int B, const double2* b, const double* tol, int m, int maxit, bool flexible,
+                Prec prec, double2* x, GmresOut& out, bool true_relres, const double2* pre_Mb) {
+  cudaStream_t st = op.st;
+  const int64_t n = op.n;
+  const bool has_M = static_cast<bool>(op.M);
   VH_REQUIRE(m >= 1 && maxit >= 1 && B >= 1, ERR_BAD_ARG, "restart and maxit must be positive");
   // ---- workspace
   DevBuf<double2> V, Zs, Xc, Wc, Zc, R, hbuf, coef, partc, d_scale;
@@ -310,30 +302,17 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
   partc.ensure((size_t)B * nch * (m + 1));
   partr.ensure((size_t)B * nch);
   nrm.ensure(B);
-  std::vector<int> pc_dummy;
   auto apply_A = [&](const std::vector<int>& act, const double2* xin, double2* yout, Prec p) {
-    const int na = (int)act.size();
-    std::vector<double2> sc(na);
-    std::vector<int> zs(na);
-    for (int a = 0; a < na; ++a) {
-      sc[a] = scale_h ? scale_h[act[a]] : make_double2(1.0, 0.0);
-      zs[a] = zslot_h ? zslot_h[act[a]] : 0;
-    }
-    VH_CUDA_TRY(cudaMemcpyAsync(d_scale.p, sc.data(), na * sizeof(double2), cudaMemcpyHostToDevice, st));
-    matvec_device(g, na, xin, yout, d_scale.p, zs.data(), p);
-    VH_CUDA_TRY(cudaStreamSynchronize(st));   // host arrays above must outlive the copies
-    out.matvecs += na;
+    op.A(act, xin, yout, p);
+    out.matvecs += (int64_t)act.size();
   };
   auto apply_M = [&](const std::vector<int>& act, const double2* xin, double2* yout) {
-    const int na = (int)act.size();
-    if (!pcs) {
-      VH_CUDA_TRY(cudaMemcpyAsync(yout, xin, (size_t)na * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    if (!has_M) {
+      VH_CUDA_TRY(cudaMemcpyAsync(yout, xin, act.size() * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
       return;
     }
-    std::vector<vh_precon*> ps(na);
-    for (int a = 0; a < na; ++a) ps[a] = pcs[act[a]];
-    precon_apply_device(g, na, ps.data(), xin, yout);
-    out.precons += na;
+    op.M(act, xin, yout);
+    out.precons += (int64_t)act.size();
   };
   auto upload_act = [&](const std::vector<int>& act) {
     VH_CUDA_TRY(cudaMemcpyAsync(d_act.p, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -360,7 +339,7 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
     VH_CUDA_TRY(cudaMemcpyAsync(R.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
   }
   std::vector<double> bnorm(B);
-  if (!flexible && pcs) {
+  if (!flexible && has_M) {
     if (pre_Mb && !any_x0) {   // M^-1 b supplied by the caller (the refinement driver already has it)
       VH_CUDA_TRY(cudaMemcpyAsync(R.p, pre_Mb, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     } else {
@@ -424,12 +403,12 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
         apply_A(run, Zc.p, Wc.p, prec);
       } else {
         apply_A(run, Xc.p, Wc.p, prec);
-        if (pcs) apply_M(run, Wc.p, Zc.p);
+        if (has_M) apply_M(run, Wc.p, Zc.p);
       }
       upload_act(run);
-      double2* w = (flexible || !pcs) ? Wc.p : Zc.p;
+      double2* w = (flexible || !has_M) ? Wc.p : Zc.p;
       // classical Gram-Schmidt: h = V^H w ; w -= V h ; h_{k+1} = |w| (pgmres_iter.m:107-110)
-      ProfScope ps(&g->ctx->prof, SEC_KRYLOV, st, nr);
+      ProfScope ps(op.prof, SEC_KRYLOV, st, nr);
       k_multidot<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, k + 1, n, partc.p);
       count_launch();
       k_reduce_partials<<<nr, 128, 0, st>>>(partc.p, nch, k + 1, hbuf.p, m + 2);
@@ -549,6 +528,119 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
     out.relres[i] = rr[i] / bb[i];
     out.flag[i] = out.relres[i] <= tol[i] ? 0 : 1;
   }
+}
+
+// The VIE system of geometry g: A = the FFT matvec (scale, z slot per RHS), M = the RHS's
+// preconditioners (nullptr: none).
+void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, const double2* scale_h,
+                  const int* zslot_h, const double* tol, int m, int maxit, bool flexible, Prec prec, double2* x,
+                  GmresOut& out, bool true_relres = true, const double2* pre_Mb = nullptr) {
+  cudaStream_t st = g->ctx->stream;
+  DevBuf<double2> d_scale;
+  d_scale.ensure(B);
+  KrylovOps op;
+  op.n = g->n;
+  op.st = st;
+  op.prof = &g->ctx->prof;
+  op.A = [&](const std::vector<int>& act, const double2* xin, double2* yout, Prec p) {
+    const int na = (int)act.size();
+    std::vector<double2> sc(na);
+    std::vector<int> zs(na);
+    for (int a = 0; a < na; ++a) {
+      sc[a] = scale_h ? scale_h[act[a]] : make_double2(1.0, 0.0);
+      zs[a] = zslot_h ? zslot_h[act[a]] : 0;
+    }
+    VH_CUDA_TRY(cudaMemcpyAsync(d_scale.p, sc.data(), na * sizeof(double2), cudaMemcpyHostToDevice, st));
+    matvec_device(g, na, xin, yout, d_scale.p, zs.data(), p);
+    VH_CUDA_TRY(cudaStreamSynchronize(st));   // host arrays above must outlive the copies
+  };
+  if (pcs)
+    op.M = [&](const std::vector<int>& act, const double2* xin, double2* yout) {
+      std::vector<vh_precon*> ps(act.size());
+      for (size_t a = 0; a < act.size(); ++a) ps[a] = pcs[act[a]];
+      precon_apply_device(g, (int)act.size(), ps.data(), xin, yout);
+    };
+  gmres_core(op, B, b, tol, m, maxit, flexible, prec, x, out, true_relres, pre_Mb);
+}
+
+// y[a] = x[a] .* w_a (mode 0) or x[a] ./ w_a (mode 1); w_a = tab[a], a device vector of n reals
+__global__ void k_rows_diag(const double2* x, double2* y, int64_t n, double* const* __restrict__ tab, int mode) {
+  const int a = blockIdx.y;
+  const double* w = tab[a];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = x[(int64_t)a * n + i];
+    const double d = w[i];
+    y[(int64_t)a * n + i] = mode ? make_double2(v.x / d, v.y / d) : make_double2(v.x * d, v.y * d);
+  }
+}
+
+// phi_b = S_b^-1 bb_b approximately, S_b = Ae diag(ainv[b]) Ae^T: restarted GMRES with the Jacobi
+// preconditioner diag(S_b) = sdiag[b], x0 = 0, stopping at |M^-1 r| <= tol[b] |M^-1 bb_b|
+// (lse_sparse_precon_multiply.m:43: gmres(fPSchur, ., min(100, num_curr - 1), prectol, 10, precond)).
+// bb: device B x nphi; phi: device, row b at phi + b * ldphi.  iters[b] = inner iterations taken.
+void schur_gmres_solve(vh_geom* g, int B, double* const* ainv, double* const* sdiag, const double2* bb, double2* phi,
+                       int64_t ldphi, const double* tol, int restart, int maxit, int* iters) {
+  cudaStream_t st = g->ctx->stream;
+  const int64_t nphi = g->nphi, nc = g->nc;
+  for (int b = 0; b < B; ++b) iters[b] = 0;
+  if (nphi == 0) return;
+  VH_CUDA_TRY(cudaMemset2DAsync(phi, ldphi * sizeof(double2), 0, nphi * sizeof(double2), B, st));
+  DevBuf<int> d_rows;
+  DevBuf<double> part, nrm;
+  std::vector<int> all(B);
+  for (int b = 0; b < B; ++b) all[b] = b;
+  const std::vector<double> nb = row_norms(bb, nphi, all, nphi, d_rows, part, nrm, st);
+  std::vector<int> live;   // a zero right-hand side keeps phi = 0
+  for (int b = 0; b < B; ++b)
+    if (nb[b] > 0.0) live.push_back(b);
+  if (live.empty()) return;
+  const int nl = (int)live.size();
+  DevBuf<double2> Bc, Xc, T;
+  DevBuf<double*> tab;
+  DevBuf<int> d_live;
+  Bc.ensure((size_t)nl * nphi);
+  Xc.ensure((size_t)nl * nphi);
+  T.ensure((size_t)nl * std::max<int64_t>(1, nc));
+  tab.ensure(nl);
+  d_live.ensure(nl);
+  VH_CUDA_TRY(cudaMemcpyAsync(d_live.p, live.data(), nl * sizeof(int), cudaMemcpyHostToDevice, st));
+  k_gather<<<dim3(grid1(nphi), nl), 256, 0, st>>>(bb, nphi, Bc.p, nphi, d_live.p, nphi);
+  count_launch();
+  VH_CUDA_TRY(cudaMemsetAsync(Xc.p, 0, (size_t)nl * nphi * sizeof(double2), st));
+  std::vector<double> tl(nl);
+  for (int a = 0; a < nl; ++a) tl[a] = tol[live[a]];
+  auto upload_tab = [&](const std::vector<int>& act, double* const* src) {
+    std::vector<double*> h(act.size());
+    for (size_t a = 0; a < act.size(); ++a) h[a] = src[live[act[a]]];
+    VH_CUDA_TRY(cudaMemcpyAsync(tab.p, h.data(), h.size() * sizeof(double*), cudaMemcpyHostToDevice, st));
+    VH_CUDA_TRY(cudaStreamSynchronize(st));   // h is consumed before it goes out of scope
+  };
+  KrylovOps op;
+  op.n = nphi;
+  op.st = st;
+  op.A = [&](const std::vector<int>& act, const double2* xin, double2* yout, Prec) {   // S v = Ae (A_inv .* Ae^T v)
+    const int na = (int)act.size();
+    upload_tab(act, ainv);
+    spmv_batched(g->AeT, na, xin, nphi, 0, T.p, nc, 0, 0, st);
+    k_rows_diag<<<dim3(grid1(nc), na), 256, 0, st>>>(T.p, T.p, nc, tab.p, 0);
+    count_launch();
+    spmv_batched(g->Ae, na, T.p, nc, 0, yout, nphi, 0, 0, st);
+    VH_CUDA_TRY(cudaGetLastError());
+  };
+  op.M = [&](const std::vector<int>& act, const double2* xin, double2* yout) {   // diag(S) \ v
+    upload_tab(act, sdiag);
+    k_rows_diag<<<dim3(grid1(nphi), (unsigned)act.size()), 256, 0, st>>>(xin, yout, nphi, tab.p, 1);
+    count_launch();
+    VH_CUDA_TRY(cudaGetLastError());
+  };
+  GmresOut o;
+  gmres_core(op, nl, Bc.p, tl.data(), restart, maxit, false, PREC_FP64, Xc.p, o, false, nullptr);
+  for (int a = 0; a < nl; ++a) {
+    VH_CUDA_TRY(cudaMemcpyAsync(phi + (int64_t)live[a] * ldphi, Xc.p + (int64_t)a * nphi, nphi * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, st));
+    iters[live[a]] = (int)o.resvec[a].size() - 1;
+  }
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
 }
 
 // Mixed precision: iterative refinement in FP64 around complex64-matvec GMRES.
@@ -751,6 +843,10 @@ void gmres_dispatch(vh_geom* g, int B, vh_precon* const* pcs, const double2* b_d
                     const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
                     double2* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
   VH_REQUIRE(B >= 1 && b_dev && x_dev && tol, ERR_BAD_ARG, "bad gmres arguments");
+  if (prec == VH_PREC_FP32 && pcs)
+    for (int i = 0; i < B; ++i)
+      VH_REQUIRE(pcs[i] && precon_kind(pcs[i]) != VH_PRECON_SCHUR_GMRES, ERR_UNSUPPORTED,
+                 "'schur_gmres' is not a fixed operator: solve with flexible GMRES in FP64");
   VH_REQUIRE(!(flexible && prec == VH_PREC_FP32), ERR_UNSUPPORTED, "mixed precision uses the left-preconditioned form");
   PoolScope pool_scope(&g->ctx->pool);
   cudaStream_t st = g->ctx->stream;

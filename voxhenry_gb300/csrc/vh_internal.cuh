@@ -1,6 +1,7 @@
 // Internal state behind the C ABI handles.
 #pragma once
 #include <atomic>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -12,6 +13,8 @@
 
 // Handles are reference counted: a geometry holds its context and a preconditioner its geometry,
 // so the owner may destroy them in any order; a parent is released with its last child.
+struct vh_precon;
+
 struct vh_ctx {
   std::atomic<int> refs{1};
   int device = 0;
@@ -92,4 +95,36 @@ namespace vh {
 // Drop one reference; the last one frees the handle (and releases its parent).
 void ctx_release(vh_ctx* c);
 void geom_release(vh_geom* g);
+}  // namespace vh
+
+namespace vh {
+struct GmresOut {
+  std::vector<int> flag, inner, outer;
+  std::vector<double> relres;
+  std::vector<std::vector<double>> resvec;
+  int64_t matvecs = 0;   // RHS-matvecs performed
+  int64_t precons = 0;
+};
+
+// A batch of linear operators for the Krylov solver: A and M act on the rows `act` of the batch
+// (x, y compact: row a of x belongs to RHS act[a]); M empty = no preconditioner.  All work is
+// ordered on `st`.
+struct KrylovOps {
+  int64_t n = 0;
+  cudaStream_t st = nullptr;
+  Profiler* prof = nullptr;   // Krylov vector work is timed here (nullptr: not timed)
+  std::function<void(const std::vector<int>& act, const double2* x, double2* y, Prec p)> A;
+  std::function<void(const std::vector<int>& act, const double2* x, double2* y)> M;
+};
+
+// Restarted left-preconditioned GMRES (pgmres.m semantics) or flexible GMRES (fpgmres.m), batched.
+void gmres_core(const KrylovOps& op, int B, const double2* b, const double* tol, int m, int maxit, bool flexible,
+                Prec prec, double2* x, GmresOut& out, bool true_relres, const double2* pre_Mb);
+
+// Inner GMRES on the Schur complements of the 'schur_gmres' preconditioner (Jacobi-preconditioned).
+void schur_gmres_solve(vh_geom* g, int B, double* const* ainv, double* const* sdiag, const double2* bb, double2* phi,
+                       int64_t ldphi, const double* tol, int restart, int maxit, int* iters);
+
+// The kind (vh_precon_kind) of a preconditioner handle.
+int precon_kind(const vh_precon* p);
 }  // namespace vh

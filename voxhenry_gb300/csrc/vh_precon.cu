@@ -17,7 +17,10 @@ struct vh_precon {
   int kind = 0;
   bool df = false;           // factor and triangular solves in double-float (VH_PRECON_SCHUR_INVERT_DF)
   double* A_inv = nullptr;   // nc reals
-  void* W = nullptr;         // factor storage: w_total doubles, or w_total FP32 pairs when `df`
+  void* W = nullptr;         // factor storage: w_total doubles, or w_total FP32 pairs when `df`;
+                             // 'schur_gmres': diag(S), nphi doubles
+  double prectol = 0.1;      // 'schur_gmres' inner tolerance
+  int64_t inner_iters = 0;   // 'schur_gmres' inner iterations over all applies
 };
 
 namespace vh {
@@ -41,6 +44,17 @@ __global__ void k_a_inv(const double2* __restrict__ z, int64_t nv, double dx, do
     out[3 * nv + v] = a[1];
     out[4 * nv + v] = a[2];
   }
+}
+
+// d[r] = S(r, r) = sum_k Ae(r, k)^2 A_inv[k]  (the Jacobi preconditioner `precond` of
+// lse_sparse_precon_prepare.m:85-86)
+__global__ void k_schur_diag(int64_t nphi, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                             const double* __restrict__ val, const double* __restrict__ ainv, double* __restrict__ d) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nphi) return;
+  double s = 0.0;
+  for (int32_t k = rp[r]; k < rp[r + 1]; ++k) s = fma(val[k] * val[k], ainv[col[k]], s);
+  d[r] = s;
 }
 
 // phi[b] = x_phi[b] - Ar (A_inv_b .* x_J[b]), stored as C: complex128 in place in y, or the
@@ -173,6 +187,41 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
     VH_CUDA_TRY(cudaMalloc(&g->pc_tmp, need * sizeof(double2)));
     g->pc_tmp_cap = need;
   }
+  if (kind == VH_PRECON_SCHUR_GMRES) {   // lse_sparse_precon_multiply.m:26-46
+    const int64_t nc = g->nc, nphi = g->nphi;
+    if (nphi > 0) {
+      auto* bb = static_cast<double2*>(g->ctx->pool.get((size_t)B * nphi * sizeof(double2)));
+      try {
+        k_precon_rhs<double2><<<dim3((unsigned)ceil_div(nphi, 256), B), 256, 0, st>>>(
+            nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val, d_ainv, x, g->n, nc, bb, nphi);   // b - Ae A_inv a
+        count_launch();
+        VH_CUDA_TRY(cudaGetLastError());
+        std::vector<double*> ai(B), sd(B);
+        std::vector<double> tl(B);
+        std::vector<int> it(B);
+        for (int b = 0; b < B; ++b) {
+          ai[b] = pcs[b]->A_inv;
+          sd[b] = static_cast<double*>(pcs[b]->W);
+          tl[b] = pcs[b]->prectol;
+        }
+        const int restart = (int)std::min<int64_t>(100, std::max<int64_t>(1, nc - 1));
+        schur_gmres_solve(g, B, ai.data(), sd.data(), bb, y + nc, g->n, tl.data(), restart, 10, it.data());
+        for (int b = 0; b < B; ++b) pcs[b]->inner_iters += it[b];
+      } catch (...) {
+        g->ctx->pool.put(bb);
+        throw;
+      }
+      g->ctx->pool.put(bb);
+    }
+    if (nc > 0) {   // c = (a + Ae^T d) .* A_inv
+      k_precon_finish<double2><<<dim3((unsigned)ceil_div(nc, 256), B), 256, 0, st>>>(
+          nc, nphi, g->AeT.rowptr, g->AeT.col, g->AeT.val, d_ainv, x, y, g->n, y + nc, g->n, false);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+    }
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    return;
+  }
   if (kind == VH_PRECON_SCHUR_APPROX) {   // lse_sparse_precon_multiply.m:48-58
     const int64_t nc = g->nc, nphi = g->nphi;
     double2* tmp = static_cast<double2*>(g->ctx->pool.get((size_t)B * std::max<int64_t>(1, g->n) * sizeof(double2)));
@@ -250,6 +299,8 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
   VH_CUDA_TRY(cudaStreamSynchronize(st));
 }
 
+int precon_kind(const vh_precon* p) { return p->kind; }
+
 }  // namespace vh
 
 using namespace vh;
@@ -285,17 +336,18 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
   }
   vh_status s = guarded_pc(g->ctx, [&] {
     VH_REQUIRE(kind == VH_PRECON_NONE || kind == VH_PRECON_SCHUR_INVERT || kind == VH_PRECON_SCHUR_INVERT_DF ||
-                   kind == VH_PRECON_SCHUR_APPROX,
-               ERR_UNSUPPORTED, "preconditioner kind not supported (schur_gmres / schur_invert_original)");
+                   kind == VH_PRECON_SCHUR_APPROX || kind == VH_PRECON_SCHUR_GMRES,
+               ERR_UNSUPPORTED, "preconditioner kind not supported (schur_invert_original)");
     const bool df = kind == VH_PRECON_SCHUR_INVERT_DF;
     const bool approx = kind == VH_PRECON_SCHUR_APPROX;
+    const bool inner = kind == VH_PRECON_SCHUR_GMRES;
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     if (kind == VH_PRECON_NONE) return;
     VH_REQUIRE(st_sparse_precon, ERR_BAD_ARG, "st_sparse_precon is required");
     cudaStream_t st = g->ctx->stream;
     if (approx)
       ensure_approx_w(g);
-    else
+    else if (!inner)
       ensure_symbolic(g);
     std::vector<const double*> D(nfreq);
     std::vector<void*> W(nfreq);
@@ -306,18 +358,26 @@ vh_status vh_precon_create_batch(vh_geom* g, vh_precon_kind kind, int nfreq, con
       p->A_inv = static_cast<double*>(g->ctx->pool.get(std::max<int64_t>(1, g->nc) * sizeof(double)));
       p->df = df;
       static_assert(sizeof(dfloat) == sizeof(double), "pair factor entries take a double's storage");
-      if (!approx) p->W = g->ctx->pool.get(std::max<int64_t>(1, g->chol.w_total) * sizeof(double));
+      if (inner)
+        p->W = g->ctx->pool.get(std::max<int64_t>(1, g->nphi) * sizeof(double));
+      else if (!approx)
+        p->W = g->ctx->pool.get(std::max<int64_t>(1, g->chol.w_total) * sizeof(double));
       const double* sp = st_sparse_precon + 6 * i;
       const double2 s1 = make_double2(sp[0], sp[1]), s2 = make_double2(sp[2], sp[3]), s3 = make_double2(sp[4], sp[5]);
       if (g->nv) {
         k_a_inv<<<256, 256, 0, st>>>(g->zslots[zs], g->nv, g->dx, s1, s2, s3, p->A_inv);
         count_launch();
       }
+      if (inner && g->nphi > 0) {
+        k_schur_diag<<<(unsigned)ceil_div(g->nphi, 256), 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val,
+                                                                        p->A_inv, static_cast<double*>(p->W));
+        count_launch();
+      }
       VH_CUDA_TRY(cudaGetLastError());
       D[i] = p->A_inv;
       W[i] = p->W;
     }
-    if (approx) {
+    if (approx || inner) {
       VH_CUDA_TRY(cudaStreamSynchronize(st));
       return;
     }
@@ -351,6 +411,18 @@ void vh_precon_destroy(vh_precon* p) {
   }
   delete p;
   geom_release(g);
+}
+
+vh_status vh_precon_set_prectol(vh_precon* p, double prectol) {
+  if (!p || !(prectol > 0.0) || !std::isfinite(prectol)) return VH_ERR_BAD_ARG;
+  p->prectol = prectol;
+  return VH_OK;
+}
+
+vh_status vh_precon_inner_iterations(const vh_precon* p, int64_t* total) {
+  if (!p || !total) return VH_ERR_BAD_ARG;
+  *total = p->inner_iters;
+  return VH_OK;
 }
 
 vh_status vh_precon_stats(const vh_precon* p, int64_t* nnz_factor, double* flops, int* nfronts, int* max_front) {

@@ -114,6 +114,8 @@ class Sweep:
                 zsl[k] = self.zslot[fi]
                 tolv[k] = executer_tol(f) if tol is None else tol
                 pcs.append(self.pcs[fi])
+        # the 'schur_gmres' apply is an inner iterative solve: flexible GMRES (VoxHenry_executer.m:294-297)
+        flexible = flexible or self.precon_kind == "schur_gmres"
         t0 = time.perf_counter()
         out = self.geom.solve(b, pcs=pcs, scale=scale, zslot=zsl, restart=restart, tol=tolv, maxit=maxit,
                               flexible=flexible, prec=prec)

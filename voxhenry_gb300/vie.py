@@ -201,7 +201,7 @@ class Geometry:
             pass
 
 
-PRECON_KIND = {"no_precond": 0, "schur_invert": 1, "schur_invert_df": 2, "schur_approx": 3}
+PRECON_KIND = {"no_precond": 0, "schur_invert": 1, "schur_invert_df": 2, "schur_approx": 3, "schur_gmres": 4}
 
 
 class Precon:
@@ -231,6 +231,17 @@ class Precon:
         nnz, fl, nf, mf = C.c_int64(), C.c_double(), C.c_int(), C.c_int()
         _lib.check(self.geom.ctx._lib.vh_precon_stats(self.handle, C.byref(nnz), C.byref(fl), C.byref(nf), C.byref(mf)))
         return {"nnz_factor": nnz.value, "flops": fl.value, "fronts": nf.value, "max_front": mf.value}
+
+    def set_prectol(self, prectol):
+        """'schur_gmres': tolerance of the inner GMRES on S (lse_sparse_precon_multiply's prectol)."""
+        _lib.check(self.geom.ctx._lib.vh_precon_set_prectol(self.handle, float(prectol)), self.geom.ctx.handle)
+        return self
+
+    def inner_iterations(self):
+        """'schur_gmres': inner GMRES iterations summed over every apply so far."""
+        t = C.c_int64()
+        _lib.check(self.geom.ctx._lib.vh_precon_inner_iterations(self.handle, C.byref(t)), self.geom.ctx.handle)
+        return t.value
 
     def apply(self, x):
         return apply_precons(self.geom, [self], x)
@@ -370,10 +381,14 @@ def lse_sparse_precon_prepare(dx, z_real, z_imag, idxS, st_sparse_precon, nodeid
 
 
 def lse_sparse_precon_multiply(JOut_full_in, Ae=None, nodeid_4_grnd=None, nodeid_4_injectcurr=None, prectol=None):
-    """lse_sparse_precon_multiply.m:1 -- applies the prepared preconditioner."""
+    """lse_sparse_precon_multiply.m:1 -- applies the prepared preconditioner ('schur_gmres' uses
+    prectol, the inner tolerance; None keeps the handle's, 0.1 by default)."""
     if _PRECON_STATE is None:
         raise RuntimeError("lse_sparse_precon_prepare has not been called")
-    return _PRECON_STATE.own().apply(np.asarray(JOut_full_in).ravel())
+    pc = _PRECON_STATE.own()
+    if prectol is not None and pc.kind == "schur_gmres":
+        pc.set_prectol(prectol)
+    return pc.apply(np.asarray(JOut_full_in).ravel())
 
 
 class MatvecHandle:
