@@ -43,6 +43,9 @@ MAXIT = 10
 # the mixed path's Schur factor and triangular solves run in double-float (FP32 pairs, ~48 bits) on
 # GB300's FP32 pipes; its FP64 refinement residuals set the final accuracy
 MIXED_PRECON = "schur_invert_df"
+# factor sharing between neighbouring frequencies for the separately reported variant: A_inv (hence S)
+# within 1e-4 of the group's factor; on this sweep it halves the factors at unchanged iteration counts
+SHARE_TOL = 1e-4
 
 
 def dist_env():
@@ -184,9 +187,24 @@ def run_ours(args, rank, world):
     def precon_kind(prec):
         return args.mixed_precon if prec == "fp32" else "schur_invert"
 
-    def device_step(prec, tol=None, maxit=MAXIT):
+    # factor sharing between neighbouring frequencies: reported as a separate line of the JSON unless
+    # --share-tol asks for it in the headline mixed path
+    def share_groups(tol):
+        return executer.factor_share_groups([executer.a_inv_classes(prob, f) for f in freqs], tol)
+
+    share_rep = np.arange(F)
+    if args.share_tol is not None:
+        share_rep = share_groups(args.share_tol)
+        cfg["factor_sharing"] = {"share_tol": args.share_tol, "factors_per_step": int(len(np.unique(share_rep)))}
+
+    def device_step(prec, tol=None, maxit=MAXIT, rep=None):
         """One sweep with device-resident inputs: factors + batched solve + R, L."""
-        pcs = g.precons(st_all, sw.zslot, kind=precon_kind(prec))
+        if rep is None:
+            rep = share_rep if prec == "fp32" else np.arange(F)
+        reps = np.unique(rep)
+        made = g.precons(st_all[reps], sw.zslot[reps], kind=precon_kind(prec))
+        by_rep = dict(zip(reps.tolist(), made))
+        pcs = [by_rep[int(r)] for r in rep]
         parr = (C.c_void_p * B)(*[pcs[k // prob.num_ports].handle for k in range(B)])
         tv = tolv if tol is None else np.full(B, tol)
         st = lib.vh_gmres_device(g.handle, B, parr, C.c_void_p(b_dev.data_ptr()), _lib.cview(scale),
@@ -199,13 +217,13 @@ def run_ours(args, rank, world):
             Y = torch.einsum("bn,np->bp", xc, rhs_dev.to(torch.complex128))   # Y(:, p) = sum rhs .* x
             Yh = Y.cpu().numpy().reshape(F, prob.num_ports, prob.num_ports).transpose(0, 2, 1)
         Z = np.linalg.inv(Yh)
-        for p in pcs:
+        for p in made:
             p.close()
         return np.abs(Z.real), np.abs(Z.imag) / (2 * np.pi * freqs)[:, None, None], iters[0::2].copy()
 
-    def timed(prec, steps, warm, profile=False):
+    def timed(prec, steps, warm, profile=False, rep=None):
         for _ in range(warm):
-            device_step(prec)
+            device_step(prec, rep=rep)
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
@@ -219,7 +237,7 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         out = None
         for _ in range(steps):
-            out = device_step(prec)
+            out = device_step(prec, rep=rep)
         e1.record(stream)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
@@ -256,16 +274,22 @@ def run_ours(args, rank, world):
     clk = clocks.stop()
     # plain FP64 GPU path on the same workload
     t_fp64, out_fp64, _, _ = timed("fp64", args.steps, args.warmup)
+    # the mixed path with one factor per group of neighbouring frequencies (A_inv within 1e-4)
+    shared = None
+    if args.share_tol is None:
+        rep_s = share_groups(SHARE_TOL)
+        t_sh, out_sh, _, _ = timed("fp32", args.steps, args.warmup, rep=rep_s)
+        shared = (rep_s, t_sh, out_sh)
     # e2e: the host-buffer C ABI call a user makes (Sweep -> vh_gmres), copies inside the region
     sw.pcs = None
     sw.precon_kind = precon_kind("fp32")
     for _ in range(args.warmup):
-        sw.prepare().solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
+        sw.prepare(share_tol=args.share_tol).solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         sw.pcs = None
-        e2e_out = sw.prepare().solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
+        e2e_out = sw.prepare(share_tol=args.share_tol).solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
     t_e2e = time.perf_counter() - t0
 
     R_m, L_m, it_m = out_mixed
@@ -336,6 +360,14 @@ def run_ours(args, rank, world):
         "sections_ms": sections, "dominant_section": dominant,
         "roofline": roof, "roofline_other_fft": roof_other, "clocks": clk,
     }
+    if shared is not None:
+        rep_s, t_sh, (R_s, L_s, it_s) = shared
+        line["factor_sharing"] = {
+            "share_tol": SHARE_TOL, "factors_per_step": int(len(np.unique(rep_s))),
+            "value": round(pts / t_sh, 4), "ms_per_step": round(1e3 * t_sh / args.steps, 3),
+            "gmres_iterations_total": int(it_s.sum()), "max_rel_err_RL": max(rl_err(R_s, L_s)),
+            "note": "mixed path with one Schur factor per group of neighbouring frequencies whose A_inv differs "
+                    "by at most share_tol (Sweep.prepare(share_tol)); the headline value factors every frequency"}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prob, freqs, sw)
     if rank == 0:
@@ -446,6 +478,9 @@ def main():
                     help="profiling aid: run a few calls of one operator instead of the benchmark")
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: run only the warm-up and timed mixed-precision sweeps, print nothing")
+    ap.add_argument("--share-tol", type=float, default=None,
+                    help="share one Schur factor between neighbouring frequencies whose A_inv differs by at most "
+                         "this (mixed path); off by default")
     ap.add_argument("--probe-rhs", type=int, default=4)
     ap.add_argument("--probe-iters", type=int, default=3)
     ap.add_argument("--probe-kind", default="schur_invert", choices=["schur_invert", "schur_invert_df"])

@@ -395,3 +395,24 @@ def test_mixed_precision_rejects_schur_gmres(lib, blob):
     sw = ex.Sweep(P, np.array([1e9]), precon="schur_gmres").prepare()
     with pytest.raises(Exception, match="schur_gmres"):
         sw.solve(restart=20, tol=1e-8, maxit=2, prec="fp32")
+
+
+def test_factor_sharing_across_frequencies(lib):
+    """Sweep.prepare(share_tol): neighbouring frequencies whose A_inv moves by at most share_tol share
+    one Schur factor; the sweep still converges and R, L equal the one-factor-per-frequency sweep."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+
+    w = geometry.two_bars(L=16, M=10, N=5, xr=(1, 15), zr=(1, 3), y1=(1, 3), y2=(6, 8))
+    S, P = problem_of(w)
+    freqs = np.logspace(3, 10, 12)
+    ref = ex.Sweep(P, freqs).prepare().solve(restart=50, tol=1e-10, maxit=10)
+    sw = ex.Sweep(P, freqs).prepare(share_tol=1e-6)
+    assert 1 < len(np.unique(sw.factor_of)) < len(freqs)
+    out = sw.solve(restart=50, tol=1e-10, maxit=10)
+    assert np.all(out["flag"] == 0)
+    assert_port_matrix_close(out["R"], ref["R"], 1e-8)
+    assert_port_matrix_close(out["L"], ref["L"], 1e-8)
+    it_ref = np.array([len(r) for r in ref["resvec"]])
+    it = np.array([len(r) for r in out["resvec"]])
+    assert np.all(it <= it_ref + 1)

@@ -53,3 +53,32 @@ def test_spiral_and_ring_build(S):
         prob = S.problem_from_workload(w)
         assert prob.rhs.shape[1] == 1 and prob.Ar.shape[1] == 5 * prob.idxS.size
         assert np.count_nonzero(prob.rhs) > 0
+
+
+def test_factor_share_groups_and_a_inv():
+    """Factor sharing across frequencies (executer.factor_share_groups): A_inv per class equals the
+    oracle's a_inv_diag, and groups break where A_inv moves by more than share_tol."""
+    from oracle import circulant, solver
+    from oracle import structure as ostruct
+    from voxhenry_gb300 import executer, geometry
+
+    w = geometry.two_bars(L=16, M=10, N=5, xr=(1, 15), zr=(1, 3), y1=(1, 3), y2=(6, 8))
+    S = ostruct.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    _, st2 = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
+    P = executer.Problem(S.L, S.M, S.N, S.dx, w.sigma_e, None, S.idxS, S.Ar, S.rhs, None, st2)
+    freqs = np.logspace(3, 10, 15)
+    A = [executer.a_inv_classes(P, f) for f in freqs]
+    for f, a in zip(freqs[::7], A[::7]):
+        om = 2 * np.pi * f
+        zr, _ = solver.z_arrays(w.sigma_e, None, om)
+        ref = solver.a_inv_diag(S.dx, zr, None, S.idxS, 1j * om * solver.MU0 * st2)
+        nv = a.shape[0]
+        np.testing.assert_allclose(np.concatenate([a[:, 0], a[:, 0], a[:, 0], a[:, 1], a[:, 2]]), ref, rtol=1e-14)
+    for tol in (0.0, 1e-8, 1e-4, 1e-2, 10.0):
+        rep = executer.factor_share_groups(A, tol)
+        assert rep[0] == 0 and np.all(np.diff(rep) >= 0) and np.all(rep <= np.arange(len(freqs)))
+        for i, r in enumerate(rep):
+            assert np.max(np.abs(A[i] - A[r]) / A[r]) <= tol
+    assert len(np.unique(executer.factor_share_groups(A, 0.0))) == len(freqs)
+    assert len(np.unique(executer.factor_share_groups(A, 10.0))) == 1
+    assert 1 < len(np.unique(executer.factor_share_groups(A, 1e-4))) < len(freqs)

@@ -448,26 +448,27 @@ template <typename T>
 struct SolveSmem {
   using C = cplx<T>;
   static __host__ __device__ size_t vec_bytes(int max_nf) { return ((size_t)max_nf * sizeof(C) + 15) & ~(size_t)15; }
-  static __host__ __device__ size_t per_warp(int max_nf) {
+  static __host__ __device__ size_t per_warp(int max_nf) {   // backward solve: vector, block, y
     return vec_bytes(max_nf) + kBlk * (kBlk + 1) * sizeof(T) + kBlk * sizeof(C);
   }
+  static __host__ __device__ size_t per_warp_fwd(int max_nf) { return vec_bytes(max_nf) + kBlk * sizeof(C); }
 };
 
 template <typename T>
-__global__ void __launch_bounds__(32 * kSolveWarps)
+__global__ void __launch_bounds__(32 * kSolveWarps, 4)
     k_chol_fsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
                   const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, T* const* __restrict__ Wp,
                   cplx<T>* __restrict__ x, int64_t ldx, int64_t xoff, cplx<T>* __restrict__ U, int64_t u_total,
                   int max_nf) {
   using C = cplx<T>;
+  using Dot = typename dot_of<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
   if (item >= (int64_t)nlev * B) return;
-  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp(max_nf);
+  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp_fwd(max_nf);
   C* t = reinterpret_cast<C*>(base);
-  T(*Lb)[kBlk + 1] = reinterpret_cast<T(*)[kBlk + 1]>(base + SolveSmem<T>::vec_bytes(max_nf));
-  C* yb = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(Lb) + kBlk * (kBlk + 1) * sizeof(T));
+  C* yb = reinterpret_cast<C*>(base + SolveSmem<T>::vec_bytes(max_nf));
   const FrontInfo f = fr[lev[item % nlev]];
   const int b = (int)(item / nlev);
   const T* F = Wp[b] + f.w_off;
@@ -509,38 +510,44 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   }
   for (int j0 = 0; j0 < ns; j0 += kBlk) {
     const int w = min(kBlk, ns - j0);
-    // the diagonal block holds L_blk^-1: y_blk = L_blk^-1 t_blk, lane i owns row i
+    // the diagonal block holds L_blk^-1: y_blk = L_blk^-1 t_blk, lane i owns row i (its 32 entries
+    // are loaded straight into registers: coalesced across lanes for each k)
+    {
+      T lv[kBlk];
 #pragma unroll
-    for (int k = 0; k < kBlk; ++k)
-      Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
-    yb[lane] = lane < w ? t[j0 + lane] : czero<C>();   // every lane: yb is read for all 32 k
-    __syncwarp();
-    C tv = czero<C>();
+      for (int k = 0; k < kBlk; ++k)
+        lv[k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
+      yb[lane] = lane < w ? t[j0 + lane] : czero<C>();   // every lane: yb is read for all 32 k
+      __syncwarp();
+      Dot tx(T(0)), ty(T(0));
 #pragma unroll
-    for (int k = 0; k < kBlk; ++k) {
-      if (k < w) {
-        const T l = Lb[lane][k];
-        tv.x = fma(l, yb[k].x, tv.x);
-        tv.y = fma(l, yb[k].y, tv.y);
+      for (int k = 0; k < kBlk; ++k) {
+        if (k < w) {
+          tx.add(lv[k], yb[k].x);
+          ty.add(lv[k], yb[k].y);
+        }
       }
+      C tv;
+      tv.x = tx.value();
+      tv.y = ty.value();
+      __syncwarp();
+      if (lane < w) t[j0 + lane] = tv;
+      yb[lane] = tv;   // zero for lanes >= w (their rows are zero); the GEMV below reads all 32
     }
     __syncwarp();
-    if (lane < w) t[j0 + lane] = tv;
-    yb[lane] = tv;   // zero for lanes >= w (their Lb rows are zero); the GEMV below reads all 32
-    __syncwarp();
     for (int r = j0 + w + lane; r < nf; r += 32) {
-      T ax = T(0), ay = T(0);
       const T* Lr = F + r + (int64_t)j0 * nf;
       T lv[kBlk];
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : T(0);   // independent loads
+      Dot ax(t[r].x), ay(t[r].y);   // t_r - sum_k L(r, k) y_k
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) {
-        ax = fma(lv[k], yb[k].x, ax);
-        ay = fma(lv[k], yb[k].y, ay);
+        ax.add(-lv[k], yb[k].x);
+        ay.add(-lv[k], yb[k].y);
       }
-      t[r].x -= ax;
-      t[r].y -= ay;
+      t[r].x = ax.value();
+      t[r].y = ay.value();
     }
     __syncwarp();
   }
@@ -560,6 +567,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
                   const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x, int64_t ldx,
                   int64_t xoff, int max_nf) {
   using C = cplx<T>;
+  using Dot = typename dot_of<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
@@ -587,7 +595,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   // cross-lane reductions)
   for (int j = lane; j < ns; j += 32) {
     const T* col = F + (int64_t)j * nf;
-    T sx = T(0), sy = T(0);
+    Dot sx(t[j].x), sy(t[j].y);   // z_j - sum_r L(r, j) x_r
     int r = ns;
     for (; r + 4 <= nf; r += 4) {
       T lv[4];
@@ -595,17 +603,17 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
       for (int u = 0; u < 4; ++u) lv[u] = col[r + u];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        sx = fma(lv[u], t[r + u].x, sx);
-        sy = fma(lv[u], t[r + u].y, sy);
+        sx.add(-lv[u], t[r + u].x);
+        sy.add(-lv[u], t[r + u].y);
       }
     }
     for (; r < nf; ++r) {
       const T l = col[r];
-      sx = fma(l, t[r].x, sx);
-      sy = fma(l, t[r].y, sy);
+      sx.add(-l, t[r].x);
+      sy.add(-l, t[r].y);
     }
-    t[j].x -= sx;
-    t[j].y -= sy;
+    t[j].x = sx.value();
+    t[j].y = sy.value();
   }
   __syncwarp();
   const int nblk = (ns + kBlk - 1) / kBlk;
@@ -617,16 +625,19 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     for (int k = 0; k < kBlk; ++k)
       Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
     __syncwarp();
-    C xv = czero<C>();
+    Dot xx(T(0)), xy(T(0));
 #pragma unroll
     for (int k = 0; k < kBlk; ++k) {
       if (k < w) {
         const T l = Lb[k][lane];
         const C zk = t[j0 + k];
-        xv.x = fma(l, zk.x, xv.x);
-        xv.y = fma(l, zk.y, xv.y);
+        xx.add(l, zk.x);
+        xy.add(l, zk.y);
       }
     }
+    C xv;
+    xv.x = xx.value();
+    xv.y = xy.value();
     __syncwarp();
     if (lane < w) t[j0 + lane] = xv;
     __syncwarp();
@@ -636,16 +647,16 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
       T lv[kBlk];
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? col[k] : T(0);
-      T sx = T(0), sy = T(0);
+      Dot sx(t[j].x), sy(t[j].y);
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) {
         if (k < w) {
-          sx = fma(lv[k], t[j0 + k].x, sx);
-          sy = fma(lv[k], t[j0 + k].y, sy);
+          sx.add(-lv[k], t[j0 + k].x);
+          sy.add(-lv[k], t[j0 + k].y);
         }
       }
-      t[j].x -= sx;
-      t[j].y -= sy;
+      t[j].x = sx.value();
+      t[j].y = sy.value();
     }
     __syncwarp();
   }
@@ -663,7 +674,7 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();
     const int mnf = s.level_max_nf[h];
-    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf);
+    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp_fwd(mnf);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
     k_chol_fsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows, s.d_relmap,
                                                            Wp, x, ldx, xoff, U, s.u_total, mnf);

@@ -84,6 +84,43 @@ __device__ __forceinline__ dfloat& operator-=(dfloat& a, dfloat b) { return a = 
 __device__ __forceinline__ dfloat& operator*=(dfloat& a, dfloat b) { return a = a * b; }
 __device__ __forceinline__ bool operator>(dfloat a, dfloat b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
 
+// Running dot product in pair precision with one normalisation at the end: Dot2 of Ogita, Rump
+// and Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005), extended to pair
+// operands by adding the cross terms hi*lo + lo*hi to each product's exact error.  `s` holds the
+// rounded running sum and `c` the sum of every product and addition error, so the loop-carried
+// dependency is a single addition per term (a pair fma carries about nine dependent operations).
+struct df_dot {
+  float s, c;
+  __device__ __forceinline__ explicit df_dot(dfloat init) : s(init.hi), c(init.lo) {}
+  // += a * b
+  __device__ __forceinline__ void add(dfloat a, dfloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    float s2, q;
+    df_two_sum(s, p, s2, q);
+    s = s2;
+    c = __fadd_rn(c, __fadd_rn(q, e));
+  }
+  __device__ __forceinline__ dfloat value() const {
+    dfloat r;
+    df_two_sum(s, c, r.hi, r.lo);   // |c| may exceed |s| after cancellation
+    df_fast_two_sum(r.hi, r.lo, r.hi, r.lo);
+    return r;
+  }
+};
+
+// The same interface over FP64 (plain fused multiply-adds), for templates over the factor type.
+struct d_dot {
+  double s;
+  __device__ __forceinline__ explicit d_dot(double init) : s(init) {}
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <typename T> struct dot_of;
+template <> struct dot_of<double> { using type = d_dot; };
+template <> struct dot_of<dfloat> { using type = df_dot; };
+
 // 1 / b: single-precision seed, then two Newton steps y <- y + y (1 - b y), each in pair arithmetic
 __device__ __forceinline__ dfloat df_recip(dfloat b) {
   dfloat y(__frcp_rn(b.hi));

@@ -59,6 +59,33 @@ def executer_tol(f: float) -> float:
     return 1e-12 if f < 1e6 else 1e-8
 
 
+def a_inv_classes(prob: Problem, f: float) -> np.ndarray:
+    """The diagonal A_inv of lse_sparse_precon_prepare.m:33-64 at frequency f, (nv, 3) for the
+    Jx/Jy/Jz, J2D and J3D classes (host copy, used to decide factor sharing)."""
+    om = 2 * np.pi * f
+    idx = np.asarray(prob.idxS).ravel() - 1
+    sig = np.asarray(prob.sigma_e).ravel(order="F")[idx]
+    lam = None if prob.lambdaL is None else np.asarray(prob.lambdaL).ravel(order="F")[idx]
+    zr, zi = z_arrays(sig, lam, om)            # elementwise: evaluated on the voxels only
+    z = zr + (0 if zi is None else zi)
+    st = 1j * om * MU0 * np.asarray(prob.st2)
+    dx = prob.dx
+    return np.abs(1.0 / np.stack([z / dx + st[0], z / (6 * dx) + st[1], z / (2 * dx) + st[2]], axis=1))
+
+
+def factor_share_groups(a_invs, share_tol: float) -> np.ndarray:
+    """Groups of consecutive frequencies that share one Schur factor: a frequency joins the current
+    group while its A_inv differs from the group's first by at most share_tol (max relative change);
+    returns the representative frequency index of each frequency."""
+    rep = np.zeros(len(a_invs), dtype=np.int64)
+    r = 0
+    for i in range(1, len(a_invs)):
+        if np.max(np.abs(a_invs[i] - a_invs[r]) / a_invs[r]) > share_tol:
+            r = i
+        rep[i] = r
+    return rep
+
+
 class Sweep:
     """Device-resident job: geometry (tensor, Ae, z slots) plus one factor per frequency."""
 
@@ -84,12 +111,28 @@ class Sweep:
         self.pcs = None
         self.t_factor = 0.0
 
-    def prepare(self):
-        """lse_sparse_precon_prepare for every frequency (VoxHenry_executer.m:273)."""
+    def prepare(self, share_tol: float | None = None):
+        """lse_sparse_precon_prepare for every frequency (VoxHenry_executer.m:273).
+
+        share_tol (not in the reference, off by default): neighbouring frequencies whose A_inv differs
+        by at most share_tol use one factor (the preconditioner of the group's first frequency).  The
+        solution still converges to tol; only the iteration count can change, since S is linear in
+        A_inv and the shared factor is S's within share_tol."""
         t0 = time.perf_counter()
         jwmu = 1j * 2 * np.pi * self.freqs * MU0
         st = jwmu[:, None] * np.asarray(self.prob.st2)[None, :]
-        self.pcs = self.geom.precons(st, self.zslot, kind=self.precon_kind)
+        if share_tol is None:
+            self.factor_of = np.arange(len(self.freqs))
+            self.pcs = self.geom.precons(st, self.zslot, kind=self.precon_kind)
+        else:
+            cache = self.__dict__.setdefault("_share_groups", {})
+            if share_tol not in cache:   # the frequencies of a sweep are fixed: group them once
+                cache[share_tol] = factor_share_groups([a_inv_classes(self.prob, f) for f in self.freqs], share_tol)
+            self.factor_of = cache[share_tol]
+            reps = np.unique(self.factor_of)
+            made = self.geom.precons(st[reps], self.zslot[reps], kind=self.precon_kind)
+            by_rep = dict(zip(reps.tolist(), made))
+            self.pcs = [by_rep[int(r)] for r in self.factor_of]
         self.t_factor = time.perf_counter() - t0
         return self
 
