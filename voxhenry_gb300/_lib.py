@@ -110,6 +110,22 @@ def as_c128(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.complex128)
 
 
+def host_empty(shape, dtype=np.complex128) -> np.ndarray:
+    """An uninitialised host array in page-locked memory when a GPU is present, so that the
+    library's host<->device copies of it run as direct DMA; a plain array otherwise.  The memory
+    comes from torch's caching host allocator (the array keeps its tensor alive)."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+            t = torch.empty(max(nbytes, 1), dtype=torch.uint8, pin_memory=True)
+            return t.numpy()[:nbytes].view(dtype).reshape(shape)
+    except ImportError:
+        pass
+    return np.empty(shape, dtype=dtype)
+
+
 def as_f64(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float64)
 

@@ -222,6 +222,8 @@ __global__ void __launch_bounds__(256) k_chol_update(const int32_t* __restrict__
 // offset of column c in the column-major lower triangle of order m (column c holds m - c entries)
 __host__ __device__ __forceinline__ int tri_off(int c, int m) { return c * m - (c * (c - 1)) / 2; }
 
+constexpr int kLoadBatch = 4;   // independent global loads per thread per step of the load phases
+
 template <int NT>
 __device__ __forceinline__ void front_bar() {
   if constexpr (NT == 32)
@@ -241,15 +243,36 @@ __global__ void __launch_bounds__(NT)
   const int nf = f.nf, ns = f.ns;
   T* F = W + f.w_off;
   T* inv_s = S + nf * (nf + 1) / 2;   // 1 / L(j, j)
+  T* coefs = inv_s + ns;                // per pivot j: S(j + 1 + c, j) / S(j, j), c < nf - j - 1
   auto col = [&](int k) { return S + tri_off(k, nf) - k; };   // col(k)[i] = (i, k), i >= k
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int nwarps = NT / 32;
-  for (int k = 0; k < nf; ++k) {
-    T* sk = col(k);
-    const T* fk = F + (int64_t)k * nf;
-    for (int i = k + tid; i < nf; i += NT) sk[i] = fk[i];
+  // Loads walk flat index ranges with kLoadBatch independent global loads per thread before any
+  // shared-memory write (a column-by-column walk leaves one load in flight per thread).
+  {
+    const int nn = nf * nf;   // column-major nf x nf storage; the lower triangle is kept
+    for (int base = tid; base < nn; base += kLoadBatch * NT) {
+      T v[kLoadBatch];
+      int off[kLoadBatch];
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u) {
+        const int idx = base + u * NT;
+        off[u] = -1;
+        if (idx < nn) {
+          const int k = idx / nf, i = idx - k * nf;
+          if (i >= k) {
+            off[u] = tri_off(k, nf) - k + i;
+            v[u] = F[idx];
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u)
+        if (off[u] >= 0) S[off[u]] = v[u];
+    }
   }
   front_bar<NT>();
+  int32_t* rms = reinterpret_cast<int32_t*>(coefs);   // a child's relative map (nb <= nf entries)
   for (int c = 0; c < 2; ++c) {
     const int ci = f.child[c];
     if (ci < 0) continue;
@@ -257,9 +280,28 @@ __global__ void __launch_bounds__(NT)
     const int nb = ch.nb;
     const int32_t* rm = relmap + ch.relmap_off;
     const T* U = W + ch.w_off + ch.ns + (int64_t)ch.ns * ch.nf;   // U(a, b) = U[a + b * ch.nf]
-    for (int t = tid; t < nb * nb; t += NT) {
-      const int a = t % nb, b = t / nb;
-      if (a >= b) col(rm[b])[rm[a]] += U[a + (int64_t)b * ch.nf];
+    for (int a = tid; a < nb; a += NT) rms[a] = rm[a];
+    front_bar<NT>();
+    const int nn = nb * nb;
+    for (int base = tid; base < nn; base += kLoadBatch * NT) {
+      T v[kLoadBatch];
+      int off[kLoadBatch];
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u) {
+        const int idx = base + u * NT;
+        off[u] = -1;
+        if (idx < nn) {
+          const int b = idx / nb, a = idx - b * nb;
+          if (a >= b) {
+            const int rb = rms[b];
+            off[u] = tri_off(rb, nf) - rb + rms[a];
+            v[u] = U[a + (int64_t)b * ch.nf];
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u)
+        if (off[u] >= 0) S[off[u]] += v[u];
     }
     front_bar<NT>();
   }
@@ -280,6 +322,8 @@ __global__ void __launch_bounds__(NT)
     }
     // S(i, k) -= S(i, j) S(k, j) / piv for j < k <= i < nf: trailing column c = k - j - 1 holds m - c entries
     const int m = nf - j - 1;
+    for (int c = tid; c < m; c += NT) coefs[c] = colj[j + 1 + c] * inv2;   // once per column, not per entry
+    front_bar<NT>();
     const int total = (m * (m + 1)) / 2;
     if (tid < total) {
       const float mf = 2.0f * m + 1.0f;
@@ -287,21 +331,22 @@ __global__ void __launch_bounds__(NT)
       c = max(0, min(c, m - 1));
       while (c > 0 && tri_off(c, m) > tid) --c;
       while (c + 1 < m && tri_off(c + 1, m) <= tid) ++c;
-      int p = tid - tri_off(c, m);   // position within column c: row k + p
-      T coef = colj[j + 1 + c] * inv2;
-      T* colk = col(j + 1 + c);
+      int p = tid - tri_off(c, m);           // position within column c: row k + p
+      T coef = coefs[c];
+      T* colk = col(j + 1 + c) + j + 1 + c;  // entry (k, k) of column k = j + 1 + c
+      const T* cj = colj + j + 1 + c;        // S(k, j)
       for (;;) {
-        const int i = j + 1 + c + p;
-        colk[i] = fma(-colj[i], coef, colk[i]);
+        colk[p] = fma(-cj[p], coef, colk[p]);
         p += NT;
         if (p >= m - c) {
-          do {
+          do {                               // next column: col(k + 1) + k + 1 = col(k) + k + (nf - k)
             p -= m - c;
+            colk += m - c;
+            ++cj;
             ++c;
           } while (c < m && p >= m - c);
           if (c >= m) break;
-          coef = colj[j + 1 + c] * inv2;
-          colk = col(j + 1 + c);
+          coef = coefs[c];
         }
       }
     }
@@ -333,19 +378,19 @@ __global__ void __launch_bounds__(NT)
       iv[j] = inv_s[k0 + j];
       F[(k0 + j) + (int64_t)(k0 + j) * nf] = iv[j];
       for (int i = j + 1; i < w; ++i) {
-        T acc = T(0);
-        for (int k = j; k < i; ++k) acc = fma(col(k0 + k)[k0 + i], iv[k], acc);
-        iv[i] = -acc * inv_s[k0 + i];
+        typename dot_of<T>::type acc(T(0));
+        for (int k = j; k < i; ++k) acc.add(col(k0 + k)[k0 + i], iv[k]);
+        iv[i] = -acc.value() * inv_s[k0 + i];
         F[(k0 + i) + (int64_t)(k0 + j) * nf] = iv[i];
       }
     }
   }
 }
 
-// packed lower triangle plus the reciprocal pivots
+// packed lower triangle, the reciprocal pivots and one pivot's column coefficients
 template <typename T>
 static size_t fused_smem_bytes(int max_nf, int max_ns) {
-  return ((size_t)max_nf * (max_nf + 1) / 2 + (size_t)max_ns) * sizeof(T);
+  return ((size_t)max_nf * (max_nf + 1) / 2 + (size_t)max_ns + (size_t)max_nf) * sizeof(T);
 }
 
 // CTA size for fronts up to order max_nf: one warp up to 64, then 2, 4, 8 warps
@@ -663,6 +708,193 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
   for (int j = lane; j < ns; j += 32) xb[rw[j]] = t[j];
 }
 
+// ---- wide triangular solves for the levels near the root, where a few large fronts leave most
+// of the GPU idle and one warp per (front, RHS) walks long serial chains: one CTA of kWideWarps
+// warps per (front, RHS).  Forward: warp 0 applies the diagonal block, all warps share the rows
+// of the block's GEMV.  Backward: the boundary dot products go one warp per column (lanes split
+// the rows: coalesced loads, then a shuffle sum), the diagonal block on warp 0 and the block's
+// column updates one thread per column.
+constexpr int kWideWarps = 8;
+constexpr int kWideMaxFronts = 16;   // levels with at most this many fronts take the wide kernels
+
+template <typename T>
+struct WideSmem {
+  using C = cplx<T>;
+  static __host__ __device__ size_t vec_bytes(int max_nf) { return ((size_t)max_nf * sizeof(C) + 15) & ~(size_t)15; }
+  static __host__ __device__ size_t bytes(int max_nf) {
+    return vec_bytes(max_nf) + kBlk * (kBlk + 1) * sizeof(T) + kBlk * sizeof(C);
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps)
+    k_chol_fsolve_wide(const int32_t* __restrict__ lev, int nlev, const FrontInfo* __restrict__ fr,
+                       const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, T* const* __restrict__ Wp,
+                       cplx<T>* __restrict__ x, int64_t ldx, int64_t xoff, cplx<T>* __restrict__ U, int64_t u_total,
+                       int max_nf) {
+  using C = cplx<T>;
+  using Dot = typename dot_of<T>::type;
+  constexpr int NT = 32 * kWideWarps;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* t = reinterpret_cast<C*>(smem_raw);
+  C* yb = reinterpret_cast<C*>(smem_raw + WideSmem<T>::vec_bytes(max_nf));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const FrontInfo f = fr[lev[blockIdx.x % nlev]];
+  const int b = (int)(blockIdx.x / nlev);
+  const T* F = Wp[b] + f.w_off;
+  C* xb = x + b * ldx + xoff;
+  C* Ub = U + b * u_total;
+  const int32_t* rw = rows + f.rows_off;
+  const int nf = f.nf, ns = f.ns;
+  for (int r = tid; r < nf; r += NT) t[r] = r < ns ? xb[rw[r]] : czero<C>();
+  __syncthreads();
+  for (int c = 0; c < 2; ++c) {
+    if (f.child[c] < 0) continue;
+    const FrontInfo ch = fr[f.child[c]];
+    const int32_t* rm = relmap + ch.relmap_off;
+    for (int a = tid; a < ch.nb; a += NT) {   // distinct targets within one child
+      const C u = Ub[ch.u_off + a];
+      C& tv = t[rm[a]];
+      tv.x -= u.x;
+      tv.y -= u.y;
+    }
+    __syncthreads();
+  }
+  for (int j0 = 0; j0 < ns; j0 += kBlk) {
+    const int w = min(kBlk, ns - j0);
+    if (warp == 0) {   // y_blk = L_blk^-1 t_blk (stored inverse), lane i owns row i
+      T lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        lv[k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
+      yb[lane] = lane < w ? t[j0 + lane] : czero<C>();
+      __syncwarp();
+      Dot tx(T(0)), ty(T(0));
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        if (k < w) {
+          tx.add(lv[k], yb[k].x);
+          ty.add(lv[k], yb[k].y);
+        }
+      C tv;
+      tv.x = tx.value();
+      tv.y = ty.value();
+      __syncwarp();
+      if (lane < w) t[j0 + lane] = tv;
+      yb[lane] = tv;
+    }
+    __syncthreads();
+    for (int r = j0 + w + tid; r < nf; r += NT) {
+      const T* Lr = F + r + (int64_t)j0 * nf;
+      T lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : T(0);
+      Dot ax(t[r].x), ay(t[r].y);
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) {
+        ax.add(-lv[k], yb[k].x);
+        ay.add(-lv[k], yb[k].y);
+      }
+      t[r].x = ax.value();
+      t[r].y = ay.value();
+    }
+    __syncthreads();
+  }
+  for (int j = tid; j < ns; j += NT) xb[rw[j]] = t[j];
+  for (int a = tid; a < f.nb; a += NT) {
+    const C v = t[ns + a];
+    C nv;
+    nv.x = -v.x;
+    nv.y = -v.y;
+    Ub[f.u_off + a] = nv;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps)
+    k_chol_bsolve_wide(const int32_t* __restrict__ lev, int nlev, const FrontInfo* __restrict__ fr,
+                       const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x,
+                       int64_t ldx, int64_t xoff, int max_nf) {
+  using C = cplx<T>;
+  using Dot = typename dot_of<T>::type;
+  constexpr int NT = 32 * kWideWarps;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* t = reinterpret_cast<C*>(smem_raw);
+  T(*Lb)[kBlk + 1] = reinterpret_cast<T(*)[kBlk + 1]>(smem_raw + WideSmem<T>::vec_bytes(max_nf));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const FrontInfo f = fr[lev[blockIdx.x % nlev]];
+  const int b = (int)(blockIdx.x / nlev);
+  const T* F = Wp[b] + f.w_off;
+  C* xb = x + b * ldx + xoff;
+  const int32_t* rw = rows + f.rows_off;
+  const int nf = f.nf, ns = f.ns;
+  for (int r = tid; r < nf; r += NT) t[r] = xb[rw[r]];
+  __syncthreads();
+  // z_j -= sum_{r >= ns} L(r, j) x_r: warp per column, lanes over the rows, then a shuffle sum
+  for (int j = warp; j < ns; j += kWideWarps) {
+    const T* col = F + (int64_t)j * nf;
+    Dot sx(T(0)), sy(T(0));
+    for (int r = ns + lane; r < nf; r += 32) {
+      const T l = col[r];
+      sx.add(l, t[r].x);
+      sy.add(l, t[r].y);
+    }
+    sx.warp_sum();
+    sy.warp_sum();
+    if (lane == 0) {
+      Dot zx(t[j].x), zy(t[j].y);
+      zx.add(T(-1), sx.value());
+      zy.add(T(-1), sy.value());
+      t[j].x = zx.value();
+      t[j].y = zy.value();
+    }
+  }
+  __syncthreads();
+  const int nblk = (ns + kBlk - 1) / kBlk;
+  for (int bi = nblk - 1; bi >= 0; --bi) {
+    const int j0 = bi * kBlk;
+    const int w = min(kBlk, ns - j0);
+    if (warp == 0) {   // x_blk = L_blk^-T z_blk: lane i: x_i = sum_{k >= i} Linv(k, i) z_k
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
+      __syncwarp();
+      Dot xx(T(0)), xy(T(0));
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        if (k < w) {
+          const T l = Lb[k][lane];
+          const C zk = t[j0 + k];
+          xx.add(l, zk.x);
+          xy.add(l, zk.y);
+        }
+      C xv;
+      xv.x = xx.value();
+      xv.y = xy.value();
+      __syncwarp();
+      if (lane < w) t[j0 + lane] = xv;
+    }
+    __syncthreads();
+    for (int j = tid; j < j0; j += NT) {   // z_j -= sum_{k in block} L(j0 + k, j) x_{j0 + k}
+      const T* col = F + (int64_t)j * nf + j0;
+      T lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? col[k] : T(0);
+      Dot sx(t[j].x), sy(t[j].y);
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        if (k < w) {
+          sx.add(-lv[k], t[j0 + k].x);
+          sy.add(-lv[k], t[j0 + k].y);
+        }
+      t[j].x = sx.value();
+      t[j].y = sy.value();
+    }
+    __syncthreads();
+  }
+  for (int j = tid; j < ns; j += NT) xb[rw[j]] = t[j];
+}
+
 template <typename T>
 void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t ldx, int64_t xoff, cplx<T>* U,
                 cudaStream_t st) {
@@ -671,9 +903,21 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
   VH_REQUIRE(sm_max <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
   VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
   VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)WideSmem<T>::bytes(s.max_nf)));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)WideSmem<T>::bytes(s.max_nf)));
+  auto wide = [&](size_t h) { return (int)s.levels[h].size() <= kWideMaxFronts; };
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();
     const int mnf = s.level_max_nf[h];
+    if (wide(h)) {
+      k_chol_fsolve_wide<T><<<(unsigned)(nlev * B), 32 * kWideWarps, WideSmem<T>::bytes(mnf), st>>>(
+          s.d_levels[h], nlev, s.d_fronts, s.d_rows, s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+      continue;
+    }
     const size_t smh = kSolveWarps * SolveSmem<T>::per_warp_fwd(mnf);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
     k_chol_fsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows, s.d_relmap,
@@ -684,6 +928,13 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
   for (size_t hh = s.levels.size(); hh-- > 0;) {
     const int nlev = (int)s.levels[hh].size();
     const int mnf = s.level_max_nf[hh];
+    if (wide(hh)) {
+      k_chol_bsolve_wide<T><<<(unsigned)(nlev * B), 32 * kWideWarps, WideSmem<T>::bytes(mnf), st>>>(
+          s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+      continue;
+    }
     const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
     k_chol_bsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp, x, ldx,

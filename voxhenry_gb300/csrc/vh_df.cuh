@@ -108,6 +108,18 @@ struct df_dot {
     df_fast_two_sum(r.hi, r.lo, r.hi, r.lo);
     return r;
   }
+  // adds another partial dot product (the same accumulation rule: exact sum of the rounded parts)
+  __device__ __forceinline__ void merge(float os, float oc) {
+    float s2, q;
+    df_two_sum(s, os, s2, q);
+    s = s2;
+    c = __fadd_rn(c, __fadd_rn(q, oc));
+  }
+  // sum over the 32 lanes of a warp (butterfly: every lane ends with the total)
+  __device__ __forceinline__ void warp_sum() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) merge(__shfl_xor_sync(0xffffffffu, s, o), __shfl_xor_sync(0xffffffffu, c, o));
+  }
 };
 
 // The same interface over FP64 (plain fused multiply-adds), for templates over the factor type.
@@ -116,6 +128,10 @@ struct d_dot {
   __device__ __forceinline__ explicit d_dot(double init) : s(init) {}
   __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
   __device__ __forceinline__ double value() const { return s; }
+  __device__ __forceinline__ void warp_sum() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  }
 };
 template <typename T> struct dot_of;
 template <> struct dot_of<double> { using type = d_dot; };

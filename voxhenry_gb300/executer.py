@@ -14,7 +14,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import scipy.sparse as sp
 
-from . import vie
+from . import _lib, vie
 
 MU0 = 4 * np.pi * 1e-7     # EMconstants.m:13
 
@@ -136,6 +136,19 @@ class Sweep:
         self.t_factor = time.perf_counter() - t0
         return self
 
+    def _rhs_batch(self) -> np.ndarray:
+        """The (F * P, n) right-hand sides, frequency-major (rhs(:, p) for every frequency), built once
+        per sweep in page-locked host memory; the solve copies it to the device on every call."""
+        b = self.__dict__.get("_b_host")
+        if b is None:
+            P, F = self.prob.num_ports, len(self.freqs)
+            b = _lib.host_empty((F * P, self.geom.n), np.complex128)
+            rhs = self.prob.rhs.astype(np.complex128)
+            for fi in range(F):
+                b[fi * P:(fi + 1) * P] = rhs.T
+            self._b_host = b
+        return b
+
     def solve(self, restart=50, tol=None, maxit=10, prec="fp64", flexible=False):
         """Solves every (frequency, port) RHS in one batch; returns R, L, Y, Z and solver stats."""
         if self.pcs is None:
@@ -143,8 +156,7 @@ class Sweep:
         P = self.prob.num_ports
         F = len(self.freqs)
         B = F * P
-        rhs = self.prob.rhs.astype(np.complex128)
-        b = np.empty((B, self.geom.n), dtype=np.complex128)
+        b = self._rhs_batch()
         scale = np.empty(B, dtype=np.complex128)
         zsl = np.empty(B, dtype=np.int32)
         tolv = np.empty(B)
@@ -152,7 +164,6 @@ class Sweep:
         for fi, f in enumerate(self.freqs):
             for p in range(P):
                 k = fi * P + p
-                b[k] = rhs[:, p]
                 scale[k] = 1j * 2 * np.pi * f * MU0
                 zsl[k] = self.zslot[fi]
                 tolv[k] = executer_tol(f) if tol is None else tol
@@ -164,10 +175,10 @@ class Sweep:
                               flexible=flexible, prec=prec)
         t_solve = time.perf_counter() - t0
         x = out["x"]
-        Y = np.zeros((F, P, P), dtype=np.complex128)
-        for fi in range(F):
-            for p in range(P):
-                Y[fi, :, p] = self.prob.rhs.T @ x[fi * P + p]
+        # Y(:, p) = sum(rhs .* x) (VoxHenry_executer.m:311-316); rhs is nonzero only on the port rows
+        rows = np.flatnonzero(np.any(self.prob.rhs != 0, axis=1))
+        Yall = x[:, rows] @ self.prob.rhs[rows]   # (B, P): Yall[k, q] = sum_n rhs[n, q] x_k[n]
+        Y = Yall.reshape(F, P, P).transpose(0, 2, 1).copy()
         Z = np.linalg.inv(Y)
         R = np.abs(Z.real)
         Lh = np.abs(Z.imag) / (2 * np.pi * self.freqs)[:, None, None]

@@ -169,7 +169,7 @@ class Geometry:
         s = None if scale is None else _lib.as_c128(np.broadcast_to(np.asarray(scale, dtype=np.complex128), (B,)))
         zs = None if zslot is None else np.ascontiguousarray(np.broadcast_to(zslot, (B,)), dtype=np.int32)
         rl = resvec_len or (restart * maxit + 1)
-        x = np.empty_like(bb)
+        x = _lib.host_empty(bb.shape, np.complex128)
         flag = np.zeros(B, dtype=np.int32)
         relres = np.zeros(B)
         it = np.zeros(2 * B, dtype=np.int32)
