@@ -38,7 +38,11 @@ typedef enum vh_status {
 } vh_status;
 
 /* arithmetic of the FFT convolution: complex128, or complex64 with fp32 accumulation */
-typedef enum vh_prec { VH_PREC_FP64 = 0, VH_PREC_FP32 = 1 } vh_prec;
+/* VH_PREC_DF (vh_matvec / vh_matvec_device only): complex128 storage and FP64 x/y transforms with
+ * the z-transform and tensor products in double-float (FP32 pairs, ~48 significant bits, relative
+ * error ~1e-13) on GB300's FP32 pipes; no counterpart in the reference.  The mixed-precision
+ * solver forms its refinement residual with it.                                                   */
+typedef enum vh_prec { VH_PREC_FP64 = 0, VH_PREC_FP32 = 1, VH_PREC_DF = 2 } vh_prec;
 
 /* preconditioner kinds of lse_sparse_precon_prepare.m:5,71,83,90 ('schur_invert_original' is not provided) */
 typedef enum vh_precon_kind {

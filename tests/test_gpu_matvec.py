@@ -9,6 +9,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12     # single FP64 matvec, relative 2-norm
 FP32_TOL = 2e-6      # complex64 FFT convolution, relative 2-norm
+DF_TOL = 1e-12       # complex128 storage, double-float z-pass (~48 significant bits), relative 2-norm
 
 
 @pytest.fixture(scope="module")
@@ -145,7 +146,7 @@ BOXES = [  # (grid, z range): padded z lengths 18 (shared-memory z-pass) and 8, 
 ]
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL)])
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL), ("df", DF_TOL)])
 @pytest.mark.parametrize("shape,zr", BOXES)
 def test_matvec_voxel_box_inside_grid(vie, prec, tol, shape, zr):
     """Voxels in a y and z sub-range of the grid: the transform visits only that box."""
@@ -163,3 +164,26 @@ def test_matvec_voxel_box_inside_grid(vie, prec, tol, shape, zr):
     for b in range(3):
         ref = solver.lse_matvect_mult(X[b], s * fN, S.Ar, z_real, None, S.dx, S.idxS5)
         assert rel(Y[b], ref) < tol
+
+
+@pytest.mark.parametrize("shape,zr", BOXES)
+def test_matvec_df_takes_the_double_float_z_pass(vie, shape, zr):
+    """VH_PREC_DF differs from FP64 only by double-float rounding where the register z-pass runs
+    (padded z length 8, 16, 32), and equals FP64 bit for bit where it falls back (length 18)."""
+    from voxhenry_gb300 import geometry
+
+    L, M, N = shape
+    w = geometry.two_bars(L=L, M=M, N=N, xr=(1, L - 1), zr=zr, y1=(1, 3), y2=(M - 4, M - 1))
+    S, fN, st = system_of(w)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS)
+    rng = np.random.default_rng(5)
+    X = np.stack([rand_c(rng, S.n) for _ in range(2)])
+    s = np.full(2, 1j * 2 * np.pi * 3e9 * solver.MU0)   # j omega mu: the convolution carries the product
+    Y64 = g.matvec(X, scale=s, prec="fp64")
+    Ydf = g.matvec(X, scale=s, prec="df")
+    d = max(rel(Ydf[b], Y64[b]) for b in range(2))
+    if 2 * N in (8, 16, 32):
+        assert 0 < d < DF_TOL
+    else:
+        assert d == 0

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(PKG, "libvhgpu.so")
 VH_OK = 0
 STATUS = {0: "VH_OK", 1: "VH_ERR_BAD_ARG", 2: "VH_ERR_OOM", 3: "VH_ERR_UNSUPPORTED", 4: "VH_ERR_TIMEOUT",
           5: "VH_ERR_NOT_CONVERGED", 6: "VH_ERR_CUDA", 7: "VH_ERR_NO_DEVICE"}
-PREC = {"fp64": 0, "fp32": 1}
+PREC = {"fp64": 0, "fp32": 1, "df": 2}
 
 _p = C.c_void_p
 _i64p = C.POINTER(C.c_int64)

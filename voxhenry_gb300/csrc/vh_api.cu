@@ -129,7 +129,7 @@ void matvec_device(vh_geom* g, int B, const double2* x, double2* y, const double
   int64_t zstride = 0;
   const double2* z = resolve_z(g, B, zslot, zstride);
   if (g->nv > 0) {
-    ProfScope ps(&g->ctx->prof, prec == PREC_FP64 ? SEC_CONV64 : SEC_CONV32, st, B);
+    ProfScope ps(&g->ctx->prof, prec == PREC_FP32 ? SEC_CONV32 : SEC_CONV64, st, B);
     conv_apply(g->conv, prec, B, x, g->n, y, g->n, scale, z, zstride, st);
   }
   // y_J -= Ae^T phi ; y_phi = Ae J   (lse_matvect_mult.m:138-140)
@@ -366,7 +366,7 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
     VH_REQUIRE(B >= 1 && x_dev && y_dev && x_dev != y_dev, ERR_BAD_ARG, "bad matvec arguments");
-    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32, ERR_BAD_ARG, "bad precision");
+    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32 || prec == VH_PREC_DF, ERR_BAD_ARG, "bad precision");
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     matvec_device(g, B, (const double2*)x_dev, (double2*)y_dev, (const double2*)scale_dev, zslot, (Prec)prec);
   });
@@ -377,7 +377,7 @@ vh_status vh_matvec(vh_geom* g, int B, const double* x, double* y, const double*
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
     VH_REQUIRE(B >= 1 && x && y, ERR_BAD_ARG, "bad matvec arguments");
-    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32, ERR_BAD_ARG, "bad precision");
+    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32 || prec == VH_PREC_DF, ERR_BAD_ARG, "bad precision");
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     cudaStream_t st = g->ctx->stream;
     if ((size_t)B > g->io_cap) {

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "vh_conv.cuh"
+#include "vh_df.cuh"
 
 namespace vh {
 
@@ -266,9 +267,18 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
 // one ky row; the five spectra of a point meet in shared memory for the tensor product.
 constexpr int kZregCols = 32;
 
-template <typename T, int Z, int NZ>
+// storage <-> arithmetic type of the z-pass (identity, or complex128 storage with double-float
+// arithmetic)
+__device__ __forceinline__ float2 zload(float2 v, float2) { return v; }
+__device__ __forceinline__ double2 zload(double2 v, double2) { return v; }
+__device__ __forceinline__ dcomplex zload(double2 v, dcomplex) { return to_c(v, dcomplex()); }
+__device__ __forceinline__ float2 zstore(float2 v, float2) { return v; }
+__device__ __forceinline__ double2 zstore(double2 v, double2) { return v; }
+__device__ __forceinline__ double2 zstore(dcomplex v, double2) { return to_d(v); }
+
+template <typename T, int Z, int NZ, typename ST = cplx<T>>
 __global__ void __launch_bounds__(5 * kZregCols)
-    k_zpass_reg(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ tens, int nz, int Y, int X, int nrhs,
+    k_zpass_reg(ST* __restrict__ Bf, const cplx<T>* __restrict__ tens, int nz, int Y, int X, int nrhs,
                 const cplx<T>* __restrict__ twg) {
   using C = cplx<T>;
   constexpr int BITS = Z == 8 ? 3 : (Z == 16 ? 4 : 5);
@@ -285,14 +295,14 @@ __global__ void __launch_bounds__(5 * kZregCols)
   const int64_t comp = (int64_t)nz * plane;   // one component of one RHS
   __syncthreads();
   for (int b = 0; b < nrhs; ++b) {
-    C* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X + kx;
+    ST* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X + kx;
     {
       C v[Z];
 #pragma unroll
       for (int i = 0; i < Z; ++i) v[i] = czero<C>();
 #pragma unroll
       for (int i = 0; i < NZ; ++i)
-        if (i < nz && col_ok) v[i] = base[warp * comp + i * plane];
+        if (i < nz && col_ok) v[i] = zload(base[warp * comp + i * plane], C());
       dif_pruned<Z, Z, NZ, -1>(v, tw);
 #pragma unroll
       for (int p = 0; p < Z; ++p) S[(warp * Z + p) * kZregCols + lane] = v[p];
@@ -315,26 +325,27 @@ __global__ void __launch_bounds__(5 * kZregCols)
       dit_pruned<Z, Z, NZ, +1>(v, tw);
 #pragma unroll
       for (int i = 0; i < NZ; ++i)
-        if (i < nz && col_ok) base[warp * comp + i * plane] = v[i];
+        if (i < nz && col_ok) base[warp * comp + i * plane] = zstore(v[i], ST());
     }
     __syncthreads();   // S is rewritten by the next RHS
   }
 }
 
-template <typename T, int Z, int NZ>
-static void launch_zpass_reg(cplx<T>* Bf, const cplx<T>* tens, int nz, int Y, int X, int B, const cplx<T>* tw,
+template <typename T, int Z, int NZ, typename ST>
+static void launch_zpass_reg(ST* Bf, const cplx<T>* tens, int nz, int Y, int X, int B, const cplx<T>* tw,
                              cudaStream_t st) {
   const size_t sm = (size_t)(Z + 5 * Z * kZregCols) * sizeof(cplx<T>);
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass_reg<T, Z, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass_reg<T, Z, NZ, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   dim3 grid((unsigned)ceil_div(X, kZregCols), (unsigned)Y);
-  k_zpass_reg<T, Z, NZ><<<grid, 5 * kZregCols, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
+  k_zpass_reg<T, Z, NZ, ST><<<grid, 5 * kZregCols, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
   count_launch();
   VH_CUDA_TRY(cudaGetLastError());
 }
 
-// true when the register z-pass handles this length (Z = 8, 16, 32; nz <= Z / 2 always holds)
-template <typename T>
-static bool zpass_reg(int Z, int nz, cplx<T>* Bf, const cplx<T>* tens, int Y, int X, int B, const cplx<T>* tw,
+// true when the register z-pass handles this length (Z = 8, 16, 32; nz <= Z / 2 always holds);
+// T is the arithmetic type, ST the storage type of the spectra
+template <typename T, typename ST = cplx<T>>
+static bool zpass_reg(int Z, int nz, ST* Bf, const cplx<T>* tens, int Y, int X, int B, const cplx<T>* tw,
                       cudaStream_t st) {
   int nzb = 2;
   while (nzb < nz) nzb *= 2;
@@ -463,10 +474,33 @@ void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2
   VH_CUDA_TRY(cudaStreamSynchronize(st));
 }
 
+// the double-float tensor spectrum and z twiddles for PREC_DF, from tens64 (once per plan)
+__global__ void k_tensor_to_df(const double2* __restrict__ in, dcomplex* __restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = to_c(in[i], dcomplex());
+}
+
+static void ensure_df_tensor(ConvPlan& p, cudaStream_t st) {
+  if (p.tensdf) return;
+  const int64_t n = 7 * p.points();
+  VH_CUDA_TRY(cudaMalloc(&p.tensdf, n * sizeof(dcomplex)));
+  k_tensor_to_df<<<1024, 256, 0, st>>>(p.tens64, static_cast<dcomplex*>(p.tensdf), n);
+  count_launch();
+  VH_CUDA_TRY(cudaGetLastError());
+  const auto t = twiddles(p.Z);
+  std::vector<dcomplex> td(p.Z);
+  for (int i = 0; i < p.Z; ++i) td[i] = dcomplex{dfloat(t[i].x), dfloat(t[i].y)};
+  VH_CUDA_TRY(cudaMalloc(&p.twdf, p.Z * sizeof(dcomplex)));
+  VH_CUDA_TRY(cudaMemcpyAsync(p.twdf, td.data(), p.Z * sizeof(dcomplex), cudaMemcpyHostToDevice, st));
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
 void conv_plan_destroy(ConvPlan& p) {
   cudaFree(p.vmap);
   cudaFree(p.tens64);
   cudaFree(p.tens32);
+  cudaFree(p.tensdf);
+  cudaFree(p.twdf);
   for (int a = 0; a < 3; ++a) { cudaFree(p.tw64[a]); cudaFree(p.tw32[a]); }
   cudaFree(p.scratchA);
   cudaFree(p.scratchB);
@@ -474,7 +508,7 @@ void conv_plan_destroy(ConvPlan& p) {
 }
 
 void conv_plan_reserve(ConvPlan& p, int B, Prec prec) {
-  const size_t cs = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
+  const size_t cs = prec == PREC_FP32 ? sizeof(float2) : sizeof(double2);
   const size_t needA = (size_t)B * 5 * p.nz * p.ny * p.X * cs;
   const size_t needB = (size_t)B * 5 * p.nz * p.Y * p.X * cs;
   if (needA > p.scratch_bytes_A) {
@@ -495,7 +529,8 @@ void conv_plan_reserve(ConvPlan& p, int B, Prec prec) {
 
 template <typename T>
 static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
-                         const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st) {
+                         const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st,
+                         bool df_z = false) {
   using C = cplx<T>;
   const bool dbl = sizeof(T) == 8;
   C* A = reinterpret_cast<C*>(p.scratchA);
@@ -527,8 +562,14 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
-  // pass 3
-  if (!zpass_reg<T>(Z, nz, Bf, tens, Y, X, B, twp[2], st)) {
+  // pass 3 (double-float arithmetic on the complex128 spectra when asked and the length allows)
+  bool z_done = false;
+  if constexpr (sizeof(T) == 8) {
+    if (df_z && p.tensdf)
+      z_done = zpass_reg<dfloat>(Z, nz, Bf, static_cast<const dcomplex*>(p.tensdf), Y, X, B,
+                                 static_cast<const dcomplex*>(p.twdf), st);
+  }
+  if (!z_done && !zpass_reg<T>(Z, nz, Bf, tens, Y, X, B, twp[2], st)) {
     const int tx = z_lines_per_cta(Z, X);
     const size_t sm = (size_t)(Z + 2 * Z * 5 * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)Y);
@@ -650,14 +691,15 @@ void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaSt
 void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
                 const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st) {
   conv_plan_reserve(p, B, prec);
-  if (prec == PREC_FP64)
-    conv_apply_t<double>(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
-  else
+  if (prec == PREC_DF) ensure_df_tensor(p, st);
+  if (prec == PREC_FP32)
     conv_apply_t<float>(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
+  else
+    conv_apply_t<double>(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st, prec == PREC_DF);
 }
 
 void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t& b_per_rhs) {
-  const size_t cs = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
+  const size_t cs = prec == PREC_FP32 ? sizeof(float2) : sizeof(double2);
   a_per_rhs = (size_t)5 * p.nz * p.ny * p.X * cs;
   b_per_rhs = (size_t)5 * p.nz * p.Y * p.X * cs;
 }
@@ -673,10 +715,10 @@ void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, i
   q.scratchB = scratchB;
   q.scratch_bytes_A = a1 * B;
   q.scratch_bytes_B = b1 * B;
-  if (prec == PREC_FP64)
-    conv_apply_t<double>(q, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
-  else
+  if (prec == PREC_FP32)
     conv_apply_t<float>(q, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
+  else   // PREC_DF uses the double-float z-pass only if the plan already holds its tensor
+    conv_apply_t<double>(q, B, x, ldx, y, ldy, scale, zdiag, zstride, st, prec == PREC_DF);
 }
 
 }  // namespace vh

@@ -8,7 +8,9 @@
 
 namespace vh {
 
-enum Prec { PREC_FP64 = 0, PREC_FP32 = 1 };
+// PREC_DF: complex128 storage and FP64 x/y transforms, the z-pass (transform, tensor products,
+// inverse) in double-float arithmetic on the FP32 pipes (~48 significant bits)
+enum Prec { PREC_FP64 = 0, PREC_FP32 = 1, PREC_DF = 2 };
 
 // Factor n into the radices the FFT supports; false if n has another prime factor.
 bool fft_factor(int n, FftDesc& d);
@@ -27,6 +29,8 @@ struct ConvPlan {
   // internal tensor spectrum, layout [ky][kz][k][kx], already divided by X*Y*Z
   double2* tens64 = nullptr;
   float2* tens32 = nullptr;
+  void* tensdf = nullptr;     // double-float copy of tens64 (pairs of floats), built on first PREC_DF use
+  void* twdf = nullptr;       // double-float z twiddles
   double2* tw64[3] = {nullptr, nullptr, nullptr};
   float2* tw32[3] = {nullptr, nullptr, nullptr};
   // scratch: A (5 * nz * ny * X per RHS) and Bf (5 * nz * Y * X per RHS), in bytes

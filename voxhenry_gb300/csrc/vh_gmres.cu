@@ -761,7 +761,7 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
         count_launch();
         k_gather<<<dim3(grid1(n), na), 256, 0, st>>>(b, n, Ba.p, n, d_act.p, n);
         count_launch();
-        Aprec(active, Xa.p, Ya.p, PREC_FP64);
+        Aprec(active, Xa.p, Ya.p, PREC_DF);   // ~48-bit product: far below the 1e-9.. tolerances
         k_sub<<<grid1((int64_t)na * n), 256, 0, st>>>(Ba.p, Ya.p, Ya.p, (int64_t)na * n);
         count_launch();
       } else {
