@@ -610,7 +610,7 @@ template <typename T>
 __global__ void __launch_bounds__(32 * kSolveWarps)
     k_chol_bsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
                   const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x, int64_t ldx,
-                  int64_t xoff, int max_nf) {
+                  int64_t xoff, int max_nf, double2* __restrict__ xd, int64_t ldxd) {
   using C = cplx<T>;
   using Dot = typename dot_of<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -705,7 +705,10 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     }
     __syncwarp();
   }
-  for (int j = lane; j < ns; j += 32) xb[rw[j]] = t[j];
+  for (int j = lane; j < ns; j += 32) {
+    xb[rw[j]] = t[j];
+    if (xd) xd[b * ldxd + rw[j]] = to_d(t[j]);   // final value, also in FP64 for the caller
+  }
 }
 
 // ---- wide triangular solves for the levels near the root, where a few large fronts leave most
@@ -814,7 +817,7 @@ template <typename T>
 __global__ void __launch_bounds__(32 * kWideWarps)
     k_chol_bsolve_wide(const int32_t* __restrict__ lev, int nlev, const FrontInfo* __restrict__ fr,
                        const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x,
-                       int64_t ldx, int64_t xoff, int max_nf) {
+                       int64_t ldx, int64_t xoff, int max_nf, double2* __restrict__ xd, int64_t ldxd) {
   using C = cplx<T>;
   using Dot = typename dot_of<T>::type;
   constexpr int NT = 32 * kWideWarps;
@@ -892,12 +895,15 @@ __global__ void __launch_bounds__(32 * kWideWarps)
     }
     __syncthreads();
   }
-  for (int j = tid; j < ns; j += NT) xb[rw[j]] = t[j];
+  for (int j = tid; j < ns; j += NT) {
+    xb[rw[j]] = t[j];
+    if (xd) xd[b * ldxd + rw[j]] = to_d(t[j]);
+  }
 }
 
 template <typename T>
 void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t ldx, int64_t xoff, cplx<T>* U,
-                cudaStream_t st) {
+                cudaStream_t st, double2* xd, int64_t ldxd) {
   if (s.nfronts == 0 || B == 0) return;
   const size_t sm_max = kSolveWarps * SolveSmem<T>::per_warp(s.max_nf);
   VH_REQUIRE(sm_max <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
@@ -930,7 +936,7 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
     const int mnf = s.level_max_nf[hh];
     if (wide(hh)) {
       k_chol_bsolve_wide<T><<<(unsigned)(nlev * B), 32 * kWideWarps, WideSmem<T>::bytes(mnf), st>>>(
-          s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf);
+          s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf, xd, ldxd);
       count_launch();
       VH_CUDA_TRY(cudaGetLastError());
       continue;
@@ -938,7 +944,7 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
     const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
     k_chol_bsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp, x, ldx,
-                                                           xoff, mnf);
+                                                           xoff, mnf, xd, ldxd);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -946,9 +952,9 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
 
 template void chol_factor<double>(const CholSymbolic&, int, const double* const*, double* const*, cudaStream_t);
 template void chol_solve<double>(const CholSymbolic&, int, double* const*, double2*, int64_t, int64_t, double2*,
-                                 cudaStream_t);
+                                 cudaStream_t, double2*, int64_t);
 template void chol_factor<dfloat>(const CholSymbolic&, int, const double* const*, dfloat* const*, cudaStream_t);
 template void chol_solve<dfloat>(const CholSymbolic&, int, dfloat* const*, dcomplex*, int64_t, int64_t, dcomplex*,
-                                 cudaStream_t);
+                                 cudaStream_t, double2*, int64_t);
 
 }  // namespace vh

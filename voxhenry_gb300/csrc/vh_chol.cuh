@@ -88,9 +88,10 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* con
 
 // Solves S x = b in place for B right-hand sides in the factor's precision.  x: device, complex of
 // T, RHS b at x + b*ldx + xoff (panel indexing); Wp: device array of B factor pointers; U: device
-// scratch of B * u_total complex values of T.
+// scratch of B * u_total complex values of T.  xd (optional): the solution is also written there
+// in complex128, RHS b at xd + b*ldxd (panel indexing).
 template <typename T>
 void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t ldx, int64_t xoff, cplx<T>* U,
-                cudaStream_t st);
+                cudaStream_t st, double2* xd = nullptr, int64_t ldxd = 0);
 
 }  // namespace vh

@@ -274,7 +274,7 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
       count_launch();
       VH_CUDA_TRY(cudaGetLastError());
       chol_solve<dfloat>(g->chol, B, reinterpret_cast<dfloat* const*>(g->pc_ptrs + B), phi_df, g->nphi, 0,
-                         reinterpret_cast<dcomplex*>(g->pc_tmp), st);
+                         reinterpret_cast<dcomplex*>(g->pc_tmp), st, y + g->nc, g->n);   // phi also into y
     } else {
       k_precon_rhs<double2><<<grid, 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val, d_ainv, x, g->n,
                                                   g->nc, y + g->nc, g->n);
@@ -283,15 +283,10 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
       chol_solve<double>(g->chol, B, g->pc_ptrs + B, y, g->n, g->nc, g->pc_tmp, st);
     }
   }
-  if (g->nc > 0 || (df && g->nphi > 0)) {
-    const int64_t rows = df ? g->nc + g->nphi : g->nc;
-    const dim3 grid((unsigned)ceil_div(rows, 256), B);
-    if (df)
-      k_precon_finish<dcomplex><<<grid, 256, 0, st>>>(g->nc, g->nphi, g->AeT.rowptr, g->AeT.col, g->AeT.val, d_ainv,
-                                                      x, y, g->n, phi_df, g->nphi, true);
-    else
-      k_precon_finish<double2><<<grid, 256, 0, st>>>(g->nc, g->nphi, g->AeT.rowptr, g->AeT.col, g->AeT.val, d_ainv,
-                                                     x, y, g->n, y + g->nc, g->n, false);
+  if (g->nc > 0) {   // phi is in y (complex128) for both factor types
+    const dim3 grid((unsigned)ceil_div(g->nc, 256), B);
+    k_precon_finish<double2><<<grid, 256, 0, st>>>(g->nc, g->nphi, g->AeT.rowptr, g->AeT.col, g->AeT.val, d_ainv,
+                                                   x, y, g->n, y + g->nc, g->n, false);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
