@@ -293,6 +293,21 @@ __global__ void __launch_bounds__(5 * kZregCols)
   const bool col_ok = kx < X;
   const int64_t plane = (int64_t)Y * X;       // one z row of one component
   const int64_t comp = (int64_t)nz * plane;   // one component of one RHS
+  // the tensor values of this thread's positions p = warp + 5 q, loaded once for all RHS when
+  // they fit in registers (they are the same for every RHS of the batch)
+  constexpr int Q = (Z + 4) / 5;
+  constexpr bool kHoist = sizeof(C) * 7 * Q <= 256;
+  C gq[kHoist ? Q : 1][7];
+  if constexpr (kHoist) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int p = warp + 5 * q;
+      const int kz = bit_reverse<BITS>(p < Z ? p : 0);
+#pragma unroll
+      for (int k = 0; k < 7; ++k)
+        gq[q][k] = (col_ok && p < Z) ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : czero<C>();
+    }
+  }
   __syncthreads();
   for (int b = 0; b < nrhs; ++b) {
     ST* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X + kx;
@@ -308,14 +323,26 @@ __global__ void __launch_bounds__(5 * kZregCols)
       for (int p = 0; p < Z; ++p) S[(warp * Z + p) * kZregCols + lane] = v[p];
     }
     __syncthreads();
-    for (int p = warp; p < Z; p += 5) {   // position p holds kz = bitrev(p)
-      const int kz = bit_reverse<BITS>(p);
-      C g[7];
+    if constexpr (kHoist) {
 #pragma unroll
-      for (int k = 0; k < 7; ++k) g[k] = col_ok ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : czero<C>();
-      C* q = S + p * kZregCols + lane;
-      constexpr int cs = Z * kZregCols;
-      tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+      for (int qi = 0; qi < Q; ++qi) {
+        const int p = warp + 5 * qi;
+        if (p < Z) {
+          C* q = S + p * kZregCols + lane;
+          constexpr int cs = Z * kZregCols;
+          tensor_apply(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+        }
+      }
+    } else {
+      for (int p = warp; p < Z; p += 5) {   // position p holds kz = bitrev(p)
+        const int kz = bit_reverse<BITS>(p);
+        C g[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) g[k] = col_ok ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : czero<C>();
+        C* q = S + p * kZregCols + lane;
+        constexpr int cs = Z * kZregCols;
+        tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+      }
     }
     __syncthreads();
     {
