@@ -488,35 +488,55 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* con
 // dot work whose loads are independent of one another.
 constexpr int kSolveWarps = 4;
 constexpr int kBlk = 32;
+// levels whose largest factor panel (nf x ns entries) fits this many bytes per warp stage the panel
+// in shared memory with cp.async at the start of the solve (its loads overlap the gather), so the
+// dependent block-by-block reads that follow hit shared memory
+constexpr size_t kStagePanelBytes = 24 * 1024;
+
+__device__ __forceinline__ void cp_async8(void* s, const void* g) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
 
 template <typename T>
 struct SolveSmem {
   using C = cplx<T>;
   static __host__ __device__ size_t vec_bytes(int max_nf) { return ((size_t)max_nf * sizeof(C) + 15) & ~(size_t)15; }
-  static __host__ __device__ size_t per_warp(int max_nf) {   // backward solve: vector, block, y
-    return vec_bytes(max_nf) + kBlk * (kBlk + 1) * sizeof(T) + kBlk * sizeof(C);
+  static __host__ __device__ size_t panel_bytes(int max_panel) { return ((size_t)max_panel * sizeof(T) + 15) & ~(size_t)15; }
+  static __host__ __device__ size_t per_warp(int max_nf, int max_panel = 0) {   // backward: vector, block, y, panel
+    return vec_bytes(max_nf) + kBlk * (kBlk + 1) * sizeof(T) + kBlk * sizeof(C) + panel_bytes(max_panel);
   }
-  static __host__ __device__ size_t per_warp_fwd(int max_nf) { return vec_bytes(max_nf) + kBlk * sizeof(C); }
+  static __host__ __device__ size_t per_warp_fwd(int max_nf, int max_panel = 0) {
+    return vec_bytes(max_nf) + kBlk * sizeof(C) + panel_bytes(max_panel);
+  }
 };
 
-template <typename T>
+template <typename T, bool STAGE>
 __global__ void __launch_bounds__(32 * kSolveWarps, 4)
     k_chol_fsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
                   const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, T* const* __restrict__ Wp,
                   cplx<T>* __restrict__ x, int64_t ldx, int64_t xoff, cplx<T>* __restrict__ U, int64_t u_total,
-                  int max_nf) {
+                  int max_nf, int max_panel) {
   using C = cplx<T>;
   using Dot = typename dot_of<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
   if (item >= (int64_t)nlev * B) return;
-  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp_fwd(max_nf);
+  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp_fwd(max_nf, STAGE ? max_panel : 0);
   C* t = reinterpret_cast<C*>(base);
   C* yb = reinterpret_cast<C*>(base + SolveSmem<T>::vec_bytes(max_nf));
+  T* panel = reinterpret_cast<T*>(yb + kBlk);
   const FrontInfo f = fr[lev[item % nlev]];
   const int b = (int)(item / nlev);
   const T* F = Wp[b] + f.w_off;
+  if constexpr (STAGE) {   // the first ns columns (rows 0..nf-1) are all the solve reads
+    for (int e = lane; e < f.nf * f.ns; e += 32) cp_async8(panel + e, F + e);
+  }
   C* xb = x + b * ldx + xoff;
   C* Ub = U + b * u_total;
   const int32_t* rw = rows + f.rows_off;
@@ -552,6 +572,11 @@ __global__ void __launch_bounds__(32 * kSolveWarps, 4)
         }
     }
     __syncwarp();
+  }
+  if constexpr (STAGE) {
+    cp_async_commit_wait();
+    __syncwarp();
+    F = panel;
   }
   for (int j0 = 0; j0 < ns; j0 += kBlk) {
     const int w = min(kBlk, ns - j0);
@@ -606,23 +631,28 @@ __global__ void __launch_bounds__(32 * kSolveWarps, 4)
   }
 }
 
-template <typename T>
+template <typename T, bool STAGE>
 __global__ void __launch_bounds__(32 * kSolveWarps)
     k_chol_bsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
                   const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x, int64_t ldx,
-                  int64_t xoff, int max_nf, double2* __restrict__ xd, int64_t ldxd) {
+                  int64_t xoff, int max_nf, double2* __restrict__ xd, int64_t ldxd, int max_panel) {
   using C = cplx<T>;
   using Dot = typename dot_of<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
   if (item >= (int64_t)nlev * B) return;
-  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp(max_nf);
+  unsigned char* base = smem_raw + warp * SolveSmem<T>::per_warp(max_nf, STAGE ? max_panel : 0);
   C* t = reinterpret_cast<C*>(base);
   T(*Lb)[kBlk + 1] = reinterpret_cast<T(*)[kBlk + 1]>(base + SolveSmem<T>::vec_bytes(max_nf));
+  T* panel = reinterpret_cast<T*>(base + SolveSmem<T>::vec_bytes(max_nf) + kBlk * (kBlk + 1) * sizeof(T) +
+                                  kBlk * sizeof(C));
   const FrontInfo f = fr[lev[item % nlev]];
   const int b = (int)(item / nlev);
   const T* F = Wp[b] + f.w_off;
+  if constexpr (STAGE) {
+    for (int e = lane; e < f.nf * f.ns; e += 32) cp_async8(panel + e, F + e);
+  }
   C* xb = x + b * ldx + xoff;
   const int32_t* rw = rows + f.rows_off;
   const int nf = f.nf, ns = f.ns;
@@ -636,6 +666,11 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
       if (ix[u] >= 0) t[r0 + 32 * u] = xb[ix[u]];
   }
   __syncwarp();
+  if constexpr (STAGE) {
+    cp_async_commit_wait();
+    __syncwarp();
+    F = panel;
+  }
   // z_own -= L21^T x_bnd, column-oriented: lane j walks its own column (contiguous rows, no
   // cross-lane reductions)
   for (int j = lane; j < ns; j += 32) {
@@ -905,15 +940,19 @@ template <typename T>
 void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t ldx, int64_t xoff, cplx<T>* U,
                 cudaStream_t st, double2* xd, int64_t ldxd) {
   if (s.nfronts == 0 || B == 0) return;
-  const size_t sm_max = kSolveWarps * SolveSmem<T>::per_warp(s.max_nf);
+  const int stage_max = (int)(kStagePanelBytes / sizeof(T));   // panel entries a warp may stage
+  const size_t sm_max = kSolveWarps * SolveSmem<T>::per_warp(s.max_nf, stage_max);
   VH_REQUIRE(sm_max <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
   VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)WideSmem<T>::bytes(s.max_nf)));
   VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)WideSmem<T>::bytes(s.max_nf)));
   auto wide = [&](size_t h) { return (int)s.levels[h].size() <= kWideMaxFronts; };
+  auto panel = [&](size_t h) { return s.level_max_nf[h] * s.level_max_ns[h]; };   // bounds every front's nf * ns
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();
     const int mnf = s.level_max_nf[h];
@@ -924,10 +963,16 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       VH_CUDA_TRY(cudaGetLastError());
       continue;
     }
-    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp_fwd(mnf);
+    const int mp = panel(h);
+    const bool stage = mp <= stage_max;
+    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp_fwd(mnf, stage ? mp : 0);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
-    k_chol_fsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows, s.d_relmap,
-                                                           Wp, x, ldx, xoff, U, s.u_total, mnf);
+    if (stage)
+      k_chol_fsolve<T, true><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows,
+                                                                  s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf, mp);
+    else
+      k_chol_fsolve<T, false><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows,
+                                                                   s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf, 0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -941,10 +986,16 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       VH_CUDA_TRY(cudaGetLastError());
       continue;
     }
-    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf);
+    const int mp = panel(hh);
+    const bool stage = mp <= stage_max;
+    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf, stage ? mp : 0);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
-    k_chol_bsolve<T><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp, x, ldx,
-                                                           xoff, mnf, xd, ldxd);
+    if (stage)
+      k_chol_bsolve<T, true><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp,
+                                                                  x, ldx, xoff, mnf, xd, ldxd, mp);
+    else
+      k_chol_bsolve<T, false><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp,
+                                                                   x, ldx, xoff, mnf, xd, ldxd, 0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
