@@ -329,12 +329,13 @@ def run_ours(args, rank, world):
                 "avg_launch_ms": round(conv_ms / conv_calls, 4),
                 "share_of_step_time": round(conv_ms / step_ms_total, 4), "note": note}
 
-    roof64 = fft_roofline(0, 16, "FFT circulant matvec, complex128 (FP64 refinement residuals; 5 passes)",
-                          "fft_matvec_c128_spiral.txt",
-                          "bound in fact by GB300's FP64 pipe (84-87 % busy in ncu), not HBM; frac is against "
-                          "HBM with the algorithmic bytes of the two-pass pruned model")
+    roof64 = fft_roofline(0, 16, "FFT circulant matvec, complex128 storage (refinement residuals, VH_PREC_DF: FP64 "
+                          "x/y passes, double-float z-pass; 5 passes)", "fft_matvec_df_spiral.txt",
+                          "x/y passes bound by GB300's FP64 pipe (84-85 % busy in ncu), the double-float z-pass "
+                          "issue-bound (62 %); frac is against HBM with the algorithmic bytes of the two-pass "
+                          "pruned model")
     roof32 = fft_roofline(1, 8, "FFT circulant matvec, complex64 (inner GMRES matvecs; 5 passes)",
-                          "fft_matvec_c64_spiral.txt", "issue-bound passes (60-71 % issue active in ncu)")
+                          "fft_matvec_c64_spiral.txt", "issue-bound passes (56-70 % issue active in ncu)")
     if roof64 and roof32 and sections["fft_conv_c64"]["ms"] > sections["fft_conv_c128"]["ms"]:
         roof, roof_other = roof32, roof64
     else:
@@ -456,8 +457,8 @@ def run_probe(args):
     B = args.probe_rhs
     x = torch.randn(B, g.n, 2, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
-    if args.probe in ("conv32", "conv64"):
-        prec = _lib.PREC["fp32" if args.probe == "conv32" else "fp64"]
+    if args.probe in ("conv32", "conv64", "convdf"):
+        prec = _lib.PREC[{"conv32": "fp32", "conv64": "fp64", "convdf": "df"}[args.probe]]
         for _ in range(args.probe_iters):
             _lib.check(lib.vh_matvec_device(g.handle, B, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), None,
                                             None, prec), g.ctx.handle)
@@ -474,7 +475,7 @@ def run_probe(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["conv32", "conv64", "precon"], default=None,
+    ap.add_argument("--probe", choices=["conv32", "conv64", "convdf", "precon"], default=None,
                     help="profiling aid: run a few calls of one operator instead of the benchmark")
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: run only the warm-up and timed mixed-precision sweeps, print nothing")
