@@ -499,16 +499,33 @@ void gmres_core(const KrylovOps& op, int B, const double2* b, const double* tol,
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     VH_CUDA_TRY(cudaStreamSynchronize(st));
-    VH_CUDA_TRY(cudaMemcpyAsync(coef.p, cr.data(), cr.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
-    VH_CUDA_TRY(cudaMemcpyAsync(d_cnt.p, cntr.data(), na * sizeof(int), cudaMemcpyHostToDevice, st));
-    k_combine<<<dim3(grid1(n), na), 256, 0, st>>>(V.p, ldv, ldb, d_act.p, coef.p, m + 2, d_cnt.p, R.p, n, n, 0);
-    count_launch();
-    VH_CUDA_TRY(cudaGetLastError());
-    VH_CUDA_TRY(cudaStreamSynchronize(st));
-    // outer loop condition of pgmres.m:153: resvec(it) > tol && outit < maxit
-    std::vector<int> still;
-    for (int bb : active)
-      if (out.resvec[bb].back() > tol[bb] && out.outer[bb] < maxit) still.push_back(bb);
+    // outer loop condition of pgmres.m:153: resvec(it) > tol && outit < maxit; only the RHS that
+    // go on to another cycle need the restart residual r = V res
+    std::vector<int> still, spos;
+    for (int a = 0; a < na; ++a) {
+      const int bb = active[a];
+      if (out.resvec[bb].back() > tol[bb] && out.outer[bb] < maxit) {
+        still.push_back(bb);
+        spos.push_back(a);
+      }
+    }
+    if (!still.empty()) {
+      const int ns = (int)still.size();
+      std::vector<double2> crs((size_t)ns * (m + 2));
+      std::vector<int> cnts(ns);
+      for (int i = 0; i < ns; ++i) {
+        std::copy(cr.begin() + (size_t)spos[i] * (m + 2), cr.begin() + (size_t)(spos[i] + 1) * (m + 2),
+                  crs.begin() + (size_t)i * (m + 2));
+        cnts[i] = cntr[spos[i]];
+      }
+      upload_act(still);
+      VH_CUDA_TRY(cudaMemcpyAsync(coef.p, crs.data(), crs.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
+      VH_CUDA_TRY(cudaMemcpyAsync(d_cnt.p, cnts.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+      k_combine<<<dim3(grid1(n), ns), 256, 0, st>>>(V.p, ldv, ldb, d_act.p, coef.p, m + 2, d_cnt.p, R.p, n, n, 0);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+      VH_CUDA_TRY(cudaStreamSynchronize(st));
+    }
     active.swap(still);
   }
   // ---- true relative residual |b - A x| / |b|  (pgmres.m:181); skipped for the inner solves of
