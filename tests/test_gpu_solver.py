@@ -416,3 +416,47 @@ def test_factor_sharing_across_frequencies(lib):
     it_ref = np.array([len(r) for r in ref["resvec"]])
     it = np.array([len(r) for r in out["resvec"]])
     assert np.all(it <= it_ref + 1)
+
+
+def test_serving_small_requests(lib):
+    """The serving loop (voxhenry_gb300.serving) on the smallest requests of the seeded stream:
+    every request converges, and a request's R and L equal a direct sweep of its workload."""
+    vie, ex = lib
+    import torch
+
+    from voxhenry_gb300 import serving, structure
+
+    reqs = [r for r in serving.request_stream(60) if r.workload.sigma_e.size < 6e4][:3]
+    free, _ = torch.cuda.mem_get_info()
+    served = serving.serve(reqs, budget_bytes=int(0.5 * free))
+    assert served["converged"].all() and len(served["service_s"]) == len(reqs)
+    assert np.all(served["service_s"] > 0)
+    w = reqs[0].workload
+    P = structure.problem_from_workload(w)
+    a = ex.Sweep(P, w.freqs, precon="schur_invert_df").prepare().solve(restart=50, tol=1e-9, maxit=10, prec="fp32")
+    b = ex.Sweep(P, w.freqs).prepare().solve(restart=50, tol=1e-12, maxit=20)
+    assert_port_matrix_close(a["R"], b["R"], 1e-6)
+    assert_port_matrix_close(a["L"], b["L"], 1e-6)
+
+
+def test_padded_grid_matches_oracle(lib):
+    """A 47 x 13 x 5 grid (padded FFT lengths 94, 26 with primes 47, 13) is grown to 48 x 14 x 5 for the
+    device FFT; R and L equal the oracle's on the original grid (scipy FFT takes any length)."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+    from voxhenry_gb300 import structure as vstructure
+
+    w = geometry.two_bars(L=47, M=13, N=5, xr=(1, 45), zr=(1, 4), y1=(1, 4), y2=(8, 11))
+    P = vstructure.problem_from_workload(w)
+    assert P.meta.get("grid_padded_from") == (47, 13, 5)
+    freqs = np.array([1e6, 5e9])
+    out = ex.Sweep(P, freqs).prepare().solve(restart=50, tol=1e-12, maxit=20)
+    fN, st = circulant.generate_circulant_tensor(w.dx, 1.0, 47, 13, 5)
+    Sy = solver_system(w)
+    ref = solver.solve_frequencies(Sy, fN, st, freqs, restart=50, tol=1e-12)
+    assert_port_matrix_close(out["R"], ref["R"], 1e-8)
+    assert_port_matrix_close(out["L"], ref["L"], 1e-8)
+
+
+def solver_system(w):
+    return structure.build_system(w.sigma_e, w.lambdaL, w.dx, w.pnt_lft, w.pnt_rght)

@@ -82,3 +82,17 @@ def test_factor_share_groups_and_a_inv():
     assert len(np.unique(executer.factor_share_groups(A, 0.0))) == len(freqs)
     assert len(np.unique(executer.factor_share_groups(A, 10.0))) == 1
     assert 1 < len(np.unique(executer.factor_share_groups(A, 1e-4))) < len(freqs)
+
+
+def test_grid_padding_to_fft_lengths_keeps_the_system():
+    """A grid with a prime dimension (47) is grown with empty voxels to 7-smooth dimensions when the
+    tensor is left to the device; the reduced incidence matrix and the RHS are unchanged."""
+    from voxhenry_gb300 import geometry, structure
+
+    assert [structure.smooth7(n) for n in (1, 11, 13, 47, 49, 97, 128)] == [1, 12, 14, 48, 49, 98, 128]
+    w = geometry.two_bars(L=47, M=13, N=5, xr=(1, 45), zr=(1, 4), y1=(1, 4), y2=(8, 11))
+    P0 = structure.build_problem(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght, tensor=(np.zeros(1), np.zeros(3)))
+    P1 = structure.build_problem(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    assert (P1.L, P1.M, P1.N) == (48, 14, 5) and P1.meta["grid_padded_from"] == (47, 13, 5)
+    assert (P0.Ar != P1.Ar).nnz == 0 and np.array_equal(P0.rhs, P1.rhs)
+    assert np.array_equal(P0.idxS.size, P1.idxS.size)

@@ -753,6 +753,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
 // the rows: coalesced loads, then a shuffle sum), the diagonal block on warp 0 and the block's
 // column updates one thread per column.
 constexpr int kWideWarps = 8;
+constexpr size_t kWarpSolveSmemMax = 160 * 1024;   // warp-per-front CTAs above this go wide
 constexpr int kWideMaxFronts = 16;   // levels with at most this many fronts take the wide kernels
 
 template <typename T>
@@ -941,18 +942,36 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
                 cudaStream_t st, double2* xd, int64_t ldxd) {
   if (s.nfronts == 0 || B == 0) return;
   const int stage_max = (int)(kStagePanelBytes / sizeof(T));   // panel entries a warp may stage
-  const size_t sm_max = kSolveWarps * SolveSmem<T>::per_warp(s.max_nf, stage_max);
-  VH_REQUIRE(sm_max <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)WideSmem<T>::bytes(s.max_nf)));
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)WideSmem<T>::bytes(s.max_nf)));
-  auto wide = [&](size_t h) { return (int)s.levels[h].size() <= kWideMaxFronts; };
   auto panel = [&](size_t h) { return s.level_max_nf[h] * s.level_max_ns[h]; };   // bounds every front's nf * ns
+  auto stage = [&](size_t h) { return panel(h) <= stage_max; };
+  auto warp_smem = [&](size_t h, bool fwd) {
+    const int mp = stage(h) ? panel(h) : 0;
+    return kSolveWarps * (fwd ? SolveSmem<T>::per_warp_fwd(s.level_max_nf[h], mp)
+                              : SolveSmem<T>::per_warp(s.level_max_nf[h], mp));
+  };
+  // a level of few fronts, or of fronts whose per-warp vectors do not fit four to a CTA, takes the
+  // wide kernels (one CTA per front and RHS)
+  auto wide = [&](size_t h) {
+    return (int)s.levels[h].size() <= kWideMaxFronts || warp_smem(h, false) > kWarpSolveSmemMax;
+  };
+  size_t sm_f[2] = {0, 0}, sm_b[2] = {0, 0}, sm_w = 0;
+  for (size_t h = 0; h < s.levels.size(); ++h) {
+    if (wide(h)) {
+      sm_w = std::max(sm_w, WideSmem<T>::bytes(s.level_max_nf[h]));
+    } else {
+      sm_f[stage(h)] = std::max(sm_f[stage(h)], warp_smem(h, true));
+      sm_b[stage(h)] = std::max(sm_b[stage(h)], warp_smem(h, false));
+    }
+  }
+  VH_REQUIRE(sm_w <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
+  if (sm_f[0]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_f[0]));
+  if (sm_f[1]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_f[1]));
+  if (sm_b[0]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b[0]));
+  if (sm_b[1]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b[1]));
+  if (sm_w) {
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w));
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w));
+  }
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();
     const int mnf = s.level_max_nf[h];
@@ -964,10 +983,10 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       continue;
     }
     const int mp = panel(h);
-    const bool stage = mp <= stage_max;
-    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp_fwd(mnf, stage ? mp : 0);
+    const bool stg = stage(h);
+    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp_fwd(mnf, stg ? mp : 0);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
-    if (stage)
+    if (stg)
       k_chol_fsolve<T, true><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[h], nlev, B, s.d_fronts, s.d_rows,
                                                                   s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf, mp);
     else
@@ -987,10 +1006,10 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       continue;
     }
     const int mp = panel(hh);
-    const bool stage = mp <= stage_max;
-    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf, stage ? mp : 0);
+    const bool stg = stage(hh);
+    const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf, stg ? mp : 0);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
-    if (stage)
+    if (stg)
       k_chol_bsolve<T, true><<<grid, 32 * kSolveWarps, smh, st>>>(s.d_levels[hh], nlev, B, s.d_fronts, s.d_rows, Wp,
                                                                   x, ldx, xoff, mnf, xd, ldxd, mp);
     else

@@ -59,11 +59,40 @@ def _node_ids(idxS, shape, apid, rows):
     return apid[pos, rows[:, 3] - 1]
 
 
+def smooth7(n: int) -> int:
+    """The least m >= n whose only prime factors are 2, 3, 5 and 7 (lengths the device FFT takes)."""
+    m = max(1, int(n))
+    while True:
+        r = m
+        for p in (2, 3, 5, 7):
+            while r % p == 0:
+                r //= p
+        if r == 1:
+            return m
+        m += 1
+
+
 def build_problem(sigma_e, lambdaL, dx, pnt_lft, pnt_rght, pnt_well_cond=None, tensor=None, meta=None):
     """Inputs of the solve loop.  tensor: (fN_all2, st2) host arrays, or None to leave the tensor to
-    the device (Problem.fN_all2 = None; Sweep then generates it in place)."""
+    the device (Problem.fN_all2 = None; Sweep then generates it in place).
+
+    With the tensor left to the device, a grid whose padded FFT lengths 2L, 2M, 2N have a prime factor
+    above 7 is extended with empty voxels at its high ends to the next lengths that do not: the
+    operator on the voxels, their order, the panel numbering and the port rows are unchanged (MATLAB's
+    FFTW takes any length; the device FFT takes radices 2, 3, 5, 7)."""
     sigma_e = np.asfortranarray(sigma_e)
     L, M, N = sigma_e.shape
+    if tensor is None and (smooth7(L), smooth7(M), smooth7(N)) != (L, M, N):
+        shape = (smooth7(L), smooth7(M), smooth7(N))
+        grown = np.zeros(shape, order="F")
+        grown[:L, :M, :N] = sigma_e
+        if lambdaL is not None:
+            lam = np.zeros(shape, order="F")
+            lam[:L, :M, :N] = lambdaL
+            lambdaL = lam
+        meta = dict(meta or {}, grid_padded_from=(L, M, N))
+        sigma_e = grown
+        L, M, N = shape
     idxS = nonempty_voxels(sigma_e, lambdaL)
     apid, num_nodes = panel_ids(idxS, L, M, N)
     Ae = incidence(apid, num_nodes)
