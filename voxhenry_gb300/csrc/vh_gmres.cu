@@ -912,6 +912,7 @@ vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, co
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     cudaStream_t st = g->ctx->stream;
     const int64_t n = g->n;
+    PoolScope pool_scope(&g->ctx->pool);   // the staging buffers come from the context pool too
     DevBuf<double2> db, dx;
     db.ensure((size_t)B * n);
     dx.ensure((size_t)B * n);
