@@ -567,9 +567,10 @@ void gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, co
       sc[a] = scale_h ? scale_h[act[a]] : make_double2(1.0, 0.0);
       zs[a] = zslot_h ? zslot_h[act[a]] : 0;
     }
+    // a host-to-device copy from pageable memory has read its source when the call returns, so the
+    // host arrays may go and the stream runs on without a host synchronisation
     VH_CUDA_TRY(cudaMemcpyAsync(d_scale.p, sc.data(), na * sizeof(double2), cudaMemcpyHostToDevice, st));
     matvec_device(g, na, xin, yout, d_scale.p, zs.data(), p);
-    VH_CUDA_TRY(cudaStreamSynchronize(st));   // host arrays above must outlive the copies
   };
   if (pcs)
     op.M = [&](const std::vector<int>& act, const double2* xin, double2* yout) {
@@ -684,11 +685,10 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
       zs[a] = zslot_h ? zslot_h[act[a]] : 0;
       sc[a] = scale_h ? scale_h[act[a]] : make_double2(1.0, 0.0);
     }
-    DevBuf<double2> dsc;
+    DevBuf<double2> dsc;   // pool buffers are reused in stream order
     dsc.ensure(na);
     VH_CUDA_TRY(cudaMemcpyAsync(dsc.p, sc.data(), na * sizeof(double2), cudaMemcpyHostToDevice, st));
     matvec_device(g, na, xin, yout, dsc.p, zs.data(), p);
-    VH_CUDA_TRY(cudaStreamSynchronize(st));
     out.matvecs += na;
   };
   auto M = [&](const std::vector<int>& act, const double2* xin, double2* yout) {

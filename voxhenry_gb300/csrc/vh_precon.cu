@@ -290,8 +290,7 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
-  // keep the host pointer table alive until the copy has been consumed
-  VH_CUDA_TRY(cudaStreamSynchronize(st));
+  // the pointer table was read from pageable host memory when its copy returned: no host wait here
 }
 
 int precon_kind(const vh_precon* p) { return p->kind; }
