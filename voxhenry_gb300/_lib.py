@@ -14,6 +14,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libvhgpu.so")
 
 VH_OK = 0
+VH_ERR_OOM = 2
 STATUS = {0: "VH_OK", 1: "VH_ERR_BAD_ARG", 2: "VH_ERR_OOM", 3: "VH_ERR_UNSUPPORTED", 4: "VH_ERR_TIMEOUT",
           5: "VH_ERR_NOT_CONVERGED", 6: "VH_ERR_CUDA", 7: "VH_ERR_NO_DEVICE"}
 PREC = {"fp64": 0, "fp32": 1, "df": 2}

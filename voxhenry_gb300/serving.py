@@ -120,7 +120,9 @@ def footprint_bytes(prob, nfreq: int, restart: int = 50, exact: bool = True) -> 
     P = 8 * prob.L * prob.M * prob.N
     n = prob.Ar.shape[0] + prob.Ar.shape[1]
     B = nfreq * prob.num_ports
-    base = 7 * P * (16 + 8 + 16) + B * n * 16 * (restart + 12)
+    # Krylov basis (restart + 1 vectors), GMRES and refinement work vectors (~20), FFT scratch of
+    # the complex128 product (two 5-component half-padded spectra per RHS)
+    base = 7 * P * (16 + 8 + 16) + B * n * 16 * (restart + 24) + B * 5 * P * 16 // 2
     if not exact:
         return int(base + nfreq * 64 * prob.Ar.shape[0] * 8)
     lib = _lib.load()
@@ -153,18 +155,29 @@ def serve(requests, budget_bytes: int, prec: str = "fp32", tol: float = 1e-9, re
         # admission: the frequencies that fit the budget together (the exact factor size only when
         # the cheap bound does not fit)
         need = footprint_bytes(prob, nf, restart, exact=False)
-        if need > budget_bytes:
+        if need > budget_bytes // 2:
             need = footprint_bytes(prob, nf, restart, exact=True)
         chunk = nf if need <= budget_bytes else max(1, int(budget_bytes // max(1, need // nf)))
         flags = []
-        for c0 in range(0, nf, chunk):
-            sw = executer.Sweep(prob, w.freqs[c0:c0 + chunk], want_fp32=True,
-                                precon="schur_invert_df" if prec == "fp32" else "schur_invert")
-            out = sw.prepare().solve(restart=restart, tol=tol, maxit=10, prec=prec)
+        c0 = 0
+        while c0 < nf:
+            sw = None
+            try:
+                sw = executer.Sweep(prob, w.freqs[c0:c0 + chunk], want_fp32=True,
+                                    precon="schur_invert_df" if prec == "fp32" else "schur_invert")
+                out = sw.prepare().solve(restart=restart, tol=tol, maxit=10, prec=prec)
+            except _lib.VHError as e:   # the model missed: halve the chunk and retry (OOM is a status)
+                if e.status != _lib.VH_ERR_OOM or chunk == 1:
+                    raise
+                chunk = max(1, chunk // 2)
+                continue
+            finally:
+                if sw is not None:
+                    for p in sw.pcs or []:
+                        p.close()
+                    sw.geom.close()
             flags.append(np.asarray(out["flag"]))
-            for p in sw.pcs:
-                p.close()
-            sw.geom.close()
+            c0 += chunk
         torch.cuda.synchronize()
         service.append(time.perf_counter() - t0)
         points.append(nf)
