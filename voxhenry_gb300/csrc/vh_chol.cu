@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(NT)
   const int nf = f.nf, ns = f.ns;
   T* F = W + f.w_off;
   T* inv_s = S + nf * (nf + 1) / 2;   // 1 / L(j, j)
-  T* coefs = inv_s + ns;                // per pivot j: S(j + 1 + c, j) / S(j, j), c < nf - j - 1
+  T* coefs = inv_s + ns;                // per pivot j: S(j + 1 + c, j) / S(j, j), c < nf - j - 1 (two arrays)
   auto col = [&](int k) { return S + tri_off(k, nf) - k; };   // col(k)[i] = (i, k), i >= k
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int nwarps = NT / 32;
@@ -305,59 +305,134 @@ __global__ void __launch_bounds__(NT)
     }
     front_bar<NT>();
   }
-  T prev_piv = T(0), prev_inv = T(0);
-  for (int j = 0; j < ns; ++j) {
-    T* colj = col(j);
-    const T piv = colj[j];        // final: updated last in step j-1, before its barrier
-    if (!(piv > T(0))) {          // uniform: every thread reads the same value
+  // Pivots go in pairs (j, j+1): pivot j's coefficients, a rank-1 update of column j+1 alone,
+  // pivot j+1's coefficients, then one walk over the remaining triangle applies both pivots to each
+  // entry with one load, one pair-precision dot (two products, one normalisation) and one store.
+  // An odd last pivot takes the single-pivot step.  Pivot columns are scaled by 1 / L(j, j) after
+  // their last use (deferred to the next step).
+  using Dot = typename dot_of<T>::type;
+  T* coefs1 = coefs + nf;   // second pivot's column coefficients
+  int ndef = 0, defj[2] = {0, 0};
+  T defpiv[2] = {T(0), T(0)}, definv[2] = {T(0), T(0)};
+  auto scale_deferred = [&]() {
+    for (int d = 0; d < ndef; ++d) {
+      T* colp = col(defj[d]);
+      for (int i = defj[d] + tid; i < nf; i += NT) colp[i] = (i == defj[d]) ? defpiv[d] * definv[d] : colp[i] * definv[d];
+    }
+    ndef = 0;
+  };
+  // position (c, p) of flat index t in the column-major lower triangle of order m
+  auto locate = [&](int t, int m, int& c, int& p) {
+    const float mf = 2.0f * m + 1.0f;
+    c = (int)((mf - sqrtf(fmaxf(mf * mf - 8.0f * t, 0.0f))) * 0.5f);
+    c = max(0, min(c, m - 1));
+    while (c > 0 && tri_off(c, m) > t) --c;
+    while (c + 1 < m && tri_off(c + 1, m) <= t) ++c;
+    p = t - tri_off(c, m);
+  };
+  for (int j = 0; j < ns;) {
+    T* c0 = col(j);
+    const T piv0 = c0[j];         // final: updated last in the previous step, before its barrier
+    if (!(piv0 > T(0))) {         // uniform: every thread reads the same value
       if (tid == 0) atomicExch(err, 1);
       return;
     }
-    const T inv = rsqrt_t(piv);
-    const T inv2 = inv * inv;
-    if (tid == 0) inv_s[j] = inv;
-    if (j > 0) {                  // deferred scaling of column j-1
-      T* colp = col(j - 1);
-      for (int i = j - 1 + tid; i < nf; i += NT) colp[i] = (i == j - 1) ? prev_piv * prev_inv : colp[i] * prev_inv;
-    }
-    // S(i, k) -= S(i, j) S(k, j) / piv for j < k <= i < nf: trailing column c = k - j - 1 holds m - c entries
-    const int m = nf - j - 1;
-    for (int c = tid; c < m; c += NT) coefs[c] = colj[j + 1 + c] * inv2;   // once per column, not per entry
+    const T inv0 = rsqrt_t(piv0);
+    const T inv0sq = inv0 * inv0;
+    if (tid == 0) inv_s[j] = inv0;
+    scale_deferred();
+    const int m0 = nf - j - 1;
+    for (int c = tid; c < m0; c += NT) coefs[c] = c0[j + 1 + c] * inv0sq;   // once per column, not per entry
     front_bar<NT>();
-    const int total = (m * (m + 1)) / 2;
-    if (tid < total) {
-      const float mf = 2.0f * m + 1.0f;
-      int c = (int)((mf - sqrtf(fmaxf(mf * mf - 8.0f * tid, 0.0f))) * 0.5f);
-      c = max(0, min(c, m - 1));
-      while (c > 0 && tri_off(c, m) > tid) --c;
-      while (c + 1 < m && tri_off(c + 1, m) <= tid) ++c;
-      int p = tid - tri_off(c, m);           // position within column c: row k + p
-      T coef = coefs[c];
-      T* colk = col(j + 1 + c) + j + 1 + c;  // entry (k, k) of column k = j + 1 + c
-      const T* cj = colj + j + 1 + c;        // S(k, j)
-      for (;;) {
-        colk[p] = fma(-cj[p], coef, colk[p]);
-        p += NT;
-        if (p >= m - c) {
-          do {                               // next column: col(k + 1) + k + 1 = col(k) + k + (nf - k)
-            p -= m - c;
-            colk += m - c;
-            ++cj;
-            ++c;
-          } while (c < m && p >= m - c);
-          if (c >= m) break;
-          coef = coefs[c];
+    if (j + 1 < ns) {
+      // column j+1 (rows j+1..nf-1) -= column j * coefficient of column j+1
+      T* c1 = col(j + 1);
+      const T cf = coefs[0];
+      for (int i = j + 1 + tid; i < nf; i += NT) c1[i] = fma(-c0[i], cf, c1[i]);
+      front_bar<NT>();
+      const T piv1 = c1[j + 1];
+      if (!(piv1 > T(0))) {
+        if (tid == 0) atomicExch(err, 1);
+        return;
+      }
+      const T inv1 = rsqrt_t(piv1);
+      const T inv1sq = inv1 * inv1;
+      if (tid == 0) inv_s[j + 1] = inv1;
+      const int m = nf - j - 2;
+      for (int c = tid; c < m; c += NT) coefs1[c] = c1[j + 2 + c] * inv1sq;
+      front_bar<NT>();
+      // S(i, k) -= S(i, j) S(k, j) / piv0 + S(i, j+1) S(k, j+1) / piv1 for j+1 < k <= i < nf
+      const int total = (m * (m + 1)) / 2;
+      if (tid < total) {
+        int c, p;
+        locate(tid, m, c, p);
+        T cf0 = coefs[c + 1], cf1 = coefs1[c];
+        T* colk = col(j + 2 + c) + j + 2 + c;   // entry (k, k) of column k = j + 2 + c
+        const T* l0 = c0 + j + 2 + c;           // S(k, j)
+        const T* l1 = c1 + j + 2 + c;           // S(k, j+1)
+        for (;;) {
+          Dot acc(colk[p]);
+          acc.add(-l0[p], cf0);
+          acc.add(-l1[p], cf1);
+          colk[p] = acc.value();
+          p += NT;
+          if (p >= m - c) {
+            do {                                // next column: col(k + 1) + k + 1 = col(k) + k + (nf - k)
+              p -= m - c;
+              colk += m - c;
+              ++l0;
+              ++l1;
+              ++c;
+            } while (c < m && p >= m - c);
+            if (c >= m) break;
+            cf0 = coefs[c + 1];
+            cf1 = coefs1[c];
+          }
         }
       }
+      front_bar<NT>();
+      ndef = 2;
+      defj[0] = j;
+      defpiv[0] = piv0;
+      definv[0] = inv0;
+      defj[1] = j + 1;
+      defpiv[1] = piv1;
+      definv[1] = inv1;
+      j += 2;
+    } else {
+      // single pivot: S(i, k) -= S(i, j) S(k, j) / piv0 for j < k <= i < nf
+      const int m = m0;
+      const int total = (m * (m + 1)) / 2;
+      if (tid < total) {
+        int c, p;
+        locate(tid, m, c, p);
+        T coef = coefs[c];
+        T* colk = col(j + 1 + c) + j + 1 + c;
+        const T* cj = c0 + j + 1 + c;
+        for (;;) {
+          colk[p] = fma(-cj[p], coef, colk[p]);
+          p += NT;
+          if (p >= m - c) {
+            do {
+              p -= m - c;
+              colk += m - c;
+              ++cj;
+              ++c;
+            } while (c < m && p >= m - c);
+            if (c >= m) break;
+            coef = coefs[c];
+          }
+        }
+      }
+      front_bar<NT>();
+      ndef = 1;
+      defj[0] = j;
+      defpiv[0] = piv0;
+      definv[0] = inv0;
+      j += 1;
     }
-    prev_piv = piv;
-    prev_inv = inv;
-    front_bar<NT>();
   }
-  if (ns > 0) {
-    T* colp = col(ns - 1);
-    for (int i = ns - 1 + tid; i < nf; i += NT) colp[i] = (i == ns - 1) ? prev_piv * prev_inv : colp[i] * prev_inv;
-  }
+  scale_deferred();
   front_bar<NT>();
   // lower triangle back to the factor storage, except the diagonal blocks of L11 (inverted below)
   for (int k = 0; k < nf; ++k) {
@@ -387,10 +462,10 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-// packed lower triangle, the reciprocal pivots and one pivot's column coefficients
+// packed lower triangle, the reciprocal pivots and two pivots' column coefficients
 template <typename T>
 static size_t fused_smem_bytes(int max_nf, int max_ns) {
-  return ((size_t)max_nf * (max_nf + 1) / 2 + (size_t)max_ns + (size_t)max_nf) * sizeof(T);
+  return ((size_t)max_nf * (max_nf + 1) / 2 + (size_t)max_ns + 2 * (size_t)max_nf) * sizeof(T);
 }
 
 // CTA size for fronts up to order max_nf: one warp up to 64, then 2, 4, 8 warps
