@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(256) k_chol_update(const int32_t* __restrict__
 __host__ __device__ __forceinline__ int tri_off(int c, int m) { return c * m - (c * (c - 1)) / 2; }
 
 constexpr int kLoadBatch = 4;   // independent global loads per thread per step of the load phases
+constexpr int kPanel = 4;       // pivots per panel of the fused front factorisation
 
 template <int NT>
 __device__ __forceinline__ void front_bar() {
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(NT)
   const int nf = f.nf, ns = f.ns;
   T* F = W + f.w_off;
   T* inv_s = S + nf * (nf + 1) / 2;   // 1 / L(j, j)
-  T* coefs = inv_s + ns;                // per pivot j: S(j + 1 + c, j) / S(j, j), c < nf - j - 1 (two arrays)
+  T* coefs = inv_s + ns;                // per panel pivot q: S(j+q+1+c, j+q) / S(j+q, j+q) at coefs[q * nf + c]
   auto col = [&](int k) { return S + tri_off(k, nf) - k; };   // col(k)[i] = (i, k), i >= k
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int nwarps = NT / 32;
@@ -305,15 +306,14 @@ __global__ void __launch_bounds__(NT)
     }
     front_bar<NT>();
   }
-  // Pivots go in pairs (j, j+1): pivot j's coefficients, a rank-1 update of column j+1 alone,
-  // pivot j+1's coefficients, then one walk over the remaining triangle applies both pivots to each
-  // entry with one load, one pair-precision dot (two products, one normalisation) and one store.
-  // An odd last pivot takes the single-pivot step.  Pivot columns are scaled by 1 / L(j, j) after
-  // their last use (deferred to the next step).
+  // Pivots go in panels of up to kPanel (j .. j+P-1): each pivot in turn gives its column
+  // coefficients and a rank-1 update of the panel's later columns; then one walk over the remaining
+  // triangle applies all P pivots to each entry with one load, one pair-precision dot (P products,
+  // one normalisation) and one store.  Pivot columns are scaled by 1 / L(j, j) after their last use
+  // (deferred to the next panel).
   using Dot = typename dot_of<T>::type;
-  T* coefs1 = coefs + nf;   // second pivot's column coefficients
-  int ndef = 0, defj[2] = {0, 0};
-  T defpiv[2] = {T(0), T(0)}, definv[2] = {T(0), T(0)};
+  int ndef = 0, defj[kPanel];
+  T defpiv[kPanel], definv[kPanel];
   auto scale_deferred = [&]() {
     for (int d = 0; d < ndef; ++d) {
       T* colp = col(defj[d]);
@@ -331,106 +331,74 @@ __global__ void __launch_bounds__(NT)
     p = t - tri_off(c, m);
   };
   for (int j = 0; j < ns;) {
-    T* c0 = col(j);
-    const T piv0 = c0[j];         // final: updated last in the previous step, before its barrier
-    if (!(piv0 > T(0))) {         // uniform: every thread reads the same value
-      if (tid == 0) atomicExch(err, 1);
-      return;
-    }
-    const T inv0 = rsqrt_t(piv0);
-    const T inv0sq = inv0 * inv0;
-    if (tid == 0) inv_s[j] = inv0;
+    const int P = min(kPanel, ns - j);
     scale_deferred();
-    const int m0 = nf - j - 1;
-    for (int c = tid; c < m0; c += NT) coefs[c] = c0[j + 1 + c] * inv0sq;   // once per column, not per entry
-    front_bar<NT>();
-    if (j + 1 < ns) {
-      // column j+1 (rows j+1..nf-1) -= column j * coefficient of column j+1
-      T* c1 = col(j + 1);
-      const T cf = coefs[0];
-      for (int i = j + 1 + tid; i < nf; i += NT) c1[i] = fma(-c0[i], cf, c1[i]);
-      front_bar<NT>();
-      const T piv1 = c1[j + 1];
-      if (!(piv1 > T(0))) {
+    for (int q = 0; q < P; ++q) {
+      const int jq = j + q;
+      T* cq = col(jq);
+      const T pv = cq[jq];        // final: updated last before the preceding barrier
+      if (!(pv > T(0))) {         // uniform: every thread reads the same value
         if (tid == 0) atomicExch(err, 1);
         return;
       }
-      const T inv1 = rsqrt_t(piv1);
-      const T inv1sq = inv1 * inv1;
-      if (tid == 0) inv_s[j + 1] = inv1;
-      const int m = nf - j - 2;
-      for (int c = tid; c < m; c += NT) coefs1[c] = c1[j + 2 + c] * inv1sq;
+      const T iv = rsqrt_t(pv);
+      const T iv2 = iv * iv;
+      if (tid == 0) inv_s[jq] = iv;
+      defj[q] = jq;
+      defpiv[q] = pv;
+      definv[q] = iv;
+      T* cf = coefs + q * nf;
+      for (int c = tid; c < nf - jq - 1; c += NT) cf[c] = cq[jq + 1 + c] * iv2;   // once per column
       front_bar<NT>();
-      // S(i, k) -= S(i, j) S(k, j) / piv0 + S(i, j+1) S(k, j+1) / piv1 for j+1 < k <= i < nf
-      const int total = (m * (m + 1)) / 2;
-      if (tid < total) {
-        int c, p;
-        locate(tid, m, c, p);
-        T cf0 = coefs[c + 1], cf1 = coefs1[c];
-        T* colk = col(j + 2 + c) + j + 2 + c;   // entry (k, k) of column k = j + 2 + c
-        const T* l0 = c0 + j + 2 + c;           // S(k, j)
-        const T* l1 = c1 + j + 2 + c;           // S(k, j+1)
-        for (;;) {
-          Dot acc(colk[p]);
-          acc.add(-l0[p], cf0);
-          acc.add(-l1[p], cf1);
-          colk[p] = acc.value();
-          p += NT;
-          if (p >= m - c) {
-            do {                                // next column: col(k + 1) + k + 1 = col(k) + k + (nf - k)
-              p -= m - c;
-              colk += m - c;
-              ++l0;
-              ++l1;
-              ++c;
-            } while (c < m && p >= m - c);
-            if (c >= m) break;
-            cf0 = coefs[c + 1];
-            cf1 = coefs1[c];
-          }
+      const int nk = P - q - 1;   // the panel's later columns jq+1 .. j+P-1 take this pivot now
+      if (nk > 0) {
+        for (int t = tid; t < nk * nf; t += NT) {
+          const int k = jq + 1 + t / nf, i = t % nf;
+          if (i >= k) col(k)[i] = fma(-cq[i], cf[k - jq - 1], col(k)[i]);
         }
+        front_bar<NT>();
       }
-      front_bar<NT>();
-      ndef = 2;
-      defj[0] = j;
-      defpiv[0] = piv0;
-      definv[0] = inv0;
-      defj[1] = j + 1;
-      defpiv[1] = piv1;
-      definv[1] = inv1;
-      j += 2;
-    } else {
-      // single pivot: S(i, k) -= S(i, j) S(k, j) / piv0 for j < k <= i < nf
-      const int m = m0;
-      const int total = (m * (m + 1)) / 2;
-      if (tid < total) {
-        int c, p;
-        locate(tid, m, c, p);
-        T coef = coefs[c];
-        T* colk = col(j + 1 + c) + j + 1 + c;
-        const T* cj = c0 + j + 1 + c;
-        for (;;) {
-          colk[p] = fma(-cj[p], coef, colk[p]);
-          p += NT;
-          if (p >= m - c) {
-            do {
-              p -= m - c;
-              colk += m - c;
-              ++cj;
-              ++c;
-            } while (c < m && p >= m - c);
-            if (c >= m) break;
-            coef = coefs[c];
-          }
-        }
-      }
-      front_bar<NT>();
-      ndef = 1;
-      defj[0] = j;
-      defpiv[0] = piv0;
-      definv[0] = inv0;
-      j += 1;
     }
+    ndef = P;
+    // S(i, k) -= sum_q S(i, j+q) S(k, j+q) / S(j+q, j+q) for j+P <= k <= i < nf
+    const int m = nf - j - P;
+    const int total = (m * (m + 1)) / 2;
+    if (tid < total) {
+      int c, p;
+      locate(tid, m, c, p);
+      const int k0 = j + P + c;
+      T* colk = col(k0) + k0;   // entry (k, k) of column k
+      const T* l[kPanel];
+      T cfv[kPanel];
+#pragma unroll
+      for (int q = 0; q < kPanel; ++q) {
+        l[q] = col(j + min(q, P - 1)) + k0;   // S(k, j+q)
+        cfv[q] = q < P ? coefs[q * nf + c + P - q - 1] : T(0);
+      }
+      for (;;) {
+        Dot acc(colk[p]);
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q)
+          if (q < P) acc.add(-l[q][p], cfv[q]);
+        colk[p] = acc.value();
+        p += NT;
+        if (p >= m - c) {
+          do {                    // next column: col(k + 1) + k + 1 = col(k) + k + (nf - k)
+            p -= m - c;
+            colk += m - c;
+#pragma unroll
+            for (int q = 0; q < kPanel; ++q) ++l[q];
+            ++c;
+          } while (c < m && p >= m - c);
+          if (c >= m) break;
+#pragma unroll
+          for (int q = 0; q < kPanel; ++q)
+            if (q < P) cfv[q] = coefs[q * nf + c + P - q - 1];
+        }
+      }
+    }
+    front_bar<NT>();
+    j += P;
   }
   scale_deferred();
   front_bar<NT>();
@@ -462,10 +430,10 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-// packed lower triangle, the reciprocal pivots and two pivots' column coefficients
+// packed lower triangle, the reciprocal pivots and a panel's column coefficients
 template <typename T>
 static size_t fused_smem_bytes(int max_nf, int max_ns) {
-  return ((size_t)max_nf * (max_nf + 1) / 2 + (size_t)max_ns + 2 * (size_t)max_nf) * sizeof(T);
+  return ((size_t)max_nf * (max_nf + 1) / 2 + (size_t)max_ns + (size_t)kPanel * max_nf) * sizeof(T);
 }
 
 // CTA size for fronts up to order max_nf: one warp up to 64, then 2, 4, 8 warps

@@ -332,10 +332,10 @@ void chol_symbolic(CholSymbolic& s, int L, int M, int N, int64_t nv, const int64
       mnf = std::max(mnf, fi.nf);
     }
   // occupancy classes of the fused fronts: CTAs per SM that the shared memory of a front allows
-  // (the kernel holds the packed lower triangle, ns pivots and two pivots' column coefficients,
-  // 8 bytes each; 228 KB per SM, 1 KB reserved per CTA, at most 16)
+  // (the kernel holds the packed lower triangle, ns pivots and a 4-pivot panel's column
+  // coefficients, 8 bytes each; 228 KB per SM, 1 KB reserved per CTA, at most 16)
   auto ctas_per_sm = [](int nf, int ns) {
-    const size_t bytes = ((size_t)nf * (nf + 1) / 2 + (size_t)ns + 2 * (size_t)nf) * 8 + 1024;
+    const size_t bytes = ((size_t)nf * (nf + 1) / 2 + (size_t)ns + 4 * (size_t)nf) * 8 + 1024;
     return (int)std::min<size_t>(16, std::max<size_t>(1, (228 * 1024) / bytes));
   };
   s.fused_classes.assign(nh, {});
