@@ -118,7 +118,7 @@ def test_matvec_batched_scales_and_slots(vie):
 
 
 def test_matvec_linearity_large(vie):
-    """Size-independent property at a BASELINE-sized grid (64 x 16 x 16 bar): A(ax + by) = aAx + bAy."""
+    """Size-independent property on the full 64 x 16 x 16 bar workload: A(ax + by) = aAx + bAy."""
     from voxhenry_gb300 import geometry
 
     w = geometry.bar()

@@ -155,11 +155,12 @@ def random_blob(shape, fill=0.6, seed=SEED, sigma=(3.5e7, 5.8e7), dx=1e-6) -> Wo
     return Workload("random_blob", s, dx, [face_nodes(m1, "-x")], [face_nodes(m2, "+x")], np.array([1e3, 1e9]))
 
 
-CONFIGS = {
-    "C1": bar,
-    "C2": square_spiral,
-    "C3": two_bars,
-    "C4": ring,
+# the benchmark workloads by name (default arguments give their full sizes)
+WORKLOADS = {
+    "bar_64x16x16": bar,
+    "square_spiral_256x256x8": square_spiral,
+    "two_bars_128x64x32": two_bars,
+    "ring_512x512x16": ring,
 }
 
 
