@@ -460,3 +460,44 @@ def test_padded_grid_matches_oracle(lib):
 
 def solver_system(w):
     return structure.build_system(w.sigma_e, w.lambdaL, w.dx, w.pnt_lft, w.pnt_rght)
+
+
+def test_two_bars_full_size_known_answer_and_mixed_vs_fp64(lib):
+    """The two-bar workload at its full size (128 x 64 x 32, copper and aluminium bars 100 x 10 x 10
+    voxels, 2 ports, 16 frequencies 1 kHz-10 GHz): at 1 kHz each bar's resistance is the DC value
+    l / (sigma A), and the mixed-precision sweep matches the FP64 sweep (relres < 1e-10) within 1e-6."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+    from voxhenry_gb300 import structure as vstructure
+
+    w = geometry.two_bars()
+    P = vstructure.problem_from_workload(w)
+    mixed = ex.Sweep(P, w.freqs, precon="schur_invert_df").prepare().solve(restart=50, tol=1e-9, maxit=10,
+                                                                           prec="fp32")
+    ref = ex.Sweep(P, w.freqs).prepare().solve(restart=50, tol=1e-11, maxit=20)
+    assert np.all(mixed["flag"] == 0) and np.all(ref["relres"] < 1e-10)
+    for p, sigma in enumerate((5.8e7, 3.5e7)):
+        r_dc = 100e-6 / (sigma * (10e-6) ** 2)
+        assert abs(ref["R"][0, p, p] - r_dc) <= 1e-6 * r_dc
+    for f in range(len(w.freqs)):
+        for p in range(2):
+            for key in ("R", "L"):
+                assert abs(mixed[key][f, p, p] - ref[key][f, p, p]) <= 1e-6 * abs(ref[key][f, p, p])
+
+
+def test_ring_full_size_mixed_vs_fp64(lib):
+    """The ring workload at its full size (512 x 512 x 16, padded FFT grid 1024 x 1024 x 32): at three
+    frequencies the mixed-precision R and L match the FP64 sweep (relres < 1e-10) within 1e-6."""
+    vie, ex = lib
+    from voxhenry_gb300 import geometry
+    from voxhenry_gb300 import structure as vstructure
+
+    w = geometry.ring()
+    P = vstructure.problem_from_workload(w)
+    freqs = w.freqs[[0, 8, 15]]
+    mixed = ex.Sweep(P, freqs, precon="schur_invert_df").prepare().solve(restart=50, tol=1e-9, maxit=10,
+                                                                         prec="fp32")
+    ref = ex.Sweep(P, freqs).prepare().solve(restart=50, tol=1e-11, maxit=20)
+    assert np.all(mixed["flag"] == 0) and np.all(ref["relres"] < 1e-10)
+    for key in ("R", "L"):
+        np.testing.assert_allclose(mixed[key], ref[key], rtol=1e-6)
