@@ -209,6 +209,26 @@ __device__ __forceinline__ void tensor_apply(const C* g, C& jx, C& jy, C& jz, C&
   j3 = o5;
 }
 
+// tensor_apply for a spectrum whose components 0, 3, 5, 6 are real and 1, 2, 4 imaginary: g[k] is
+// the real part or the imaginary part, and each product is two real multiplications
+template <typename C, typename T>
+__device__ __forceinline__ void tensor_apply_ri(const T* g, C& jx, C& jy, C& jz, C& j2, C& j3) {
+  auto rm = [](T s, const C& v) { C r; r.x = s * v.x; r.y = s * v.y; return r; };    // s v
+  auto im = [](T s, const C& v) { C r; r.x = -s * v.y; r.y = s * v.x; return r; };   // i s v
+  const C a = im(g[1], jx);               // G2 Jx
+  const C bb = im(g[2], jy);              // G3 Jy
+  const C o1 = cadd(rm(g[0], jx), im(g[1], cadd(j2, j3)));
+  const C o2 = cadd(rm(g[0], jy), im(g[2], csub(j2, j3)));
+  const C o3 = cadd(rm(g[0], jz), im(g[4], j3));
+  const C o4 = cadd(csub(cneg(a), bb), cadd(rm(g[3], j2), rm(g[5], j3)));
+  const C o5 = cadd(cadd(csub(bb, a), cneg(im(g[4], jz))), cadd(rm(g[5], j2), rm(g[6], j3)));
+  jx = o1;
+  jy = o2;
+  jz = o3;
+  j2 = o4;
+  j3 = o5;
+}
+
 // pass 3: z-FFT, tensor product, inverse z-FFT.  B[b][c][z<N][ky][kx] in place.
 // blockDim = Z * tx; thread (kz, tx) keeps the 7 tensor values of its point in registers.
 template <typename T>
@@ -276,9 +296,9 @@ __device__ __forceinline__ float2 zstore(float2 v, float2) { return v; }
 __device__ __forceinline__ double2 zstore(double2 v, double2) { return v; }
 __device__ __forceinline__ double2 zstore(dcomplex v, double2) { return to_d(v); }
 
-template <typename T, int Z, int NZ, typename ST = cplx<T>>
+template <typename T, int Z, int NZ, typename ST = cplx<T>, typename GT = cplx<T>>
 __global__ void __launch_bounds__(5 * kZregCols)
-    k_zpass_reg(ST* __restrict__ Bf, const cplx<T>* __restrict__ tens, int nz, int Y, int X, int nrhs,
+    k_zpass_reg(ST* __restrict__ Bf, const GT* __restrict__ tens, int nz, int Y, int X, int nrhs,
                 const cplx<T>* __restrict__ twg) {
   using C = cplx<T>;
   constexpr int BITS = Z == 8 ? 3 : (Z == 16 ? 4 : 5);
@@ -296,8 +316,9 @@ __global__ void __launch_bounds__(5 * kZregCols)
   // the tensor values of this thread's positions p = warp + 5 q, loaded once for all RHS when
   // they fit in registers (they are the same for every RHS of the batch)
   constexpr int Q = (Z + 4) / 5;
-  constexpr bool kHoist = sizeof(C) * 7 * Q <= 256;
-  C gq[kHoist ? Q : 1][7];
+  constexpr bool kRI = sizeof(GT) < sizeof(C);   // real/imaginary tensor: one T per component
+  constexpr bool kHoist = sizeof(GT) * 7 * Q <= 256;
+  GT gq[kHoist ? Q : 1][7];
   if constexpr (kHoist) {
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -305,7 +326,7 @@ __global__ void __launch_bounds__(5 * kZregCols)
       const int kz = bit_reverse<BITS>(p < Z ? p : 0);
 #pragma unroll
       for (int k = 0; k < 7; ++k)
-        gq[q][k] = (col_ok && p < Z) ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : czero<C>();
+        gq[q][k] = (col_ok && p < Z) ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : GT{};
     }
   }
   __syncthreads();
@@ -330,18 +351,24 @@ __global__ void __launch_bounds__(5 * kZregCols)
         if (p < Z) {
           C* q = S + p * kZregCols + lane;
           constexpr int cs = Z * kZregCols;
-          tensor_apply(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+          if constexpr (kRI)
+            tensor_apply_ri(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+          else
+            tensor_apply(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
         }
       }
     } else {
       for (int p = warp; p < Z; p += 5) {   // position p holds kz = bitrev(p)
         const int kz = bit_reverse<BITS>(p);
-        C g[7];
+        GT g[7];
 #pragma unroll
-        for (int k = 0; k < 7; ++k) g[k] = col_ok ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : czero<C>();
+        for (int k = 0; k < 7; ++k) g[k] = col_ok ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : GT{};
         C* q = S + p * kZregCols + lane;
         constexpr int cs = Z * kZregCols;
-        tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+        if constexpr (kRI)
+          tensor_apply_ri(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+        else
+          tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
       }
     }
     __syncthreads();
@@ -358,21 +385,22 @@ __global__ void __launch_bounds__(5 * kZregCols)
   }
 }
 
-template <typename T, int Z, int NZ, typename ST>
-static void launch_zpass_reg(ST* Bf, const cplx<T>* tens, int nz, int Y, int X, int B, const cplx<T>* tw,
+template <typename T, int Z, int NZ, typename ST, typename GT>
+static void launch_zpass_reg(ST* Bf, const GT* tens, int nz, int Y, int X, int B, const cplx<T>* tw,
                              cudaStream_t st) {
   const size_t sm = (size_t)(Z + 5 * Z * kZregCols) * sizeof(cplx<T>);
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass_reg<T, Z, NZ, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass_reg<T, Z, NZ, ST, GT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sm));
   dim3 grid((unsigned)ceil_div(X, kZregCols), (unsigned)Y);
-  k_zpass_reg<T, Z, NZ, ST><<<grid, 5 * kZregCols, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
+  k_zpass_reg<T, Z, NZ, ST, GT><<<grid, 5 * kZregCols, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
   count_launch();
   VH_CUDA_TRY(cudaGetLastError());
 }
 
 // true when the register z-pass handles this length (Z = 8, 16, 32; nz <= Z / 2 always holds);
 // T is the arithmetic type, ST the storage type of the spectra
-template <typename T, typename ST = cplx<T>>
-static bool zpass_reg(int Z, int nz, ST* Bf, const cplx<T>* tens, int Y, int X, int B, const cplx<T>* tw,
+template <typename T, typename ST = cplx<T>, typename GT = cplx<T>>
+static bool zpass_reg(int Z, int nz, ST* Bf, const GT* tens, int Y, int X, int B, const cplx<T>* tw,
                       cudaStream_t st) {
   int nzb = 2;
   while (nzb < nz) nzb *= 2;
@@ -447,6 +475,42 @@ __global__ void k_tensor_permute(const double2* __restrict__ raw, C* __restrict_
   }
 }
 
+// max |Re| and max |Im| of each of the 7 components of fN_all (column-major 2L,2M,2N,7): out[2k],
+// out[2k+1] as the bit patterns of non-negative doubles (ordered like the values)
+__global__ void k_tensor_reim_max(const double2* __restrict__ raw, int64_t P, unsigned long long* out) {
+  double mr[7] = {0, 0, 0, 0, 0, 0, 0}, mi[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < 7 * P; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / P);
+    const double2 v = raw[idx];
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+      if (q == k) {
+        mr[q] = fmax(mr[q], fabs(v.x));
+        mi[q] = fmax(mi[q], fabs(v.y));
+      }
+  }
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    atomicMax(&out[2 * q], (unsigned long long)__double_as_longlong(mr[q]));
+    atomicMax(&out[2 * q + 1], (unsigned long long)__double_as_longlong(mi[q]));
+  }
+}
+
+// fN_all -> internal [ky][kz][k][kx] layout, divided by X*Y*Z, one float per component: the real
+// part of components 0, 3, 5, 6 and the imaginary part of 1, 2, 4
+__global__ void k_tensor_permute_ri(const double2* __restrict__ raw, float* __restrict__ out, int X, int Y, int Z,
+                                    double s) {
+  const int64_t P = (int64_t)X * Y * Z;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < 7 * P; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int kx = idx % X;
+    const int k = (idx / X) % 7;
+    const int kz = (idx / (7 * (int64_t)X)) % Z;
+    const int ky = idx / (7 * (int64_t)X * Z);
+    const double2 v = raw[kx + (int64_t)X * (ky + (int64_t)Y * (kz + (int64_t)Z * k))];
+    out[idx] = (float)((k == 1 || k == 2 || k == 4 ? v.y : v.x) * s);
+  }
+}
+
 // ------------------------------------------------------------------------------------------
 void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2* fN_all_dev, int64_t nv,
                       const int64_t* idxS_host, bool want32, cudaStream_t st) {
@@ -497,6 +561,31 @@ void conv_plan_create(ConvPlan& p, int L, int M, int N, double dx, const double2
     k_tensor_permute<float2><<<1024, 256, 0, st>>>(fN_all_dev, p.tens32, p.X, p.Y, p.Z, s);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
+    // real/imaginary check of each component over the whole spectrum
+    unsigned long long* d_mx = nullptr;
+    VH_CUDA_TRY(cudaMalloc(&d_mx, 14 * sizeof(unsigned long long)));
+    VH_CUDA_TRY(cudaMemsetAsync(d_mx, 0, 14 * sizeof(unsigned long long), st));
+    k_tensor_reim_max<<<1024, 256, 0, st>>>(fN_all_dev, P, d_mx);
+    count_launch();
+    VH_CUDA_TRY(cudaGetLastError());
+    unsigned long long hmx[14];
+    VH_CUDA_TRY(cudaMemcpyAsync(hmx, d_mx, sizeof(hmx), cudaMemcpyDeviceToHost, st));
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(d_mx);
+    bool ri = true;
+    for (int k = 0; k < 7; ++k) {
+      double re, im;
+      std::memcpy(&re, &hmx[2 * k], sizeof(double));
+      std::memcpy(&im, &hmx[2 * k + 1], sizeof(double));
+      const bool imag_kind = (k == 1 || k == 2 || k == 4);
+      ri = ri && (imag_kind ? re <= 1e-9 * im : im <= 1e-9 * re);
+    }
+    if (ri) {
+      VH_CUDA_TRY(cudaMalloc(&p.tens32ri, 7 * P * sizeof(float)));
+      k_tensor_permute_ri<<<1024, 256, 0, st>>>(fN_all_dev, p.tens32ri, p.X, p.Y, p.Z, s);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+    }
   }
   VH_CUDA_TRY(cudaStreamSynchronize(st));
 }
@@ -526,6 +615,7 @@ void conv_plan_destroy(ConvPlan& p) {
   cudaFree(p.vmap);
   cudaFree(p.tens64);
   cudaFree(p.tens32);
+  cudaFree(p.tens32ri);
   cudaFree(p.tensdf);
   cudaFree(p.twdf);
   for (int a = 0; a < 3; ++a) { cudaFree(p.tw64[a]); cudaFree(p.tw32[a]); }
@@ -595,6 +685,9 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     if (df_z && p.tensdf)
       z_done = zpass_reg<dfloat>(Z, nz, Bf, static_cast<const dcomplex*>(p.tensdf), Y, X, B,
                                  static_cast<const dcomplex*>(p.twdf), st);
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (p.tens32ri) z_done = zpass_reg<float>(Z, nz, Bf, static_cast<const float*>(p.tens32ri), Y, X, B, twp[2], st);
   }
   if (!z_done && !zpass_reg<T>(Z, nz, Bf, tens, Y, X, B, twp[2], st)) {
     const int tx = z_lines_per_cta(Z, X);

@@ -29,6 +29,11 @@ struct ConvPlan {
   // internal tensor spectrum, layout [ky][kz][k][kx], already divided by X*Y*Z
   double2* tens64 = nullptr;
   float2* tens32 = nullptr;
+  // complex64 products with a real/imaginary tensor: every component of the spectrum is real (0, 3,
+  // 5, 6) or imaginary (1, 2, 4) -- the kernel is even or odd along each axis -- so tens32ri holds
+  // one float per component (the real or the imaginary part, layout as tens32); set when the
+  // spectrum was checked to be of that form to within 1e-9 of each component's magnitude
+  float* tens32ri = nullptr;
   void* tensdf = nullptr;     // double-float copy of tens64 (pairs of floats), built on first PREC_DF use
   void* twdf = nullptr;       // double-float z twiddles
   double2* tw64[3] = {nullptr, nullptr, nullptr};
