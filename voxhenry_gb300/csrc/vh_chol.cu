@@ -16,6 +16,8 @@
 // from 3-28 to 7-80+).
 #include <vector>
 
+#include <type_traits>
+
 #include "vh_chol.cuh"
 #include "vh_df.cuh"
 
@@ -535,6 +537,14 @@ constexpr int kBlk = 32;
 // in shared memory with cp.async at the start of the solve (its loads overlap the gather), so the
 // dependent block-by-block reads that follow hit shared memory
 constexpr size_t kStagePanelBytes = 24 * 1024;
+// the pair-precision forward solve holds kSub entries of a factor row in registers at a time, which
+// keeps the unstaged kernel within the register budget of kFsolveCtasPerSm resident CTAs (more
+// warps to hide the load latency); the staged kernel's shared memory allows fewer CTAs anyway
+constexpr int kSub = 16;
+constexpr int kFsolveCtasPerSm = 6;
+// the unstaged pair-precision backward solve: shared memory (vector + 32 x 33 block per warp) of the
+// leaf level's fronts allows five CTAs per SM, and the registers are held to that
+constexpr int kBsolveCtasPerSm = 5;
 
 __device__ __forceinline__ void cp_async8(void* s, const void* g) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
@@ -559,13 +569,14 @@ struct SolveSmem {
 };
 
 template <typename T, bool STAGE>
-__global__ void __launch_bounds__(32 * kSolveWarps, 4)
+__global__ void __launch_bounds__(32 * kSolveWarps, (STAGE || std::is_same<T, double>::value) ? 4 : kFsolveCtasPerSm)
     k_chol_fsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
                   const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, T* const* __restrict__ Wp,
                   cplx<T>* __restrict__ x, int64_t ldx, int64_t xoff, cplx<T>* __restrict__ U, int64_t u_total,
                   int max_nf, int max_panel) {
   using C = cplx<T>;
   using Dot = typename dot_of<T>::type;
+  constexpr int SUB = std::is_same<T, double>::value ? kBlk : kSub;   // row entries held in registers
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t item = (int64_t)blockIdx.x * kSolveWarps + warp;
@@ -626,18 +637,23 @@ __global__ void __launch_bounds__(32 * kSolveWarps, 4)
     // the diagonal block holds L_blk^-1: y_blk = L_blk^-1 t_blk, lane i owns row i (its 32 entries
     // are loaded straight into registers: coalesced across lanes for each k)
     {
-      T lv[kBlk];
-#pragma unroll
-      for (int k = 0; k < kBlk; ++k)
-        lv[k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
       yb[lane] = lane < w ? t[j0 + lane] : czero<C>();   // every lane: yb is read for all 32 k
       __syncwarp();
       Dot tx(T(0)), ty(T(0));
 #pragma unroll
-      for (int k = 0; k < kBlk; ++k) {
-        if (k < w) {
-          tx.add(lv[k], yb[k].x);
-          ty.add(lv[k], yb[k].y);
+      for (int h = 0; h < kBlk; h += SUB) {   // SUB entries of the row in registers at a time
+        if (h >= w) break;
+        T lv[SUB];
+#pragma unroll
+        for (int k = 0; k < SUB; ++k) {
+          const int kk = h + k;
+          lv[k] = (kk < w && lane < w && lane >= kk) ? F[(j0 + lane) + (int64_t)(j0 + kk) * nf] : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < SUB; ++k) {
+          if (h + k >= w) break;
+          tx.add(lv[k], yb[h + k].x);
+          ty.add(lv[k], yb[h + k].y);
         }
       }
       C tv;
@@ -650,14 +666,19 @@ __global__ void __launch_bounds__(32 * kSolveWarps, 4)
     __syncwarp();
     for (int r = j0 + w + lane; r < nf; r += 32) {
       const T* Lr = F + r + (int64_t)j0 * nf;
-      T lv[kBlk];
-#pragma unroll
-      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : T(0);   // independent loads
       Dot ax(t[r].x), ay(t[r].y);   // t_r - sum_k L(r, k) y_k
 #pragma unroll
-      for (int k = 0; k < kBlk; ++k) {
-        ax.add(-lv[k], yb[k].x);
-        ay.add(-lv[k], yb[k].y);
+      for (int h = 0; h < kBlk; h += SUB) {
+        if (h >= w) break;   // a partial block stops at w (warp-uniform); zero terms add nothing
+        T lv[SUB];
+#pragma unroll
+        for (int k = 0; k < SUB; ++k) lv[k] = h + k < w ? Lr[(int64_t)(h + k) * nf] : T(0);   // independent loads
+#pragma unroll
+        for (int k = 0; k < SUB; ++k) {
+          if (SUB < kBlk && h + k >= w) break;   // (FP64: one full-width pass, no early exit)
+          ax.add(-lv[k], yb[h + k].x);
+          ay.add(-lv[k], yb[h + k].y);
+        }
       }
       t[r].x = ax.value();
       t[r].y = ay.value();
@@ -674,8 +695,34 @@ __global__ void __launch_bounds__(32 * kSolveWarps, 4)
   }
 }
 
+// Lb[c][r] = L(r0 + r, c0 + c) for r < wr, c < wc of a column-major panel with leading dimension
+// nf: lane r loads row r0 + r, one load per column (each coalesced across the lanes), and stores it
+// down a column of the padded block, so that lane c can then read column c0 + c without conflicts.
+template <typename T>
+__device__ __forceinline__ void tile_to_smem(const T* F, int nf, int r0, int c0, int wr, int wc, T (*Lb)[kBlk + 1],
+                                             int lane) {
+  if (lane < wr) {
+    const T* p = F + (r0 + lane) + (int64_t)c0 * nf;
+#pragma unroll
+    for (int h = 0; h < kBlk; h += 16) {   // 16 independent loads in flight per lane
+      if (h >= wc) break;
+      T v[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        if (h + c >= wc) break;
+        v[c] = p[(int64_t)(h + c) * nf];
+      }
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        if (h + c >= wc) break;
+        Lb[h + c][lane] = v[c];
+      }
+    }
+  }
+}
+
 template <typename T, bool STAGE>
-__global__ void __launch_bounds__(32 * kSolveWarps)
+__global__ void __launch_bounds__(32 * kSolveWarps, (STAGE || std::is_same<T, double>::value) ? 1 : kBsolveCtasPerSm)
     k_chol_bsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
                   const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x, int64_t ldx,
                   int64_t xoff, int max_nf, double2* __restrict__ xd, int64_t ldxd, int max_panel) {
@@ -714,29 +761,30 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     __syncwarp();
     F = panel;
   }
-  // z_own -= L21^T x_bnd, column-oriented: lane j walks its own column (contiguous rows, no
-  // cross-lane reductions)
-  for (int j = lane; j < ns; j += 32) {
-    const T* col = F + (int64_t)j * nf;
-    Dot sx(t[j].x), sy(t[j].y);   // z_j - sum_r L(r, j) x_r
-    int r = ns;
-    for (; r + 4 <= nf; r += 4) {
-      T lv[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) lv[u] = col[r + u];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        sx.add(-lv[u], t[r + u].x);
-        sy.add(-lv[u], t[r + u].y);
+  // z_own -= L21^T x_bnd: lane j accumulates column c0 + j over the boundary rows in order.  Each
+  // 32 x 32 tile of L21 is read coalesced (lane = row, one load per column) into the padded block
+  // Lb and read back transposed, so no lane walks a column of the column-major panel alone.
+  for (int c0 = 0; c0 < ns; c0 += kBlk) {
+    const int wc = min(kBlk, ns - c0);
+    const C z0 = lane < wc ? t[c0 + lane] : czero<C>();
+    Dot sx(z0.x), sy(z0.y);   // z_j - sum_r L(r, j) x_r
+    for (int r0 = ns; r0 < nf; r0 += kBlk) {
+      const int wr = min(kBlk, nf - r0);
+      tile_to_smem<T>(F, nf, r0, c0, wr, wc, Lb, lane);
+      __syncwarp();
+#pragma unroll 8
+      for (int k = 0; k < wr; ++k) {
+        const T l = Lb[lane][k];
+        const C xr = t[r0 + k];
+        sx.add(-l, xr.x);
+        sy.add(-l, xr.y);
       }
+      __syncwarp();
     }
-    for (; r < nf; ++r) {
-      const T l = col[r];
-      sx.add(-l, t[r].x);
-      sy.add(-l, t[r].y);
+    if (lane < wc) {
+      t[c0 + lane].x = sx.value();
+      t[c0 + lane].y = sy.value();
     }
-    t[j].x = sx.value();
-    t[j].y = sy.value();
   }
   __syncwarp();
   const int nblk = (ns + kBlk - 1) / kBlk;
@@ -764,22 +812,23 @@ __global__ void __launch_bounds__(32 * kSolveWarps)
     __syncwarp();
     if (lane < w) t[j0 + lane] = xv;
     __syncwarp();
-    // z_j -= sum_{r in block} L(r, j) x_r for the own columns j < j0 (lane per column)
-    for (int j = lane; j < j0; j += 32) {
-      const T* col = F + (int64_t)j * nf + j0;
-      T lv[kBlk];
-#pragma unroll
-      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? col[k] : T(0);
-      Dot sx(t[j].x), sy(t[j].y);
-#pragma unroll
-      for (int k = 0; k < kBlk; ++k) {
-        if (k < w) {
-          sx.add(-lv[k], t[j0 + k].x);
-          sy.add(-lv[k], t[j0 + k].y);
-        }
+    // z_j -= sum_{r in block} L(r, j) x_r for the own columns j < j0 (lane per column, the block's
+    // rows read as transposed tiles like the boundary rows above)
+    for (int c0 = 0; c0 < j0; c0 += kBlk) {
+      tile_to_smem<T>(F, nf, j0, c0, w, kBlk, Lb, lane);
+      __syncwarp();
+      const C zj = t[c0 + lane];
+      Dot sx(zj.x), sy(zj.y);
+#pragma unroll 8
+      for (int k = 0; k < w; ++k) {
+        const T l = Lb[lane][k];
+        const C xr = t[j0 + k];
+        sx.add(-l, xr.x);
+        sy.add(-l, xr.y);
       }
-      t[j].x = sx.value();
-      t[j].y = sy.value();
+      __syncwarp();
+      t[c0 + lane].x = sx.value();
+      t[c0 + lane].y = sy.value();
     }
     __syncwarp();
   }
