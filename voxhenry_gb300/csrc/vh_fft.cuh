@@ -179,10 +179,78 @@ __device__ __forceinline__ void fft_stage(const C* __restrict__ src, C* __restri
   }
 }
 
+// ---- the same stages for a power-of-two length fixed at compile time: the index arithmetic is
+// shifts and masks, and the twiddle strides and the radix sequence (radix 8 while it divides, then
+// one radix 4 or 2, the order fft_factor gives) are constants.  Every stage does the arithmetic of
+// the runtime stage above, so the results are identical.
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+template <int R, int N, int NS, int DIR, typename C>
+__device__ __forceinline__ void fft_stage_p2(const C* __restrict__ src, C* __restrict__ dst, const C* __restrict__ tw,
+                                             int es, int ls, int nlines, int lognl, bool jfast) {
+  constexpr int nb = N / R;
+  constexpr int lognb = ilog2c(nb);
+  constexpr int logns = ilog2c(NS);
+  constexpr int twmul = N / (NS * R);
+  const int total = nb * nlines;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int line, j;
+    if (jfast) { j = t & (nb - 1); line = t >> lognb; } else { line = t & (nlines - 1); j = t >> lognl; }
+    const int k = j & (NS - 1);
+    const int base = line * ls;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[base + (j + r * nb) * es];
+    if constexpr (NS > 1) {
+      const int step = k * twmul;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = tw[r * step];
+        v[r] = (DIR < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+      }
+    }
+    if constexpr (R == 2) dft2<DIR>(v[0], v[1]);
+    else if constexpr (R == 4) dft4<DIR>(v);
+    else dft8<DIR>(v);
+    const int d0 = ((j >> logns) << (logns + ilog2c(R))) + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[base + (d0 + r * NS) * es] = v[r];
+  }
+}
+
+template <int N, int NS, int DIR, typename C>
+__device__ __forceinline__ C* fft_stages_p2(C* src, C* dst, const C* tw, int es, int ls, int nlines, int lognl,
+                                            bool jfast) {
+  if constexpr (NS >= N) {
+    return src;
+  } else {
+    constexpr int rem = N / NS;
+    constexpr int R = rem % 8 == 0 ? 8 : (rem % 4 == 0 ? 4 : 2);
+    fft_stage_p2<R, N, NS, DIR>(src, dst, tw, es, ls, nlines, lognl, jfast);
+    __syncthreads();
+    return fft_stages_p2<N, NS * R, DIR>(dst, src, tw, es, ls, nlines, lognl, jfast);
+  }
+}
+
 // Runs all stages; returns the buffer holding the result (buf0 or buf1).
 // Must be called by all threads of the CTA; ends with a __syncthreads().
 template <int DIR, typename C>
 __device__ C* fft_lines(C* buf0, C* buf1, const C* tw, const FftDesc& d, int es, int ls, int nlines, bool jfast) {
+  // power-of-two lengths 16..2048 (and, for the line-interleaved layout, a power-of-two line
+  // count) take the compile-time stages
+  if ((d.n & (d.n - 1)) == 0 && d.n >= 16 && d.n <= 2048 && (jfast || (nlines & (nlines - 1)) == 0)) {
+    const int lognl = jfast ? 0 : __ffs(nlines) - 1;
+    switch (__ffs(d.n) - 1) {
+      case 4: return fft_stages_p2<16, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+      case 5: return fft_stages_p2<32, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+      case 6: return fft_stages_p2<64, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+      case 7: return fft_stages_p2<128, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+      case 8: return fft_stages_p2<256, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+      case 9: return fft_stages_p2<512, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+      case 10: return fft_stages_p2<1024, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+      default: return fft_stages_p2<2048, 1, DIR>(buf0, buf1, tw, es, ls, nlines, lognl, jfast);
+    }
+  }
   C* src = buf0;
   C* dst = buf1;
   int Ns = 1;
