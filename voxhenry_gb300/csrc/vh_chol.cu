@@ -857,7 +857,21 @@ struct WideSmem {
   }
 };
 
+// The wide kernels stage the front's panel (its ns columns, rows 0..nf-1) in shared memory when it
+// fits (STAGE): every column is copied with cp.async at the start, overlapping the gathers, so the
+// block-by-block chain that follows reads shared memory instead of making two dependent global
+// round trips per 32-column block.  The staged panel's leading dimension is odd, so that lanes
+// walking columns (the backward updates) hit distinct banks.
+constexpr size_t kWideStageMax = 220 * 1024;   // shared memory of a staged wide CTA
+__host__ __device__ __forceinline__ int staged_ld(int nf) { return nf | 1; }
+
 template <typename T>
+__device__ __forceinline__ void stage_panel(T* panel, const T* F, int nf, int ns, int ldp, int warp, int lane) {
+  for (int c = warp; c < ns; c += kWideWarps)
+    for (int r = lane; r < nf; r += 32) cp_async8(panel + r + (int64_t)c * ldp, F + r + (int64_t)c * nf);
+}
+
+template <typename T, bool STAGE>
 __global__ void __launch_bounds__(32 * kWideWarps)
     k_chol_fsolve_wide(const int32_t* __restrict__ lev, int nlev, const FrontInfo* __restrict__ fr,
                        const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, T* const* __restrict__ Wp,
@@ -869,6 +883,7 @@ __global__ void __launch_bounds__(32 * kWideWarps)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* t = reinterpret_cast<C*>(smem_raw);
   C* yb = reinterpret_cast<C*>(smem_raw + WideSmem<T>::vec_bytes(max_nf));
+  T* panel = reinterpret_cast<T*>(smem_raw + WideSmem<T>::bytes(max_nf));
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const FrontInfo f = fr[lev[blockIdx.x % nlev]];
   const int b = (int)(blockIdx.x / nlev);
@@ -877,6 +892,8 @@ __global__ void __launch_bounds__(32 * kWideWarps)
   C* Ub = U + b * u_total;
   const int32_t* rw = rows + f.rows_off;
   const int nf = f.nf, ns = f.ns;
+  int ld = nf;
+  if constexpr (STAGE) stage_panel(panel, F, nf, ns, staged_ld(nf), warp, lane);
   for (int r = tid; r < nf; r += NT) t[r] = r < ns ? xb[rw[r]] : czero<C>();
   __syncthreads();
   for (int c = 0; c < 2; ++c) {
@@ -891,13 +908,19 @@ __global__ void __launch_bounds__(32 * kWideWarps)
     }
     __syncthreads();
   }
+  if constexpr (STAGE) {
+    cp_async_commit_wait();
+    __syncthreads();
+    F = panel;
+    ld = staged_ld(nf);
+  }
   for (int j0 = 0; j0 < ns; j0 += kBlk) {
     const int w = min(kBlk, ns - j0);
     if (warp == 0) {   // y_blk = L_blk^-1 t_blk (stored inverse), lane i owns row i
       T lv[kBlk];
 #pragma unroll
       for (int k = 0; k < kBlk; ++k)
-        lv[k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
+        lv[k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * ld] : T(0);
       yb[lane] = lane < w ? t[j0 + lane] : czero<C>();
       __syncwarp();
       Dot tx(T(0)), ty(T(0));
@@ -916,10 +939,10 @@ __global__ void __launch_bounds__(32 * kWideWarps)
     }
     __syncthreads();
     for (int r = j0 + w + tid; r < nf; r += NT) {
-      const T* Lr = F + r + (int64_t)j0 * nf;
+      const T* Lr = F + r + (int64_t)j0 * ld;
       T lv[kBlk];
 #pragma unroll
-      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : T(0);
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * ld] : T(0);
       Dot ax(t[r].x), ay(t[r].y);
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) {
@@ -941,7 +964,7 @@ __global__ void __launch_bounds__(32 * kWideWarps)
   }
 }
 
-template <typename T>
+template <typename T, bool STAGE>
 __global__ void __launch_bounds__(32 * kWideWarps)
     k_chol_bsolve_wide(const int32_t* __restrict__ lev, int nlev, const FrontInfo* __restrict__ fr,
                        const int32_t* __restrict__ rows, T* const* __restrict__ Wp, cplx<T>* __restrict__ x,
@@ -952,6 +975,7 @@ __global__ void __launch_bounds__(32 * kWideWarps)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* t = reinterpret_cast<C*>(smem_raw);
   T(*Lb)[kBlk + 1] = reinterpret_cast<T(*)[kBlk + 1]>(smem_raw + WideSmem<T>::vec_bytes(max_nf));
+  T* panel = reinterpret_cast<T*>(smem_raw + WideSmem<T>::bytes(max_nf));
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const FrontInfo f = fr[lev[blockIdx.x % nlev]];
   const int b = (int)(blockIdx.x / nlev);
@@ -959,11 +983,18 @@ __global__ void __launch_bounds__(32 * kWideWarps)
   C* xb = x + b * ldx + xoff;
   const int32_t* rw = rows + f.rows_off;
   const int nf = f.nf, ns = f.ns;
+  int ld = nf;
+  if constexpr (STAGE) stage_panel(panel, F, nf, ns, staged_ld(nf), warp, lane);
   for (int r = tid; r < nf; r += NT) t[r] = xb[rw[r]];
+  if constexpr (STAGE) {
+    cp_async_commit_wait();
+    F = panel;
+    ld = staged_ld(nf);
+  }
   __syncthreads();
   // z_j -= sum_{r >= ns} L(r, j) x_r: warp per column, lanes over the rows, then a shuffle sum
   for (int j = warp; j < ns; j += kWideWarps) {
-    const T* col = F + (int64_t)j * nf;
+    const T* col = F + (int64_t)j * ld;
     Dot sx(T(0)), sy(T(0));
     for (int r = ns + lane; r < nf; r += 32) {
       const T l = col[r];
@@ -988,7 +1019,7 @@ __global__ void __launch_bounds__(32 * kWideWarps)
     if (warp == 0) {   // x_blk = L_blk^-T z_blk: lane i: x_i = sum_{k >= i} Linv(k, i) z_k
 #pragma unroll
       for (int k = 0; k < kBlk; ++k)
-        Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
+        Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * ld] : T(0);
       __syncwarp();
       Dot xx(T(0)), xy(T(0));
 #pragma unroll
@@ -1007,7 +1038,7 @@ __global__ void __launch_bounds__(32 * kWideWarps)
     }
     __syncthreads();
     for (int j = tid; j < j0; j += NT) {   // z_j -= sum_{k in block} L(j0 + k, j) x_{j0 + k}
-      const T* col = F + (int64_t)j * nf + j0;
+      const T* col = F + (int64_t)j * ld + j0;
       T lv[kBlk];
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? col[k] : T(0);
@@ -1046,30 +1077,46 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
   auto wide = [&](size_t h) {
     return (int)s.levels[h].size() <= kWideMaxFronts || warp_smem(h, false) > kWarpSolveSmemMax;
   };
-  size_t sm_f[2] = {0, 0}, sm_b[2] = {0, 0}, sm_w = 0;
+  // a wide level stages its panels when the largest (max ns columns of odd leading dimension) fits
+  auto wide_smem = [&](size_t h, bool staged) {
+    const size_t base = WideSmem<T>::bytes(s.level_max_nf[h]);
+    return staged ? base + (size_t)s.level_max_ns[h] * staged_ld(s.level_max_nf[h]) * sizeof(T) : base;
+  };
+  auto wide_stage = [&](size_t h) { return wide_smem(h, true) <= kWideStageMax; };
+  size_t sm_f[2] = {0, 0}, sm_b[2] = {0, 0}, sm_w[2] = {0, 0};
   for (size_t h = 0; h < s.levels.size(); ++h) {
     if (wide(h)) {
-      sm_w = std::max(sm_w, WideSmem<T>::bytes(s.level_max_nf[h]));
+      const bool ws = wide_stage(h);
+      sm_w[ws] = std::max(sm_w[ws], wide_smem(h, ws));
     } else {
       sm_f[stage(h)] = std::max(sm_f[stage(h)], warp_smem(h, true));
       sm_b[stage(h)] = std::max(sm_b[stage(h)], warp_smem(h, false));
     }
   }
-  VH_REQUIRE(sm_w <= 220 * 1024, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
+  VH_REQUIRE(sm_w[0] <= kWideStageMax, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
   if (sm_f[0]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_f[0]));
   if (sm_f[1]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_f[1]));
   if (sm_b[0]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b[0]));
   if (sm_b[1]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b[1]));
-  if (sm_w) {
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w));
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w));
+  if (sm_w[0]) {
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[0]));
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[0]));
+  }
+  if (sm_w[1]) {
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[1]));
+    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[1]));
   }
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();
     const int mnf = s.level_max_nf[h];
     if (wide(h)) {
-      k_chol_fsolve_wide<T><<<(unsigned)(nlev * B), 32 * kWideWarps, WideSmem<T>::bytes(mnf), st>>>(
-          s.d_levels[h], nlev, s.d_fronts, s.d_rows, s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf);
+      const unsigned g = (unsigned)(nlev * B);
+      if (wide_stage(h))
+        k_chol_fsolve_wide<T, true><<<g, 32 * kWideWarps, wide_smem(h, true), st>>>(
+            s.d_levels[h], nlev, s.d_fronts, s.d_rows, s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf);
+      else
+        k_chol_fsolve_wide<T, false><<<g, 32 * kWideWarps, wide_smem(h, false), st>>>(
+            s.d_levels[h], nlev, s.d_fronts, s.d_rows, s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf);
       count_launch();
       VH_CUDA_TRY(cudaGetLastError());
       continue;
@@ -1091,8 +1138,13 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
     const int nlev = (int)s.levels[hh].size();
     const int mnf = s.level_max_nf[hh];
     if (wide(hh)) {
-      k_chol_bsolve_wide<T><<<(unsigned)(nlev * B), 32 * kWideWarps, WideSmem<T>::bytes(mnf), st>>>(
-          s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf, xd, ldxd);
+      const unsigned g = (unsigned)(nlev * B);
+      if (wide_stage(hh))
+        k_chol_bsolve_wide<T, true><<<g, 32 * kWideWarps, wide_smem(hh, true), st>>>(
+            s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf, xd, ldxd);
+      else
+        k_chol_bsolve_wide<T, false><<<g, 32 * kWideWarps, wide_smem(hh, false), st>>>(
+            s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf, xd, ldxd);
       count_launch();
       VH_CUDA_TRY(cudaGetLastError());
       continue;

@@ -116,7 +116,67 @@ static int z_lines_per_cta(int Z, int X) {
 }
 
 // ------------------------------------------------------------------------------------------
+// The x and y passes run with kPassThreads threads.  Their transforms take the fully static stages
+// for the usual power-of-two lengths with the line counts x_lines_per_cta / y_lines_per_cta give
+// them, else the runtime stages.
+constexpr int kPassThreads = 256;
+
+template <int DIR, typename C>
+__device__ __forceinline__ C* fft_x_lines(C* b0, C* b1, const C* tw, const FftDesc& fd, int nl) {
+  if (blockDim.x == kPassThreads) {
+    if (fd.n == 256 && nl == 8) return fft_stages_fixed<256, 1, 8, true, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 512 && nl == 4) return fft_stages_fixed<512, 1, 4, true, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 1024 && nl == 2) return fft_stages_fixed<1024, 1, 2, true, DIR, kPassThreads>(b0, b1, tw);
+  }
+  return fft_lines<DIR>(b0, b1, tw, fd, 1, fd.n, nl, true);
+}
+
+template <int DIR, typename C>
+__device__ __forceinline__ C* fft_y_lines(C* b0, C* b1, const C* tw, const FftDesc& fd, int tx) {
+  if (blockDim.x == kPassThreads) {
+    if (fd.n == 256 && tx == 8) return fft_stages_fixed<256, 1, 8, false, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 256 && tx == 4) return fft_stages_fixed<256, 1, 4, false, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 512 && tx == 8) return fft_stages_fixed<512, 1, 8, false, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 512 && tx == 4) return fft_stages_fixed<512, 1, 4, false, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 1024 && tx == 4) return fft_stages_fixed<1024, 1, 4, false, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 1024 && tx == 2) return fft_stages_fixed<1024, 1, 2, false, DIR, kPassThreads>(b0, b1, tw);
+  }
+  return fft_lines<DIR>(b0, b1, tw, fd, tx, 1, tx, false);
+}
+
 // pass 1: fwd-x.  CTA handles `nl` consecutive lines (y fastest, then z, c, b), line-major smem.
+// Each line's voxel-map row and vector offset are decoded once per CTA (XLine, after b1).
+struct XLine {
+  int64_t vbase;   // vmap offset of the line's (y, z) row; -1 past the last line
+  int64_t xoff;    // b * ld + c * nv
+  int32_t b, c;
+};
+
+__device__ __forceinline__ void decode_lines(XLine* li, int64_t l0, int nl, int64_t nlines_total, int L, int M,
+                                             int y0, int ny, int z0, int nz, int64_t ld, int64_t nv) {
+  for (int line = threadIdx.x; line < nl; line += blockDim.x) {
+    const int64_t gl = l0 + line;
+    XLine q;
+    q.vbase = -1;
+    q.xoff = 0;
+    q.b = q.c = 0;
+    if (gl < nlines_total) {
+      const int64_t y = y0 + gl % ny;
+      const int64_t z = z0 + (gl / ny) % nz;
+      const int64_t c = (gl / ((int64_t)ny * nz)) % 5;
+      const int64_t b = gl / ((int64_t)ny * nz * 5);
+      q.vbase = (int64_t)L * (y + (int64_t)M * z);
+      q.xoff = b * ld + c * nv;
+      q.b = (int32_t)b;
+      q.c = (int32_t)c;
+    }
+    li[line] = q;
+  }
+}
+
+// t / n for the element loops (a shift when n is a power of two)
+__device__ __forceinline__ int div_line(int t, int n, bool p2, int ln) { return p2 ? t >> ln : t / n; }
+
 template <typename T>
 __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int32_t* __restrict__ vmap, int L, int M,
                         int y0, int ny, int z0, int nz, int64_t nv, int64_t nlines_total, cplx<T>* __restrict__ A,
@@ -127,39 +187,54 @@ __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int3
   C* tw = reinterpret_cast<C*>(smem_raw);
   C* b0 = tw + X;
   C* b1 = b0 + X * nl;
+  XLine* li = reinterpret_cast<XLine*>(b1 + X * nl);
   for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
   const int64_t l0 = (int64_t)blockIdx.x * nl;
-  const int tot = X * nl;
-  for (int t0 = threadIdx.x; t0 < tot; t0 += 4 * blockDim.x) {
+  decode_lines(li, l0, nl, nlines_total, L, M, y0, ny, z0, nz, ldx, nv);
+  __syncthreads();
+  // the zero half of each line (i >= L), then the gather of i < L: every thread runs the same
+  // number of gather rounds, so that a warp none of whose elements is a voxel skips the loads and
+  // the complex128 -> complex64 conversions (FP64-pipe work on GB300) as a whole
+  const int XL = X - L;
+  for (int t = threadIdx.x; t < XL * nl; t += blockDim.x) {
+    const int line = t / XL;
+    b0[line * X + L + (t - line * XL)] = czero<C>();
+  }
+  const bool p2 = (L & (L - 1)) == 0;
+  const int ll = __ffs(L) - 1;
+  const int tot = L * nl;
+  for (int base = 0; base < tot; base += 4 * blockDim.x) {
     int32_t vid[4];
     int64_t off[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {     // independent voxel-map loads
-      const int t = t0 + u * blockDim.x;
-      const int line = t / X, i = t - (t / X) * X;
-      const int64_t gl = l0 + line;
+      const int t = base + threadIdx.x + u * blockDim.x;
       vid[u] = -1;
       off[u] = 0;
-      if (t < tot && gl < nlines_total && i < L) {
-        const int64_t y = y0 + gl % ny;
-        const int64_t z = z0 + (gl / ny) % nz;
-        const int64_t c = (gl / ((int64_t)ny * nz)) % 5;
-        const int64_t b = gl / ((int64_t)ny * nz * 5);
-        vid[u] = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
-        off[u] = b * ldx + c * nv;
+      if (t < tot) {
+        const int line = div_line(t, L, p2, ll), i = t - line * L;
+        const XLine q = li[line];
+        if (q.vbase >= 0) {
+          vid[u] = vmap[i + q.vbase];
+          off[u] = q.xoff;
+        }
       }
     }
-    C v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = vid[u] >= 0 ? to_c(xin[off[u] + vid[u]], C()) : czero<C>();
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int t = t0 + u * blockDim.x;
-      if (t < tot) b0[t] = v[u];
+      const int t = base + threadIdx.x + u * blockDim.x;
+      C v = czero<C>();
+      if (__any_sync(0xffffffffu, vid[u] >= 0)) {
+        if (vid[u] >= 0) v = to_c(xin[off[u] + vid[u]], C());
+      }
+      if (t < tot) {
+        const int line = div_line(t, L, p2, ll);
+        b0[line * X + (t - line * L)] = v;
+      }
     }
   }
   __syncthreads();
-  C* r = fft_lines<-1>(b0, b1, tw, fd, 1, X, nl, true);
+  C* r = fft_x_lines<-1>(b0, b1, tw, fd, nl);
   const int rows = (nlines_total - l0 < nl) ? (int)(nlines_total - l0) : nl;
   tile_store(A + l0 * X, X, r, X, rows, X);
 }
@@ -187,7 +262,7 @@ __global__ void k_pass_y(const cplx<T>* __restrict__ src, int src_rows, int nin,
   tile_load(b0 + in_off * tx, tx, s + kx0, X, Y - in_off, nin, tx, cv);
   cp_async_wait_all();
   __syncthreads();
-  C* r = fft_lines<DIR>(b0, b1, tw, fd, tx, 1, tx, false);
+  C* r = fft_y_lines<DIR>(b0, b1, tw, fd, tx);
   tile_store(d + kx0, X, r + out_off * tx, tx, nout, cv);
 }
 
@@ -432,31 +507,48 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
   C* tw = reinterpret_cast<C*>(smem_raw);
   C* b0 = tw + X;
   C* b1 = b0 + X * nl;
+  XLine* li = reinterpret_cast<XLine*>(b1 + X * nl);
   for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
   const int64_t l0 = (int64_t)blockIdx.x * nl;
   const int rows_valid = (nlines_total - l0 < nl) ? (int)(nlines_total - l0) : nl;
+  float2* sline = reinterpret_cast<float2*>(li + nl);   // the line's RHS scale in FP32 (complex64 product)
+  decode_lines(li, l0, nl, nlines_total, L, M, y0, ny, z0, nz, ldx, nv);
+  if constexpr (sizeof(T) == 4) {
+    for (int line = threadIdx.x; line < nl; line += blockDim.x) sline[line] = to_c(scale[li[line].b], float2());
+  }
   tile_load(b0, X, A + l0 * X, X, nl, rows_valid, X, X);
   cp_async_wait_all();
   __syncthreads();
-  C* r = fft_lines<+1>(b0, b1, tw, fd, 1, X, nl, true);
+  C* r = fft_x_lines<+1>(b0, b1, tw, fd, nl);
+  const bool p2 = (L & (L - 1)) == 0;
+  const int ll = __ffs(L) - 1;
   for (int t = threadIdx.x; t < L * nl; t += blockDim.x) {
-    const int line = t / L, i = t % L;
-    const int64_t gl = l0 + line;
-    if (gl >= nlines_total) continue;
-    const int64_t y = y0 + gl % ny;
-    const int64_t z = z0 + (gl / ny) % nz;
-    const int64_t c = (gl / ((int64_t)ny * nz)) % 5;
-    const int64_t b = gl / ((int64_t)ny * nz * 5);
-    const int32_t vid = vmap[i + (int64_t)L * (y + (int64_t)M * z)];
+    const int line = div_line(t, L, p2, ll), i = t - line * L;
+    const XLine q = li[line];
+    if (q.vbase < 0) continue;
+    const int64_t b = q.b, c = q.c;
+    const int32_t vid = vmap[i + q.vbase];
     if (vid < 0) continue;
-    const double2 conv = to_d(r[line * X + i]);
-    const double2 s = scale[b];
     const double2 zz = zdiag[b * zstride + vid];
     const double2 xj = xin[b * ldx + c * nv + vid];
     const double ck = (c < 3 ? 1.0 : (c == 3 ? 1.0 / 6.0 : 0.5)) * inv_dx;
-    double2 out = cmul(s, conv);
-    out = cadd(out, cscale(cmul(zz, xj), ck));
-    yout[b * ldy + c * nv + vid] = out;
+    if constexpr (sizeof(T) == 4) {
+      // complex64 product: the diagonal term in FP32 too (rounding ~1e-7, below the complex64
+      // transform's own error), which keeps GB300's FP64 pipe to the conversions
+      const float2 conv = r[line * X + i];
+      const float2 sf = sline[line], zf = to_c(zz, float2()), xf = to_c(xj, float2());
+      const float2 d = cmul(zf, xf);
+      const float ckf = (float)ck;
+      float2 o = cmul(sf, conv);
+      o.x = fmaf(ckf, d.x, o.x);
+      o.y = fmaf(ckf, d.y, o.y);
+      yout[b * ldy + c * nv + vid] = make_double2((double)o.x, (double)o.y);
+    } else {
+      const double2 conv = to_d(r[line * X + i]);
+      double2 out = cmul(scale[b], conv);
+      out = cadd(out, cscale(cmul(zz, xj), ck));
+      yout[b * ldy + c * nv + vid] = out;
+    }
   }
 }
 
@@ -662,10 +754,10 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
     const int64_t lines = (int64_t)ny * nz * 5 * B;
-    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C);
+    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C) + nl * sizeof(XLine);
     const unsigned grid = (unsigned)ceil_div(lines, nl);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_fwd_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_fwd_x<T><<<grid, 256, sm, st>>>(x, ldx, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, A, p.fx, twp[0], nl);
+    k_fwd_x<T><<<grid, kPassThreads, sm, st>>>(x, ldx, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, A, p.fx, twp[0], nl);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -675,7 +767,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
     VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_pass_y<T, -1><<<grid, 256, sm, st>>>(A, ny, ny, Bf, Y, Y, X, p.fy, twp[1], tx, y0, 0);
+    k_pass_y<T, -1><<<grid, kPassThreads, sm, st>>>(A, ny, ny, Bf, Y, Y, X, p.fy, twp[1], tx, y0, 0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -704,7 +796,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
     VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_pass_y<T, +1><<<grid, 256, sm, st>>>(Bf, Y, Y, A, ny, ny, X, p.fy, twp[1], tx, 0, y0);
+    k_pass_y<T, +1><<<grid, kPassThreads, sm, st>>>(Bf, Y, Y, A, ny, ny, X, p.fy, twp[1], tx, 0, y0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
   }
@@ -712,10 +804,10 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
     const int64_t lines = (int64_t)ny * nz * 5 * B;
-    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C);
+    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C) + nl * (sizeof(XLine) + sizeof(float2));
     const unsigned grid = (unsigned)ceil_div(lines, nl);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_inv_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_inv_x<T><<<grid, 256, sm, st>>>(A, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, x, ldx, y, ldy, scale, zdiag,
+    k_inv_x<T><<<grid, kPassThreads, sm, st>>>(A, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, x, ldx, y, ldy, scale, zdiag,
                                       zstride, 1.0 / p.dx, p.fx, twp[0], nl);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
@@ -800,7 +892,7 @@ void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaSt
     const size_t sm = (size_t)(n + 2 * n * tx) * sizeof(double2);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_fft_axis_inplace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     dim3 grid((unsigned)ceil_div(inner, tx), (unsigned)planes);
-    k_fft_axis_inplace<<<grid, 256, sm, st>>>(data, inner, fd, tw, tx, contiguous);
+    k_fft_axis_inplace<<<grid, kPassThreads, sm, st>>>(data, inner, fd, tw, tx, contiguous);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     VH_CUDA_TRY(cudaStreamSynchronize(st));

@@ -232,6 +232,59 @@ __device__ __forceinline__ C* fft_stages_p2(C* src, C* dst, const C* tw, int es,
   }
 }
 
+// ---- fully static stages: length N, NL lines, layout (JF: line-major, element stride 1 and line
+// stride N; else line-interleaved, element stride NL and line stride 1) and NT threads fixed at
+// compile time, so each stage is a fixed number of unrolled rounds without bound checks.  The
+// arithmetic is that of the stages above.
+template <int R, int N, int NS, int NL, bool JF, int DIR, int NT, typename C>
+__device__ __forceinline__ void fft_stage_fixed(const C* __restrict__ src, C* __restrict__ dst, const C* __restrict__ tw) {
+  constexpr int nb = N / R;
+  constexpr int total = nb * NL;
+  constexpr int ES = JF ? 1 : NL, LS = JF ? N : 1;
+  constexpr int lognb = ilog2c(nb), lognl = ilog2c(NL), logns = ilog2c(NS);
+  constexpr int twmul = N / (NS * R);
+  static_assert(JF || (NL & (NL - 1)) == 0, "interleaved lines: power-of-two count");
+#pragma unroll
+  for (int t0 = 0; t0 < total; t0 += NT) {
+    const int t = t0 + (int)threadIdx.x;
+    if (total % NT != 0 && t >= total) break;
+    int line, j;
+    if constexpr (JF) { j = t & (nb - 1); line = t >> lognb; } else { line = t & (NL - 1); j = t >> lognl; }
+    const int k = j & (NS - 1);
+    const int base = line * LS;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[base + (j + r * nb) * ES];
+    if constexpr (NS > 1) {
+      const int step = k * twmul;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = tw[r * step];
+        v[r] = (DIR < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+      }
+    }
+    if constexpr (R == 2) dft2<DIR>(v[0], v[1]);
+    else if constexpr (R == 4) dft4<DIR>(v);
+    else dft8<DIR>(v);
+    const int d0 = ((j >> logns) << (logns + ilog2c(R))) + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[base + (d0 + r * NS) * ES] = v[r];
+  }
+}
+
+template <int N, int NS, int NL, bool JF, int DIR, int NT, typename C>
+__device__ __forceinline__ C* fft_stages_fixed(C* src, C* dst, const C* tw) {
+  if constexpr (NS >= N) {
+    return src;
+  } else {
+    constexpr int rem = N / NS;
+    constexpr int R = rem % 8 == 0 ? 8 : (rem % 4 == 0 ? 4 : 2);
+    fft_stage_fixed<R, N, NS, NL, JF, DIR, NT>(src, dst, tw);
+    __syncthreads();
+    return fft_stages_fixed<N, NS * R, NL, JF, DIR, NT>(dst, src, tw);
+  }
+}
+
 // Runs all stages; returns the buffer holding the result (buf0 or buf1).
 // Must be called by all threads of the CTA; ends with a __syncthreads().
 template <int DIR, typename C>
