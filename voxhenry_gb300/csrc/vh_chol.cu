@@ -461,6 +461,47 @@ static void launch_front(int max_nf, const int32_t* lev, unsigned count, unsigne
   }
 }
 
+// the side streams and events of the concurrent level classes (on the current device)
+static void ensure_side_streams(const CholSymbolic& s) {
+  if (s.ev_fork) return;
+  for (int i = 0; i < CholSymbolic::kSideStreams; ++i) {
+    VH_CUDA_TRY(cudaStreamCreateWithFlags(&s.side[i], cudaStreamNonBlocking));
+    VH_CUDA_TRY(cudaEventCreateWithFlags(&s.ev_join[i], cudaEventDisableTiming));
+  }
+  VH_CUDA_TRY(cudaEventCreateWithFlags(&s.ev_fork, cudaEventDisableTiming));
+}
+
+// the fronts of level hl too large for one CTA: extend-add of the children's update matrices,
+// then blocks of kNB pivots (diagonal block, panel, trailing update), all on stream bs
+template <typename T>
+static void blocked_level(const CholSymbolic& s, size_t hl, unsigned nz, T* const* Wp, int* d_err, cudaStream_t bs) {
+  const unsigned nf = (unsigned)s.levels_blocked[hl].size();
+  const int32_t* lev = s.d_levels_blocked[hl];
+  if (hl > 0) {
+    const unsigned cy = (unsigned)std::min(1024, std::max(1, s.blocked_max_nf[hl]));
+    for (int which = 0; which < 2; ++which) {
+      k_chol_extend_add<T><<<dim3(nf, cy, nz), 128, 0, bs>>>(lev, s.d_fronts, s.d_relmap, Wp, which);
+      count_launch();
+      VH_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  const int max_ns = s.blocked_max_ns[hl];
+  const int max_nf = s.blocked_max_nf[hl];
+  for (int k0 = 0; k0 < max_ns; k0 += kNB) {
+    k_chol_diag<T><<<dim3(nf, 1, nz), 256, 0, bs>>>(lev, s.d_fronts, Wp, k0, d_err);
+    count_launch();
+    const int rows = max_nf - k0;
+    if (rows > 0) {
+      k_chol_panel<T><<<dim3(nf, (unsigned)ceil_div(rows, 128), nz), 128, 0, bs>>>(lev, s.d_fronts, Wp, k0);
+      count_launch();
+      const int nt = (int)ceil_div(rows, kTS);
+      k_chol_update<T><<<dim3(nf, (unsigned)(nt * (nt + 1) / 2), nz), 256, 0, bs>>>(lev, s.d_fronts, Wp, k0);
+      count_launch();
+    }
+    VH_CUDA_TRY(cudaGetLastError());
+  }
+}
+
 template <typename T>
 void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* const* W, cudaStream_t st) {
   if (s.nfronts == 0 || nfac == 0) return;
@@ -490,35 +531,46 @@ void chol_factor(const CholSymbolic& s, int nfac, const double* const* D, T* con
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
     for (size_t hl = 0; hl < s.levels.size(); ++hl) {
-      for (const auto& fc : s.fused_classes[hl])
+      // the class with the most fronts runs on st; the level's other classes and its blocked fronts
+      // on the side streams (forked from st at the level start, joined into st at its end)
+      const auto& cls = s.fused_classes[hl];
+      const bool has_blocked = !s.levels_blocked[hl].empty();
+      int main_c = -1;
+      for (int c = 0; c < (int)cls.size(); ++c)
+        if (main_c < 0 || cls[c].count > cls[main_c].count) main_c = c;
+      const int nside = (int)cls.size() - (main_c >= 0 ? 1 : 0) + (has_blocked ? 1 : 0);
+      bool used[CholSymbolic::kSideStreams] = {};
+      int next_side = 0;
+      auto side_stream = [&]() -> cudaStream_t {
+        const int i = next_side++ % CholSymbolic::kSideStreams;
+        if (!used[i]) {
+          VH_CUDA_TRY(cudaStreamWaitEvent(s.side[i], s.ev_fork, 0));
+          used[i] = true;
+        }
+        return s.side[i];
+      };
+      if (nside > 0) {
+        ensure_side_streams(s);
+        VH_CUDA_TRY(cudaEventRecord(s.ev_fork, st));
+      }
+      for (int c = 0; c < (int)cls.size(); ++c) {
+        if (c == main_c) continue;
+        const auto& fc = cls[c];
+        launch_front<T>(fc.max_nf, s.d_levels_fused[hl] + fc.offset, (unsigned)fc.count, nz,
+                        fused_smem_bytes<T>(fc.max_nf, fc.max_ns), s, Wp, d_err, side_stream());
+      }
+      cudaStream_t bs = has_blocked ? side_stream() : st;
+      if (main_c >= 0) {
+        const auto& fc = cls[main_c];
         launch_front<T>(fc.max_nf, s.d_levels_fused[hl] + fc.offset, (unsigned)fc.count, nz,
                         fused_smem_bytes<T>(fc.max_nf, fc.max_ns), s, Wp, d_err, st);
-      if (s.levels_blocked[hl].empty()) continue;
-      const unsigned nf = (unsigned)s.levels_blocked[hl].size();
-      const int32_t* lev = s.d_levels_blocked[hl];
-      if (hl > 0) {
-        const unsigned cy = (unsigned)std::min(1024, std::max(1, s.blocked_max_nf[hl]));
-        for (int which = 0; which < 2; ++which) {
-          k_chol_extend_add<T><<<dim3(nf, cy, nz), 128, 0, st>>>(lev, s.d_fronts, s.d_relmap, Wp, which);
-          count_launch();
-          VH_CUDA_TRY(cudaGetLastError());
-        }
       }
-      const int max_ns = s.blocked_max_ns[hl];
-      const int max_nf = s.blocked_max_nf[hl];
-      for (int k0 = 0; k0 < max_ns; k0 += kNB) {
-        k_chol_diag<T><<<dim3(nf, 1, nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0, d_err);
-        count_launch();
-        const int rows = max_nf - k0;
-        if (rows > 0) {
-          k_chol_panel<T><<<dim3(nf, (unsigned)ceil_div(rows, 128), nz), 128, 0, st>>>(lev, s.d_fronts, Wp, k0);
-          count_launch();
-          const int nt = (int)ceil_div(rows, kTS);
-          k_chol_update<T><<<dim3(nf, (unsigned)(nt * (nt + 1) / 2), nz), 256, 0, st>>>(lev, s.d_fronts, Wp, k0);
-          count_launch();
+      if (has_blocked) blocked_level<T>(s, hl, nz, Wp, d_err, bs);
+      for (int i = 0; i < CholSymbolic::kSideStreams; ++i)
+        if (used[i]) {
+          VH_CUDA_TRY(cudaEventRecord(s.ev_join[i], s.side[i]));
+          VH_CUDA_TRY(cudaStreamWaitEvent(st, s.ev_join[i], 0));
         }
-        VH_CUDA_TRY(cudaGetLastError());
-      }
     }
     int herr = 0;
     VH_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));

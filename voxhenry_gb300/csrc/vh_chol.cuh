@@ -68,6 +68,12 @@ struct CholSymbolic {
   int* d_err = nullptr;             // factorisation status flag
   mutable void** d_tab = nullptr;   // device pointer table of the batched factorisation
   mutable int tab_cap = 0;
+  // side streams of the factorisation: the occupancy classes and the blocked fronts of one level
+  // are independent and run concurrently, joined before the next level (created on first use)
+  static constexpr int kSideStreams = 3;
+  mutable cudaStream_t side[kSideStreams] = {};
+  mutable cudaEvent_t ev_fork = nullptr;
+  mutable cudaEvent_t ev_join[kSideStreams] = {};
   int64_t n_asm = 0;
   void free_all();
 };

@@ -33,6 +33,14 @@ void CholSymbolic::free_all() {
   cudaFree(d_tab);
   d_tab = nullptr;
   tab_cap = 0;
+  for (int i = 0; i < kSideStreams; ++i) {
+    if (side[i]) cudaStreamDestroy(side[i]);
+    if (ev_join[i]) cudaEventDestroy(ev_join[i]);
+    side[i] = nullptr;
+    ev_join[i] = nullptr;
+  }
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  ev_fork = nullptr;
   d_levels.clear();
   d_fronts = nullptr; d_rows = nullptr; d_relmap = nullptr; d_asm = nullptr; d_asm_q = nullptr; d_asm_c = nullptr;
 }
