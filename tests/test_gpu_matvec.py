@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12     # single FP64 matvec, relative 2-norm
 FP32_TOL = 2e-6      # complex64 FFT convolution, relative 2-norm
-DF_TOL = 1e-12       # complex128 storage, double-float z-pass (~48 significant bits), relative 2-norm
+DF_TOL = 1e-12       # double-float passes (~48 significant bits), relative 2-norm
 
 
 @pytest.fixture(scope="module")
@@ -166,10 +166,18 @@ def test_matvec_voxel_box_inside_grid(vie, prec, tol, shape, zr):
         assert rel(Y[b], ref) < tol
 
 
-@pytest.mark.parametrize("shape,zr", BOXES)
-def test_matvec_df_takes_the_double_float_z_pass(vie, shape, zr):
-    """VH_PREC_DF differs from FP64 only by double-float rounding where the register z-pass runs
-    (padded z length 8, 16, 32), and equals FP64 bit for bit where it falls back (length 18)."""
+DF_BOXES = BOXES + [  # padded x and y lengths 256 (the double-float passes' shapes), z 8 / 16 / 18
+    ((128, 128, 4), (1, 3)),
+    ((128, 128, 8), (2, 5)),
+    ((128, 128, 9), (2, 6)),
+]
+
+
+@pytest.mark.parametrize("shape,zr", DF_BOXES)
+def test_matvec_df_takes_the_double_float_passes(vie, shape, zr):
+    """VH_PREC_DF differs from FP64 only by double-float rounding where the double-float passes run
+    (padded x and y lengths 256, 512 or 1024 and z length 8, 16 or 32), and equals FP64 bit for bit
+    where it falls back to the complex128 product."""
     from voxhenry_gb300 import geometry
 
     L, M, N = shape
@@ -183,7 +191,9 @@ def test_matvec_df_takes_the_double_float_z_pass(vie, shape, zr):
     Y64 = g.matvec(X, scale=s, prec="fp64")
     Ydf = g.matvec(X, scale=s, prec="df")
     d = max(rel(Ydf[b], Y64[b]) for b in range(2))
-    if 2 * N in (8, 16, 32):
+    if 2 * L in (256, 512, 1024) and 2 * M in (256, 512, 1024) and 2 * N in (8, 16, 32):
         assert 0 < d < DF_TOL
+        ref = solver.lse_matvect_mult(X[0], s[0] * fN, S.Ar, z_real, None, S.dx, S.idxS5)
+        assert rel(Ydf[0], ref) < DF_TOL   # and against the oracle
     else:
         assert d == 0

@@ -34,8 +34,12 @@ struct ConvPlan {
   // one float per component (the real or the imaginary part, layout as tens32); set when the
   // spectrum was checked to be of that form to within 1e-9 of each component's magnitude
   float* tens32ri = nullptr;
-  void* tensdf = nullptr;     // double-float copy of tens64 (pairs of floats), built on first PREC_DF use
+  bool ri = false;            // the spectrum has the real/imaginary form above (checked at creation)
+  void* tensdf = nullptr;     // double-float real/imaginary tensor (one pair of floats per component,
+                              // layout as tens32ri), built on first PREC_DF use when ri holds
   void* twdf = nullptr;       // double-float z twiddles
+  void* twxdf = nullptr;      // double-float x and y twiddles
+  void* twydf = nullptr;
   double2* tw64[3] = {nullptr, nullptr, nullptr};
   float2* tw32[3] = {nullptr, nullptr, nullptr};
   // scratch: A (5 * nz * ny * X per RHS) and Bf (5 * nz * Y * X per RHS), in bytes

@@ -35,6 +35,8 @@ struct dcomplex {
 template <> struct cplx_t<dfloat> { using type = dcomplex; };
 
 __device__ __forceinline__ dcomplex to_c(double2 a, dcomplex) { return dcomplex{dfloat(a.x), dfloat(a.y)}; }
+__device__ __forceinline__ dcomplex to_c(dcomplex a, dcomplex) { return a; }
+__host__ __device__ __forceinline__ dcomplex mk(dfloat a, dfloat b) { return dcomplex{a, b}; }
 __device__ __forceinline__ double2 to_d(dcomplex a) { return make_double2(a.x.to_double(), a.y.to_double()); }
 
 // s + e = a + b exactly (Knuth)
