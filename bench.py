@@ -312,7 +312,7 @@ def run_ours(args, rank, world):
     ms, calls, units = prof
     peak, peak_kind = measured_hbm_peak()
     sections = {name: {"ms": round(float(ms[i]), 3), "calls": int(calls[i]), "rhs": int(units[i])}
-                for i, name in enumerate(["fft_conv_c128", "fft_conv_c64", "incidence_spmv", "schur_factor",
+                for i, name in enumerate(["fft_conv_df", "fft_conv_c64", "incidence_spmv", "schur_factor",
                                           "precon_apply", "krylov_vectors", "tensor"])}
     step_ms_total = 1e3 * t_mixed
     dominant = max(sections, key=lambda k: sections[k]["ms"])
@@ -334,11 +334,10 @@ def run_ours(args, rank, world):
                 "avg_launch_ms": round(conv_ms / conv_calls, 4),
                 "share_of_step_time": round(conv_ms / step_ms_total, 4), "note": note}
 
-    roof64 = fft_roofline(0, 16, "FFT circulant matvec, complex128 storage (refinement residuals, VH_PREC_DF: FP64 "
-                          "x/y passes, double-float z-pass; 5 passes)", "fft_matvec_df_spiral.txt",
-                          "x/y passes bound by GB300's FP64 pipe (84-85 % busy in ncu), the double-float z-pass "
-                          "issue-bound (62 %); frac is against HBM with the algorithmic bytes of the two-pass "
-                          "pruned model")
+    roof64 = fft_roofline(0, 16, "FFT circulant matvec in double-float (refinement residuals, VH_PREC_DF: all 5 "
+                          "passes in pair arithmetic, pair storage between passes)", "fft_matvec_df_spiral.txt",
+                          "pair-arithmetic passes issue-bound on the FP32 pipes, the z-pass half of the call; "
+                          "frac is against HBM with the algorithmic bytes of the two-pass pruned model")
     roof32 = fft_roofline(1, 8, "FFT circulant matvec, complex64 (inner GMRES matvecs; 5 passes)",
                           "fft_matvec_c64_spiral.txt", "issue-bound passes (56-70 % issue active in ncu)")
     # the preconditioner apply (double-float triangular solves and the SpMVs around them): per
@@ -396,7 +395,7 @@ def run_ours(args, rank, world):
     # RHS-matvecs per second of the FFT operator, from the live section timing of the mixed step
     line["matvecs_per_s"] = {
         "complex64": round(sections["fft_conv_c64"]["rhs"] / max(1e-9, sections["fft_conv_c64"]["ms"] / 1e3), 1),
-        "complex128_storage_df": round(sections["fft_conv_c128"]["rhs"] / max(1e-9, sections["fft_conv_c128"]["ms"] / 1e3), 1),
+        "double_float": round(sections["fft_conv_df"]["rhs"] / max(1e-9, sections["fft_conv_df"]["ms"] / 1e3), 1),
         "note": "one RHS-matvec = the full operator of lse_matvect_mult.m on one vector; batched calls of ~11 "
                 "(complex64) and 32 (refinement residual) vectors"}
     if args.serving_requests >= 0 and world == 1:
