@@ -621,7 +621,7 @@ struct SolveSmem {
 };
 
 template <typename T, bool STAGE>
-__global__ void __launch_bounds__(32 * kSolveWarps, (STAGE || std::is_same<T, double>::value) ? 4 : kFsolveCtasPerSm)
+__global__ void __launch_bounds__(32 * kSolveWarps, std::is_same<T, double>::value ? 4 : (STAGE ? 5 : kFsolveCtasPerSm))
     k_chol_fsolve(const int32_t* __restrict__ lev, int nlev, int B, const FrontInfo* __restrict__ fr,
                   const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap, T* const* __restrict__ Wp,
                   cplx<T>* __restrict__ x, int64_t ldx, int64_t xoff, cplx<T>* __restrict__ U, int64_t u_total,
