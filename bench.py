@@ -523,16 +523,30 @@ def run_probe(args):
         st = (1j * 2 * np.pi * w.freqs[:B] * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
         pcs = g.precons(st, np.zeros(B, dtype=np.int32), kind=args.probe_kind)
         parr = (C.c_void_p * B)(*[p.handle for p in pcs])
-        for _ in range(args.probe_iters):
-            _lib.check(lib.vh_precon_apply_device(g.handle, B, parr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr())),
-                       g.ctx.handle)
+        if args.probe == "gmres":   # one restart cycle of the mixed-precision inner GMRES (no refinement)
+            tol = np.full(B, 1e-30)
+            flag = np.zeros(B, dtype=np.int32)
+            it = np.zeros(2 * B, dtype=np.int32)
+            nres = np.zeros(B, dtype=np.int32)
+            relres = np.zeros(B)
+            ip = C.POINTER(C.c_int)
+            scale = np.full(B, 1j * 2 * np.pi * w.freqs[0] * executer.MU0)
+            for _ in range(args.probe_iters):
+                _lib.check(lib.vh_gmres_device(g.handle, B, parr, C.c_void_p(x.data_ptr()), _lib.cview(scale), None,
+                                               args.probe_restart, _lib.dptr(tol), 1, 0, _lib.PREC["fp64"],
+                                               C.c_void_p(y.data_ptr()), flag.ctypes.data_as(ip), _lib.dptr(relres),
+                                               it.ctypes.data_as(ip), None, 0, nres.ctypes.data_as(ip)), g.ctx.handle)
+        else:
+            for _ in range(args.probe_iters):
+                _lib.check(lib.vh_precon_apply_device(g.handle, B, parr, C.c_void_p(x.data_ptr()),
+                                                      C.c_void_p(y.data_ptr())), g.ctx.handle)
     g.ctx.synchronize()
     print(json.dumps({"probe": args.probe, "rhs": B, "iters": args.probe_iters, "launches": int(lib.vh_launch_count())}))
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["conv32", "conv64", "convdf", "precon"], default=None,
+    ap.add_argument("--probe", choices=["conv32", "conv64", "convdf", "precon", "gmres"], default=None,
                     help="profiling aid: run a few calls of one operator instead of the benchmark")
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: run only the warm-up and timed mixed-precision sweeps, print nothing")
@@ -544,6 +558,7 @@ def main():
                          "this (mixed path); off by default")
     ap.add_argument("--probe-rhs", type=int, default=4)
     ap.add_argument("--probe-iters", type=int, default=3)
+    ap.add_argument("--probe-restart", type=int, default=20)
     ap.add_argument("--probe-kind", default="schur_invert", choices=["schur_invert", "schur_invert_df"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)

@@ -139,6 +139,28 @@ template <typename T> struct dot_of;
 template <> struct dot_of<double> { using type = d_dot; };
 template <> struct dot_of<dfloat> { using type = df_dot; };
 
+// double -> pair on the integer and FP32 pipes (GB300's FP64 pipe, which the conversion
+// instructions use, runs at 1/64 of the FP32 rate).  hi takes the sign, the exponent and the top 23
+// fraction bits of d (truncated); lo the remaining 29 fraction bits, rounded to a float.  hi + lo
+// equals d to within 2^-47 |d| and |lo| < ulp(hi).  Zero (and FP64 subnormals) give zero; magnitudes
+// outside [2^-74, 2^127) -- where lo would leave the normal float range or hi overflow -- take the
+// conversion instructions.
+__device__ __forceinline__ dfloat df_split(double d) {
+  const unsigned hw = (unsigned)__double2hiint(d), lw = (unsigned)__double2loint(d);
+  const unsigned e = (hw >> 20) & 0x7FFu;   // biased binary64 exponent
+  if (e - 949u <= 1150u - 949u) {
+    const unsigned s = hw & 0x80000000u;
+    dfloat r;
+    r.hi = __uint_as_float(s | ((e - 896u) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+    // the remainder's weight is 2^(e - 1075); e >= 949 keeps that power of two a normal float
+    const float rem = __uint2float_rn(lw & 0x1FFFFFFFu) * __uint_as_float((e - 948u) << 23);
+    r.lo = __uint_as_float(__float_as_uint(rem) | s);
+    return r;
+  }
+  if (e == 0) return dfloat(0.0f);
+  return dfloat(d);
+}
+
 // 1 / b: single-precision seed, then two Newton steps y <- y + y (1 - b y), each in pair arithmetic
 __device__ __forceinline__ dfloat df_recip(dfloat b) {
   dfloat y(__frcp_rn(b.hi));

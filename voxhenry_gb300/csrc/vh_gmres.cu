@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/voxhenry_gpu.h"
+#include "vh_df.cuh"
 #include "vh_internal.cuh"
 
 namespace vh {
@@ -101,6 +102,122 @@ __global__ void k_cgs_update(const double2* __restrict__ V, int64_t ldv, int64_t
     za[i] = q;
     s = fma(q.x, q.x, fma(q.y, q.y, s));
   }
+  __shared__ double red[kChunkThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    partial[(int64_t)a * nch + c] = t;
+  }
+}
+
+// ---- the same Gram-Schmidt steps in pair arithmetic on the FP32 pipes, for the inner GMRES of the
+// mixed-precision solver.  The FP64 versions above keep GB300's FP64 pipe ~87 % busy at ~25 % of HBM
+// bandwidth (4 FP64 FMAs per 16-byte basis element).  Here each FP64 operand is split into a float
+// pair with integer operations (df_split) and the sums run as Dot2 accumulations (~48 bits); the
+// basis and the work vectors stay complex128.
+constexpr int kChunkPer = kChunkElems / kChunkThreads;   // elements per thread in a chunk
+
+// partial[a][c][j] = sum_{i in chunk c} conj(V_b[j][i]) z_a[i], as k_multidot over chunks of
+// kDotDfChunk elements: kDotDfPer per thread, their z split once and kept in registers, the V loads
+// of one basis vector all issued before its arithmetic; one barrier per basis vector (the warp
+// sums alternate between two shared rows)
+constexpr int kDotDfPer = 4;
+constexpr int kDotDfChunk = kChunkThreads * kDotDfPer;
+
+__global__ void __launch_bounds__(kChunkThreads)
+    k_multidot_df(const double2* __restrict__ V, int64_t ldv, int64_t ldb, const double2* __restrict__ z, int64_t ldz,
+                  const int* __restrict__ act, int nj, int64_t n, double2* __restrict__ partial) {
+  const int a = blockIdx.y;
+  const int c = blockIdx.x;
+  const int nch = gridDim.x;
+  const double2* Vb = V + (int64_t)act[a] * ldb;
+  const double2* za = z + (int64_t)a * ldz;
+  const int64_t i0 = (int64_t)c * kDotDfChunk + threadIdx.x;
+  dfloat zx[kDotDfPer], zy[kDotDfPer];
+#pragma unroll
+  for (int u = 0; u < kDotDfPer; ++u) {
+    const int64_t i = i0 + (int64_t)u * kChunkThreads;
+    const double2 q = i < n ? za[i] : make_double2(0.0, 0.0);
+    zx[u] = df_split(q.x);
+    zy[u] = df_split(q.y);
+  }
+  __shared__ double2 red[2][kChunkThreads / 32];
+  for (int j = 0; j < nj; ++j) {
+    const double2* v = Vb + (int64_t)j * ldv;
+    double2 p[kDotDfPer];
+#pragma unroll
+    for (int u = 0; u < kDotDfPer; ++u) {
+      const int64_t i = i0 + (int64_t)u * kChunkThreads;
+      p[u] = i < n ? v[i] : make_double2(0.0, 0.0);
+    }
+    df_dot sx(dfloat(0.0f)), sy(dfloat(0.0f));
+#pragma unroll
+    for (int u = 0; u < kDotDfPer; ++u) {
+      const dfloat px = df_split(p[u].x), py = df_split(p[u].y);
+      sx.add(px, zx[u]);    // Re conj(p) q = px qx + py qy
+      sx.add(py, zy[u]);
+      sy.add(px, zy[u]);    // Im conj(p) q = px qy - py qx
+      sy.add(-py, zx[u]);
+    }
+    sx.warp_sum();
+    sy.warp_sum();
+    if ((threadIdx.x & 31) == 0)
+      red[j & 1][threadIdx.x >> 5] = make_double2(sx.value().to_double(), sy.value().to_double());
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double2 t = make_double2(0.0, 0.0);
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t.x += red[j & 1][w].x; t.y += red[j & 1][w].y; }
+      partial[((int64_t)a * nch + c) * nj + j] = t;
+    }
+  }
+}
+
+constexpr int kCgsDfMaxNj = 128;   // basis vectors held (split) in shared memory
+
+// z_a -= sum_{j<nj} h[a][j] V_b[j];  partial[a][c] = sum |z_a|^2 over the chunk, as k_cgs_update
+__global__ void __launch_bounds__(kChunkThreads)
+    k_cgs_update_df(const double2* __restrict__ V, int64_t ldv, int64_t ldb, double2* __restrict__ z, int64_t ldz,
+                    const int* __restrict__ act, const double2* __restrict__ h, int ldh, int nj, int64_t n,
+                    double* __restrict__ partial) {
+  const int a = blockIdx.y;
+  const int c = blockIdx.x;
+  const int nch = gridDim.x;
+  const double2* Vb = V + (int64_t)act[a] * ldb;
+  double2* za = z + (int64_t)a * ldz;
+  __shared__ dfloat hs[kCgsDfMaxNj][2];
+  for (int j = threadIdx.x; j < nj; j += blockDim.x) {
+    const double2 hj = h[(int64_t)a * ldh + j];
+    hs[j][0] = df_split(hj.x);
+    hs[j][1] = df_split(hj.y);
+  }
+  __syncthreads();
+  const int64_t i0 = (int64_t)c * kChunkElems + threadIdx.x;
+  df_dot nrm(dfloat(0.0f));
+  for (int u = 0; u < kChunkPer; ++u) {
+    const int64_t i = i0 + (int64_t)u * kChunkThreads;
+    if (i >= n) break;
+    const double2 q = za[i];
+    df_dot qx(df_split(q.x)), qy(df_split(q.y));
+#pragma unroll 4
+    for (int j = 0; j < nj; ++j) {
+      const double2 v = Vb[(int64_t)j * ldv + i];
+      const dfloat vx = df_split(v.x), vy = df_split(v.y);
+      const dfloat hx = hs[j][0], hy = hs[j][1];
+      qx.add(-hx, vx);     // Re(q - h v) = qx - hx vx + hy vy
+      qx.add(hy, vy);
+      qy.add(-hx, vy);     // Im(q - h v) = qy - hx vy - hy vx
+      qy.add(-hy, vx);
+    }
+    const dfloat rx = qx.value(), ry = qy.value();
+    za[i] = make_double2(rx.to_double(), ry.to_double());
+    nrm.add(rx, rx);
+    nrm.add(ry, ry);
+  }
+  double s = nrm.value().to_double();
   __shared__ double red[kChunkThreads / 32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -299,7 +416,8 @@ void gmres_core(const KrylovOps& op, int B, const double2* b, const double* tol,
   d_act.ensure(B);
   d_cnt.ensure(B);
   const int nch = (int)std::max<int64_t>(1, ceil_div(n, kChunkElems));
-  partc.ensure((size_t)B * nch * (m + 1));
+  const int nch_df = (int)std::max<int64_t>(1, ceil_div(n, kDotDfChunk));   // chunks of k_multidot_df
+  partc.ensure((size_t)B * std::max(nch, nch_df) * (m + 1));
   partr.ensure((size_t)B * nch);
   nrm.ensure(B);
   auto apply_A = [&](const std::vector<int>& act, const double2* xin, double2* yout, Prec p) {
@@ -409,12 +527,21 @@ void gmres_core(const KrylovOps& op, int B, const double2* b, const double* tol,
       double2* w = (flexible || !has_M) ? Wc.p : Zc.p;
       // classical Gram-Schmidt: h = V^H w ; w -= V h ; h_{k+1} = |w| (pgmres_iter.m:107-110)
       ProfScope ps(op.prof, SEC_KRYLOV, st, nr);
-      k_multidot<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, k + 1, n, partc.p);
+      // the mixed path's inner iterations take the pair-arithmetic kernels (FP32 pipes)
+      const bool pair = prec == PREC_FP32 && k + 1 <= kCgsDfMaxNj;
+      if (pair)
+        k_multidot_df<<<dim3(nch_df, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, k + 1, n, partc.p);
+      else
+        k_multidot<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, k + 1, n, partc.p);
       count_launch();
-      k_reduce_partials<<<nr, 128, 0, st>>>(partc.p, nch, k + 1, hbuf.p, m + 2);
+      k_reduce_partials<<<nr, 128, 0, st>>>(partc.p, pair ? nch_df : nch, k + 1, hbuf.p, m + 2);
       count_launch();
-      k_cgs_update<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, hbuf.p, m + 2, k + 1, n,
-                                                            partr.p);
+      if (pair)
+        k_cgs_update_df<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, hbuf.p, m + 2, k + 1,
+                                                                 n, partr.p);
+      else
+        k_cgs_update<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, hbuf.p, m + 2, k + 1, n,
+                                                              partr.p);
       count_launch();
       k_reduce_norm<<<nr, 32, 0, st>>>(partr.p, nch, nrm.p);
       count_launch();
