@@ -63,18 +63,25 @@ __global__ void k_multidot(const double2* __restrict__ V, int64_t ldv, int64_t l
   }
 }
 
-// out[a * ldo + j] = sum_c partial[a][c][j]   (fixed order: deterministic)
+// out[a * ldo + j] = sum_c partial[a][c][j]: one warp per j, lanes striding the chunks, then a fixed
+// butterfly (deterministic order)
 __global__ void k_reduce_partials(const double2* __restrict__ partial, int nch, int nj, double2* __restrict__ out,
                                   int ldo) {
   const int a = blockIdx.x;
-  for (int j = threadIdx.x; j < nj; j += blockDim.x) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int j = threadIdx.x >> 5; j < nj; j += nw) {
     double2 t = make_double2(0.0, 0.0);
-    for (int c = 0; c < nch; ++c) {
+    for (int c = lane; c < nch; c += 32) {
       const double2 p = partial[((int64_t)a * nch + c) * nj + j];
       t.x += p.x;
       t.y += p.y;
     }
-    out[(int64_t)a * ldo + j] = t;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      t.x += __shfl_xor_sync(0xffffffffu, t.x, o);
+      t.y += __shfl_xor_sync(0xffffffffu, t.y, o);
+    }
+    if (lane == 0) out[(int64_t)a * ldo + j] = t;
   }
 }
 
@@ -255,13 +262,15 @@ __global__ void k_norm2_partial(const double2* __restrict__ x, int64_t ldx, cons
   }
 }
 
+// out[a] = sqrt(sum_c partial[a][c]): one warp per RHS (launched with 32 threads), lanes striding the
+// chunks, then a fixed butterfly
 __global__ void k_reduce_norm(const double* __restrict__ partial, int nch, double* __restrict__ out) {
   const int a = blockIdx.x;
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int c = 0; c < nch; ++c) t += partial[(int64_t)a * nch + c];
-    out[a] = sqrt(t);
-  }
+  double t = 0.0;
+  for (int c = threadIdx.x; c < nch; c += 32) t += partial[(int64_t)a * nch + c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (threadIdx.x == 0) out[a] = sqrt(t);
 }
 
 // dst_b = src_a * (1 / nrm[a])  (zero when nrm == 0: breakdown)
@@ -534,7 +543,7 @@ void gmres_core(const KrylovOps& op, int B, const double2* b, const double* tol,
       else
         k_multidot<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, k + 1, n, partc.p);
       count_launch();
-      k_reduce_partials<<<nr, 128, 0, st>>>(partc.p, pair ? nch_df : nch, k + 1, hbuf.p, m + 2);
+      k_reduce_partials<<<nr, 256, 0, st>>>(partc.p, pair ? nch_df : nch, k + 1, hbuf.p, m + 2);
       count_launch();
       if (pair)
         k_cgs_update_df<<<dim3(nch, nr), kChunkThreads, 0, st>>>(V.p, ldv, ldb, w, n, d_act.p, hbuf.p, m + 2, k + 1,
