@@ -277,7 +277,10 @@ __global__ void k_reduce_norm(const double* __restrict__ partial, int nch, doubl
 __global__ void k_scale_into(const double2* __restrict__ src, int64_t lds, double2* __restrict__ dst, int64_t ldd,
                              const int* __restrict__ act, const double* __restrict__ nrm, int64_t n) {
   const int a = blockIdx.y;
-  const double s = nrm[a] > 0.0 ? 1.0 / nrm[a] : 0.0;
+  __shared__ double s_sh;   // one FP64 division per block, not per thread (GB300's FP64 pipe is slow)
+  if (threadIdx.x == 0) s_sh = nrm[a] > 0.0 ? 1.0 / nrm[a] : 0.0;
+  __syncthreads();
+  const double s = s_sh;
   const double2* sa = src + (int64_t)a * lds;
   double2* db = dst + (int64_t)act[a] * ldd;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {

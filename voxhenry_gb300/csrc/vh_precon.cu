@@ -79,6 +79,30 @@ __global__ void k_precon_rhs(int64_t nphi, const int32_t* __restrict__ rp, const
   phi[b * ldphi + r] = to_c(acc, C());
 }
 
+// the same for the double-float factor, on the FP32 pipes: the FP64 operands are split into pairs
+// with integer operations (df_split) and each row's sum runs as a Dot2 accumulation, so neither the
+// arithmetic nor the conversion of phi to pairs uses GB300's FP64 pipe
+__global__ void k_precon_rhs_df(int64_t nphi, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                const double* __restrict__ val, double* const* __restrict__ ainv,
+                                const double2* __restrict__ x, int64_t ld, int64_t nc, dcomplex* __restrict__ phi,
+                                int64_t ldphi) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (r >= nphi) return;
+  const double2* xb = x + b * ld;
+  const double* ai = ainv[b];
+  const double2 x0 = xb[nc + r];
+  df_dot ax(df_split(x0.x)), ay(df_split(x0.y));
+  for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
+    const int32_t q = col[k];
+    const dfloat a = df_split(val[k]) * df_split(ai[q]);
+    const double2 xq = xb[q];
+    ax.add(-a, df_split(xq.x));
+    ay.add(-a, df_split(xq.y));
+  }
+  phi[b * ldphi + r] = dcomplex{ax.value(), ay.value()};
+}
+
 // y_J[b] = (x_J[b] + Ar^T phi[b]) .* A_inv_b;  y_phi[b] = phi[b] when phi is not y's own storage
 template <typename C>
 __global__ void k_precon_finish(int64_t nc, int64_t nphi, const int32_t* __restrict__ rp,
@@ -269,8 +293,8 @@ void precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const double2
   if (g->nphi > 0) {
     const dim3 grid((unsigned)ceil_div(g->nphi, 256), B);
     if (df) {
-      k_precon_rhs<dcomplex><<<grid, 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val, d_ainv, x, g->n,
-                                                   g->nc, phi_df, g->nphi);
+      k_precon_rhs_df<<<grid, 256, 0, st>>>(g->nphi, g->Ae.rowptr, g->Ae.col, g->Ae.val, d_ainv, x, g->n, g->nc,
+                                            phi_df, g->nphi);
       count_launch();
       VH_CUDA_TRY(cudaGetLastError());
       chol_solve<dfloat>(g->chol, B, reinterpret_cast<dfloat* const*>(g->pc_ptrs + B), phi_df, g->nphi, 0,
