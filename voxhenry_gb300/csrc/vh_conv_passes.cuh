@@ -78,12 +78,26 @@ static int z_lines_per_cta(int Z, int X) {
 // them, else the runtime stages.
 constexpr int kPassThreads = 256;
 
+// The x passes' line-major buffers: on the static path they hold element a at a + (a >> XPAD)
+// with one padding element per 128 bytes (every 16 complex64, every 8 of 16-byte elements), which
+// makes the first stage's stride-8 stores conflict-free.
+template <typename C> __host__ __device__ constexpr int xpad_log() { return sizeof(C) == 8 ? 4 : 3; }
+__host__ __device__ __forceinline__ bool x_static(int n, int nl) {
+  return (n == 256 && nl == 8) || (n == 512 && nl == 4) || (n == 1024 && nl == 2);
+}
+// elements of a buffer holding m padded logical elements, rounded up to whole 16 bytes so that the
+// second buffer (and the 16-byte tile copies of the unpadded path) stay 16-byte aligned
+template <typename C> __host__ __device__ constexpr int xpad_len(int m) {
+  return (m + (m >> xpad_log<C>()) + (int)(16 / sizeof(C)) - 1) / (int)(16 / sizeof(C)) * (int)(16 / sizeof(C));
+}
+
 template <int DIR, typename C>
 __device__ __forceinline__ C* fft_x_lines(C* b0, C* b1, const C* tw, const FftDesc& fd, int nl) {
+  constexpr int PL = xpad_log<C>();
   if (blockDim.x == kPassThreads) {
-    if (fd.n == 256 && nl == 8) return fft_stages_fixed<256, 1, 8, true, DIR, kPassThreads>(b0, b1, tw);
-    if (fd.n == 512 && nl == 4) return fft_stages_fixed<512, 1, 4, true, DIR, kPassThreads>(b0, b1, tw);
-    if (fd.n == 1024 && nl == 2) return fft_stages_fixed<1024, 1, 2, true, DIR, kPassThreads>(b0, b1, tw);
+    if (fd.n == 256 && nl == 8) return fft_stages_fixed<256, 1, 8, true, DIR, kPassThreads, PL>(b0, b1, tw);
+    if (fd.n == 512 && nl == 4) return fft_stages_fixed<512, 1, 4, true, DIR, kPassThreads, PL>(b0, b1, tw);
+    if (fd.n == 1024 && nl == 2) return fft_stages_fixed<1024, 1, 2, true, DIR, kPassThreads, PL>(b0, b1, tw);
   }
   if constexpr (std::is_same<C, dcomplex>::value) {
     return b0;   // not reached: the double-float product is admitted only for the shapes above
@@ -151,8 +165,10 @@ __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int3
   const int X = fd.n;
   C* tw = reinterpret_cast<C*>(smem_raw);
   C* b0 = tw + X;
-  C* b1 = b0 + X * nl;
-  XLine* li = reinterpret_cast<XLine*>(b1 + X * nl);
+  C* b1 = b0 + xpad_len<C>(X * nl);
+  XLine* li = reinterpret_cast<XLine*>(b1 + xpad_len<C>(X * nl));
+  const bool pad = x_static(X, nl) && blockDim.x == kPassThreads;   // the layout fft_x_lines uses
+  auto P = [&](int a) { return pad ? a + (a >> xpad_log<C>()) : a; };
   for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
   const int64_t l0 = (int64_t)blockIdx.x * nl;
   decode_lines(li, l0, nl, nlines_total, L, M, y0, ny, z0, nz, ldx, nv);
@@ -163,7 +179,7 @@ __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int3
   const int XL = X - L;
   for (int t = threadIdx.x; t < XL * nl; t += blockDim.x) {
     const int line = t / XL;
-    b0[line * X + L + (t - line * XL)] = czero<C>();
+    b0[P(line * X + L + (t - line * XL))] = czero<C>();
   }
   const bool p2 = (L & (L - 1)) == 0;
   const int ll = __ffs(L) - 1;
@@ -194,14 +210,19 @@ __global__ void k_fwd_x(const double2* __restrict__ xin, int64_t ldx, const int3
       }
       if (t < tot) {
         const int line = div_line(t, L, p2, ll);
-        b0[line * X + (t - line * L)] = v;
+        b0[P(line * X + (t - line * L))] = v;
       }
     }
   }
   __syncthreads();
   C* r = fft_x_lines<-1>(b0, b1, tw, fd, nl);
   const int rows = (nlines_total - l0 < nl) ? (int)(nlines_total - l0) : nl;
-  tile_store(A + l0 * X, X, r, X, rows, X);
+  if (pad) {   // element by element out of the padded buffer (coalesced on the global side)
+    C* Ag = A + l0 * X;
+    for (int q = threadIdx.x; q < rows * X; q += blockDim.x) Ag[q] = r[P(q)];
+  } else {
+    tile_store(A + l0 * X, X, r, X, rows, X);
+  }
 }
 
 // pass 2 / 4: FFT along y.  Rows of `nin` input (index < nin), `nout` output rows written.
@@ -473,8 +494,10 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
   const int X = fd.n;
   C* tw = reinterpret_cast<C*>(smem_raw);
   C* b0 = tw + X;
-  C* b1 = b0 + X * nl;
-  XLine* li = reinterpret_cast<XLine*>(b1 + X * nl);
+  C* b1 = b0 + xpad_len<C>(X * nl);
+  XLine* li = reinterpret_cast<XLine*>(b1 + xpad_len<C>(X * nl));
+  const bool pad = x_static(X, nl) && blockDim.x == kPassThreads;   // the layout fft_x_lines uses
+  auto P = [&](int a) { return pad ? a + (a >> xpad_log<C>()) : a; };
   for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = twg[i];
   const int64_t l0 = (int64_t)blockIdx.x * nl;
   const int rows_valid = (nlines_total - l0 < nl) ? (int)(nlines_total - l0) : nl;
@@ -483,8 +506,13 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
   if constexpr (sizeof(T) == 4) {
     for (int line = threadIdx.x; line < nl; line += blockDim.x) sline[line] = to_c(scale[li[line].b], float2());
   }
-  tile_load(b0, X, A + l0 * X, X, nl, rows_valid, X, X);
-  cp_async_wait_all();
+  if (pad) {   // element by element into the padded buffer (rows past the last line read as zero)
+    const C* Ag = A + l0 * X;
+    for (int q = threadIdx.x; q < nl * X; q += blockDim.x) b0[P(q)] = q < rows_valid * X ? Ag[q] : czero<C>();
+  } else {
+    tile_load(b0, X, A + l0 * X, X, nl, rows_valid, X, X);
+    cp_async_wait_all();
+  }
   __syncthreads();
   C* r = fft_x_lines<+1>(b0, b1, tw, fd, nl);
   const bool p2 = (L & (L - 1)) == 0;
@@ -502,7 +530,7 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
     if constexpr (sizeof(T) == 4) {
       // complex64 product: the diagonal term in FP32 too (rounding ~1e-7, below the complex64
       // transform's own error), which keeps GB300's FP64 pipe to the conversions
-      const float2 conv = r[line * X + i];
+      const float2 conv = r[P(line * X + i)];
       const float2 sf = sline[line], zf = to_c(zz, float2()), xf = to_c(xj, float2());
       const float2 d = cmul(zf, xf);
       const float ckf = (float)ck;
@@ -511,7 +539,7 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
       o.y = fmaf(ckf, d.y, o.y);
       yout[b * ldy + c * nv + vid] = make_double2((double)o.x, (double)o.y);
     } else {
-      const double2 conv = to_d(r[line * X + i]);
+      const double2 conv = to_d(r[P(line * X + i)]);
       double2 out = cmul(scale[b], conv);
       out = cadd(out, cscale(cmul(zz, xj), ck));
       yout[b * ldy + c * nv + vid] = out;
@@ -574,7 +602,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
     const int64_t lines = (int64_t)ny * nz * 5 * B;
-    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C) + nl * sizeof(XLine);
+    const size_t sm = (size_t)(X + 2 * xpad_len<C>(X * nl)) * sizeof(C) + nl * sizeof(XLine);
     const unsigned grid = (unsigned)ceil_div(lines, nl);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_fwd_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_fwd_x<T><<<grid, kPassThreads, sm, st>>>(x, ldx, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, A, p.fx, twp[0], nl);
@@ -622,7 +650,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
     const int64_t lines = (int64_t)ny * nz * 5 * B;
-    const size_t sm = (size_t)(X + 2 * X * nl) * sizeof(C) + nl * (sizeof(XLine) + sizeof(float2));
+    const size_t sm = (size_t)(X + 2 * xpad_len<C>(X * nl)) * sizeof(C) + nl * (sizeof(XLine) + sizeof(float2));
     const unsigned grid = (unsigned)ceil_div(lines, nl);
     VH_CUDA_TRY(cudaFuncSetAttribute(k_inv_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_inv_x<T><<<grid, kPassThreads, sm, st>>>(A, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, x, ldx, y, ldy, scale, zdiag,

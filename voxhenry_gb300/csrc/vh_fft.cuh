@@ -236,7 +236,15 @@ __device__ __forceinline__ C* fft_stages_p2(C* src, C* dst, const C* tw, int es,
 // stride N; else line-interleaved, element stride NL and line stride 1) and NT threads fixed at
 // compile time, so each stage is a fixed number of unrolled rounds without bound checks.  The
 // arithmetic is that of the stages above.
-template <int R, int N, int NS, int NL, bool JF, int DIR, int NT, typename C>
+// PADLOG > 0: the buffers hold logical element a at a + (a >> PADLOG) (one padding element per
+// 2^PADLOG), which spreads a stage's strided stores over the banks.
+template <int PADLOG>
+__device__ __forceinline__ int pad_index(int a) {
+  if constexpr (PADLOG > 0) return a + (a >> PADLOG);
+  else return a;
+}
+
+template <int R, int N, int NS, int NL, bool JF, int DIR, int NT, int PADLOG, typename C>
 __device__ __forceinline__ void fft_stage_fixed(const C* __restrict__ src, C* __restrict__ dst, const C* __restrict__ tw) {
   constexpr int nb = N / R;
   constexpr int total = nb * NL;
@@ -254,7 +262,7 @@ __device__ __forceinline__ void fft_stage_fixed(const C* __restrict__ src, C* __
     const int base = line * LS;
     C v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = src[base + (j + r * nb) * ES];
+    for (int r = 0; r < R; ++r) v[r] = src[pad_index<PADLOG>(base + (j + r * nb) * ES)];
     if constexpr (NS > 1) {
       const int step = k * twmul;
 #pragma unroll
@@ -268,20 +276,20 @@ __device__ __forceinline__ void fft_stage_fixed(const C* __restrict__ src, C* __
     else dft8<DIR>(v);
     const int d0 = ((j >> logns) << (logns + ilog2c(R))) + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[base + (d0 + r * NS) * ES] = v[r];
+    for (int r = 0; r < R; ++r) dst[pad_index<PADLOG>(base + (d0 + r * NS) * ES)] = v[r];
   }
 }
 
-template <int N, int NS, int NL, bool JF, int DIR, int NT, typename C>
+template <int N, int NS, int NL, bool JF, int DIR, int NT, int PADLOG = 0, typename C>
 __device__ __forceinline__ C* fft_stages_fixed(C* src, C* dst, const C* tw) {
   if constexpr (NS >= N) {
     return src;
   } else {
     constexpr int rem = N / NS;
     constexpr int R = rem % 8 == 0 ? 8 : (rem % 4 == 0 ? 4 : 2);
-    fft_stage_fixed<R, N, NS, NL, JF, DIR, NT>(src, dst, tw);
+    fft_stage_fixed<R, N, NS, NL, JF, DIR, NT, PADLOG>(src, dst, tw);
     __syncthreads();
-    return fft_stages_fixed<N, NS * R, NL, JF, DIR, NT>(dst, src, tw);
+    return fft_stages_fixed<N, NS * R, NL, JF, DIR, NT, PADLOG>(dst, src, tw);
   }
 }
 
