@@ -227,6 +227,15 @@ __host__ __device__ __forceinline__ int tri_off(int c, int m) { return c * m - (
 constexpr int kLoadBatch = 4;   // independent global loads per thread per step of the load phases
 constexpr int kPanel = 4;       // pivots per panel of the fused front factorisation
 
+// a / d for 0 <= a < 2^24 and d >= 1, given rd = 1/d rounded to a float: the float estimate is
+// within one of the quotient (|a rd - a/d| < a/d * 2^-23), and the integer check corrects it
+__device__ __forceinline__ int div_small(int a, int d, float rd) {
+  int q = (int)((float)a * rd);
+  if (q * d > a) --q;
+  else if ((q + 1) * d <= a) ++q;
+  return q;
+}
+
 template <int NT>
 __device__ __forceinline__ void front_bar() {
   if constexpr (NT == 32)
@@ -254,6 +263,7 @@ __global__ void __launch_bounds__(NT)
   // shared-memory write (a column-by-column walk leaves one load in flight per thread).
   {
     const int nn = nf * nf;   // column-major nf x nf storage; the lower triangle is kept
+    const float rnf = __frcp_rn((float)nf);
     for (int base = tid; base < nn; base += kLoadBatch * NT) {
       T v[kLoadBatch];
       int off[kLoadBatch];
@@ -262,7 +272,7 @@ __global__ void __launch_bounds__(NT)
         const int idx = base + u * NT;
         off[u] = -1;
         if (idx < nn) {
-          const int k = idx / nf, i = idx - k * nf;
+          const int k = div_small(idx, nf, rnf), i = idx - k * nf;
           if (i >= k) {
             off[u] = tri_off(k, nf) - k + i;
             v[u] = F[idx];
@@ -286,6 +296,7 @@ __global__ void __launch_bounds__(NT)
     for (int a = tid; a < nb; a += NT) rms[a] = rm[a];
     front_bar<NT>();
     const int nn = nb * nb;
+    const float rnb = __frcp_rn((float)max(nb, 1));
     for (int base = tid; base < nn; base += kLoadBatch * NT) {
       T v[kLoadBatch];
       int off[kLoadBatch];
@@ -294,7 +305,7 @@ __global__ void __launch_bounds__(NT)
         const int idx = base + u * NT;
         off[u] = -1;
         if (idx < nn) {
-          const int b = idx / nb, a = idx - b * nb;
+          const int b = div_small(idx, nb, rnb), a = idx - b * nb;
           if (a >= b) {
             const int rb = rms[b];
             off[u] = tri_off(rb, nf) - rb + rms[a];
@@ -354,9 +365,11 @@ __global__ void __launch_bounds__(NT)
       front_bar<NT>();
       const int nk = P - q - 1;   // the panel's later columns jq+1 .. j+P-1 take this pivot now
       if (nk > 0) {
-        for (int t = tid; t < nk * nf; t += NT) {
-          const int k = jq + 1 + t / nf, i = t % nf;
-          if (i >= k) col(k)[i] = fma(-cq[i], cf[k - jq - 1], col(k)[i]);
+        for (int kk = 0; kk < nk; ++kk) {   // column by column, rows k.. only (no index division)
+          const int k = jq + 1 + kk;
+          T* ck = col(k);
+          const T cfk = cf[kk];
+          for (int i = k + tid; i < nf; i += NT) ck[i] = fma(-cq[i], cfk, ck[i]);
         }
         front_bar<NT>();
       }
