@@ -18,6 +18,21 @@ namespace vh {
 
 using ::fma;   // keep the FP64 / FP32 overloads visible next to the pair overload below
 
+// float -> double, exact, with integer operations: sign, exponent rebiased by 1023 - 127 and the
+// 23 fraction bits moved to the top of the 52 (GB300 runs the conversion instruction on its slow
+// FP64 pipe).  Zero, subnormal, infinite and NaN floats take the conversion instruction.
+__host__ __device__ __forceinline__ double f2d_exact(float f) {
+#ifdef __CUDA_ARCH__
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  if (e - 1u < 254u) {
+    const unsigned hw = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hw, (int)((u & 7u) << 29));
+  }
+#endif
+  return (double)f;
+}
+
 struct dfloat {
   float hi, lo;
   dfloat() = default;
@@ -26,7 +41,7 @@ struct dfloat {
   __host__ __device__ constexpr dfloat(int v) : hi((float)v), lo(0.0f) {}
   // nearest pair to a double: hi = rn(d), lo = rn(d - hi) (d - hi is exact in double)
   __host__ __device__ explicit dfloat(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
-  __host__ __device__ double to_double() const { return (double)hi + (double)lo; }
+  __host__ __device__ double to_double() const { return f2d_exact(hi) + f2d_exact(lo); }
 };
 
 struct dcomplex {
