@@ -343,7 +343,8 @@ def run_ours(args, rank, world):
                           "pair-arithmetic passes issue-bound on the FP32 pipes, the z-pass half of the call; "
                           "frac is against HBM with the algorithmic bytes of the two-pass pruned model")
     roof32 = fft_roofline(1, 8, "FFT circulant matvec, complex64 (inner GMRES matvecs; 5 passes)",
-                          "fft_matvec_c64_spiral.txt", "issue-bound passes (56-70 % issue active in ncu)")
+                          "fft_matvec_c64_spiral.txt", "passes bound by shared-memory traffic and issue (Stockham "
+                          "stages in shared memory; the register z-pass issue-bound)")
     # the preconditioner apply (double-float triangular solves and the SpMVs around them): per
     # RHS-apply the pair-precision factor is read once in each direction and the complex128 vectors
     # (input, output, the Schur part written and read) pass once
@@ -361,7 +362,8 @@ def run_ours(args, rank, world):
                  "algorithmic_bytes_per_launch": round(apply_bytes * units[4] / calls[4], 1),
                  "avg_rhs_per_launch": round(units[4] / calls[4], 2), "launches": int(calls[4]),
                  "avg_launch_ms": round(ms[4] / calls[4], 4), "share_of_step_time": round(ms[4] / step_ms_total, 4),
-                 "note": "leaf level at 1.9-2.4 TB/s, upper levels latency chains; nnz(L) = %d pair entries" % nnz_l}
+                 "note": "leaf level at 2.5-3 TB/s (partly issue-bound), upper levels latency chains; "
+                         "nnz(L) = %d pair entries" % nnz_l}
     # the dominant kernel group of the step is `roofline`; the others follow
     cands = [r for r in ((roofp, ms[4]), (roof32, ms[1]), (roof64, ms[0])) if r[0] is not None]
     cands.sort(key=lambda r: -r[1])
