@@ -75,18 +75,20 @@ def volume_volume_batch(W, pts, k0, r_m, dx):
     Yg = r_m[:, 1:2] + h * Y[None, :]
     Zg = r_m[:, 2:3] + h * Z[None, :]
     R = np.sqrt((Xg - h * Xp[None, :]) ** 2 + (Yg - h * Yp[None, :]) ** 2 + (Zg - h * Zp[None, :]) ** 2)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        ker = _kernel_far(R, k0)
     Xt, Yt, Zt = h * X, h * Y, h * Z
     Xpb, Ypb, Zpb = h * Xp, h * Yp, h * Zp
-    Wk = W[None, :] * ker
-    K1 = Wk.sum(axis=1) * J
-    K3 = (Wk * Xt[None, :]).sum(axis=1) * J
-    K5 = (Wk * Yt[None, :]).sum(axis=1) * J
-    K7 = (Wk * Zt[None, :]).sum(axis=1) * J
-    K8 = (Wk * (Xpb * Xt)[None, :]).sum(axis=1) * J
-    K9 = (Wk * (Ypb * Yt)[None, :]).sum(axis=1) * J
-    K10 = (Wk * (Zpb * Zt)[None, :]).sum(axis=1) * J
+    # a centre at the origin (the self cell) has coincident points (R = 0): its entries are not
+    # finite here and are replaced by the near-field values afterwards
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ker = _kernel_far(R, k0)
+        Wk = W[None, :] * ker
+        K1 = Wk.sum(axis=1) * J
+        K3 = (Wk * Xt[None, :]).sum(axis=1) * J
+        K5 = (Wk * Yt[None, :]).sum(axis=1) * J
+        K7 = (Wk * Zt[None, :]).sum(axis=1) * J
+        K8 = (Wk * (Xpb * Xt)[None, :]).sum(axis=1) * J
+        K9 = (Wk * (Ypb * Yt)[None, :]).sum(axis=1) * J
+        K10 = (Wk * (Zpb * Zt)[None, :]).sum(axis=1) * J
     # volume_volume.m:100-115
     return np.stack([K1, -K3, K5, K8 + K9, 2 * K7, K8 - K9, K8 + K9 + 4 * K10], axis=1)
 
