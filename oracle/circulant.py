@@ -102,12 +102,14 @@ def volume_volume_sym_batch(W, pts, k0, r_m, dx):
     Yg = r_m[:, 1:2] + h * Y[None, :]
     Zg = r_m[:, 2:3] + h * Z[None, :]
     R = np.sqrt((Xg - h * Xp[None, :]) ** 2 + (Yg - h * Yp[None, :]) ** 2 + (Zg - h * Zp[None, :]) ** 2)
+    # the self cell's coincident points (R = 0) give non-finite entries, replaced by the near-field
+    # values afterwards
     with np.errstate(divide="ignore", invalid="ignore"):
         ker = _kernel_far(R, k0)
-    Wk = W[None, :] * ker
-    K1 = Wk.sum(axis=1) * J
-    K2 = (Wk * (h * X)[None, :]).sum(axis=1) * J
-    K3 = (Wk * ((h * Xp) * (h * X))[None, :]).sum(axis=1) * J
+        Wk = W[None, :] * ker
+        K1 = Wk.sum(axis=1) * J
+        K2 = (Wk * (h * X)[None, :]).sum(axis=1) * J
+        K3 = (Wk * ((h * Xp) * (h * X))[None, :]).sum(axis=1) * J
     return np.stack([K1, K2, K3], axis=1)
 
 
