@@ -38,10 +38,12 @@ typedef enum vh_status {
 } vh_status;
 
 /* arithmetic of the FFT convolution: complex128, or complex64 with fp32 accumulation */
-/* VH_PREC_DF (vh_matvec / vh_matvec_device only): complex128 storage and FP64 x/y transforms with
- * the z-transform and tensor products in double-float (FP32 pairs, ~48 significant bits, relative
- * error ~1e-13) on GB300's FP32 pipes; no counterpart in the reference.  The mixed-precision
- * solver forms its refinement residual with it.                                                   */
+/* VH_PREC_DF (vh_matvec / vh_matvec_device only): the FFT passes and the tensor products in
+ * double-float (pairs of floats, ~48 significant bits, relative error ~1e-13) on GB300's FP32 pipes,
+ * the spectra stored as pairs between the passes; no counterpart in the reference.  Grids whose
+ * padded x or y length is not 256, 512 or 1024, whose z length has no register pass, or whose tensor
+ * spectrum is not real/imaginary per component, get the complex128 product instead.  The
+ * mixed-precision solver forms its refinement residual with it.                                   */
 typedef enum vh_prec { VH_PREC_FP64 = 0, VH_PREC_FP32 = 1, VH_PREC_DF = 2 } vh_prec;
 
 /* preconditioner kinds of lse_sparse_precon_prepare.m:5,71,83,90 ('schur_invert_original' is not provided) */
@@ -174,7 +176,8 @@ vh_status vh_precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const
  *      formed in FP64 after the first refinement step and then updated, r <- r - A d, with the complex64
  *      product of each (small) correction d, which keeps it within ~1e-6 |A d| (~1e-11 |b| at tol 1e-9)
  *      of the FP64 residual.  iter then counts inner iterations / cycles summed over refinement steps;
- *      resvec holds that relative residual after each step, relres its last value.              */
+ *      resvec holds that relative residual after each step, relres its last value.  The inner
+ *      GMRES keeps its Krylov basis in complex128 and runs its Gram-Schmidt sums in double-float.  */
 vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
                    int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
                    double* relres, int* iter, double* resvec, int resvec_len, int* nres);
