@@ -525,7 +525,7 @@ def run_probe(args):
         st = (1j * 2 * np.pi * w.freqs[:B] * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
         pcs = g.precons(st, np.zeros(B, dtype=np.int32), kind=args.probe_kind)
         parr = (C.c_void_p * B)(*[p.handle for p in pcs])
-        if args.probe == "gmres":   # one restart cycle of the mixed-precision inner GMRES (no refinement)
+        if args.probe == "gmres":   # one restart cycle of FP64 GMRES (the FP64 Gram-Schmidt kernels)
             tol = np.full(B, 1e-30)
             flag = np.zeros(B, dtype=np.int32)
             it = np.zeros(2 * B, dtype=np.int32)
