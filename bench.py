@@ -1,14 +1,22 @@
 """Benchmark: frequency points per second of the batched VIE sweep on one GB300.
 
-Workload (the batched configuration of the reference's solve path): 4-turn square spiral coil on a
-256 x 256 x 8 voxel grid (1 um voxels, 5 um trace, 4 voxels thick, 2 um turn spacing,
-sigma = 5.8e7 S/m), one port across the spiral ends, 32 frequencies log-spaced 1 MHz - 20 GHz,
-solved as 32 right-hand sides in one batch (GMRES tol 1e-9, restart 50).  A step is one sweep:
-the Schur-complement factorisation of every frequency plus the batched Krylov solve and the
-R, L extraction.  The circulant tensor, Ae and the symbolic analysis are set up once before the
-timed region (resident in HBM).
+Headline workload (the largest single-GPU configuration, mixed precision): single-turn circular
+ring coil on a 512 x 512 x 16 voxel grid (padded FFT grid 1024 x 1024 x 32), 1 um voxels, radius
+150 um, 10 x 10 um square cross-section voxelised by a centre-in-ring test, sigma = 5.8e7 S/m, one
+port across a 2 um gap, 16 frequencies log-spaced 1 MHz - 20 GHz solved as 16 right-hand sides in
+one batch.  A step is one sweep: the Schur-complement factorisation of every frequency plus the
+batched Krylov solve and the R, L extraction.  The circulant tensor, Ae and the symbolic analysis
+are set up once before the timed region (resident in HBM).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+The other configurations are reported under "configs" with the same measurement:
+  C1 straight bar 64 x 16 x 16 (0.5 um voxels, 8 frequencies 1 kHz - 10 GHz; plain FP64 at GMRES
+     tol 1e-8, restart 50 -- its own settings -- and both paths at the common tolerance);
+  C2 square spiral 256 x 256 x 8 (32 frequencies 1 MHz - 20 GHz);
+  C3 two parallel bars 128 x 64 x 32, copper and aluminium (2 ports x 16 frequencies 1 kHz - 10 GHz).
+Every configuration's R and L (and the current density x) are compared with the oracle's values
+committed in tests/golden/config_<workload>.npz (FP64 reference path converged to tol 1e-12).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--configs C1,C2,C3]
 
 value  = mixed precision (complex64 FFT matvec inside FP64 refinement), inputs on the device.
 e2e    = the same through the host-buffer C ABI call (vh_gmres), copies included.
@@ -29,14 +37,14 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 
 import numpy as np  # noqa: E402
 
 METRIC = "freq-points/s, mixed-prec batched vs plain FP64 on GB300 @1e-6 R,L; p50/p99 lat"
 UNIT = "freq-points/s"
-# GMRES tolerance: the loosest that keeps R and L within 1e-6 of the converged solution for both the
-# FP64 and the mixed path on this workload (tol 1e-8 leaves 3.8e-6 (FP64) / 5.1e-6 (mixed) in R, L;
-# tol 1e-9 leaves 4.0e-7 / 7.6e-7, measured against a tol-1e-12 FP64 solve)
+# GMRES tolerance of the mixed and the FP64 path: the loosest that keeps R and L within 1e-6 of the
+# oracle's converged values on these workloads (tol 1e-8 leaves up to ~5e-6 in R, L)
 TOL = 1e-9
 RESTART = 50
 MAXIT = 10
@@ -44,8 +52,24 @@ MAXIT = 10
 # GB300's FP32 pipes; its FP64 refinement residuals set the final accuracy
 MIXED_PRECON = "schur_invert_df"
 # factor sharing between neighbouring frequencies for the separately reported variant: A_inv (hence S)
-# within 1e-4 of the group's factor; on this sweep it halves the factors at unchanged iteration counts
+# within 1e-4 of the group's factor
 SHARE_TOL = 1e-4
+
+CONFIGS = {
+    "C1": {"workload": "bar_64x16x16", "own_tol": 1e-8,
+           "text": "straight copper bar, grid 64x16x16 (padded FFT grid 128x32x32), voxel 0.5 um, all voxels "
+                   "sigma 5.8e7 S/m, port x=0 face to x=end face, 8 freqs 1 kHz-10 GHz log"},
+    "C2": {"workload": "square_spiral_256x256x8",
+           "text": "square spiral coil, 4 turns, grid 256x256x8 (padded FFT grid 512x512x16), voxel 1 um, "
+                   "trace 5 um x 4 voxels, spacing 2 um, sigma 5.8e7 S/m, 1 port, 32 freqs 1 MHz-20 GHz log"},
+    "C3": {"workload": "two_bars_128x64x32",
+           "text": "two parallel bars 100x10x10 voxels (copper 5.8e7, aluminium 3.5e7 S/m), 20-voxel gap, grid "
+                   "128x64x32 (padded FFT grid 256x128x64), voxel 1 um, 2 ports x 16 freqs 1 kHz-10 GHz log"},
+    "C4": {"workload": "ring_512x512x16",
+           "text": "circular ring coil, radius 150 um, 10x10 um cross-section, grid 512x512x16 (padded FFT grid "
+                   "1024x1024x32), voxel 1 um, sigma 5.8e7 S/m, 1 port across a 2 um gap, 16 freqs 1 MHz-20 GHz log"},
+}
+HEADLINE = "C4"
 
 
 def dist_env():
@@ -55,20 +79,19 @@ def dist_env():
     return rank, world, local
 
 
-def workload():
+def workload(cid):
     from voxhenry_gb300 import geometry
 
-    w = geometry.square_spiral()
+    w = geometry.WORKLOADS[CONFIGS[cid]["workload"]]()
+    L, M, N = w.shape
     cfg = {
-        "workload": "square spiral coil, 4 turns, grid 256x256x8 (padded FFT grid 512x512x16), voxel 1 um, "
-                    "trace 5 um x 4 voxels, spacing 2 um, sigma 5.8e7 S/m, 1 port, 32 freqs 1 MHz-20 GHz log",
-        "grid": [256, 256, 8],
-        "voxels": int((w.sigma_e > 0).sum()),
-        "rhs_per_step": len(w.freqs),
+        "workload": CONFIGS[cid]["text"], "config_id": cid, "grid": [L, M, N], "fft_grid": [2 * L, 2 * M, 2 * N],
+        "voxels": int((w.sigma_e > 0).sum()), "ports": len(w.pnt_lft), "freqs": len(w.freqs),
+        "rhs_per_step": len(w.freqs) * len(w.pnt_lft),
         "gmres": {"tol": TOL, "restart": RESTART, "maxit": MAXIT, "preconditioner": "schur_invert (left)",
                   "schur_factor": {"mixed": "double-float (FP32 pairs)", "fp64": "fp64"}},
-        "l2": "per-RHS vectors (~9.6 MB complex128 each) x 32 RHS and the 470 MB complex128 tensor exceed "
-              "the 129 MB L2; no flush needed",
+        "l2": "inputs larger than L2: per-RHS vectors of n complex128 and the tensor spectrum (>= 7 x 2L x 2M x 2N "
+              "values) per step exceed the 129 MB L2 at C2-C4; C1's working set is re-read from L2 (no flush)",
     }
     return w, cfg
 
@@ -126,8 +149,8 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def conv_traffic_from_profile(name, key="dram_bytes_per_rhs_matvec"):
-    """DRAM bytes per RHS (matvec or preconditioner apply) from a committed ncu summary."""
+def profile_figure(name, key):
+    """A per-unit figure (DRAM bytes per RHS-matvec or per RHS-apply) from a committed ncu summary."""
     p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
@@ -146,106 +169,129 @@ def fft_algorithmic_bytes_per_rhs(nv, L, M, N, s, st, B):
     return s * (10 * nv) + s * (4 * 5 * 4 * lmn) + st * 7 * 8 * lmn / B
 
 
+def fixture_accuracy(cid, freqs, R, L, X=None, nc=None):
+    """Max relative R, L error (and the current density's) against the oracle fixture, at the
+    fixture's frequencies; X: the (F*P, n) solutions of the sweep (host), or None."""
+    import config_fixtures as cf
+
+    name = CONFIGS[cid]["workload"]
+    if not os.path.exists(cf.path(name)):
+        return {"reference": f"missing fixture tests/golden/config_{name}.npz"}
+    fx = cf.load(name)
+    fi = fx["freq_idx"]
+    P = int(fx["ports"])
+
+    def err(a, b):   # per frequency, relative to the largest entry of the port matrix
+        return float(max(np.abs(a[k] - b[k]).max() / np.abs(b[k]).max() for k in range(b.shape[0])))
+
+    out = {"reference": f"oracle (FP64 reference path, GMRES tol {float(fx['tol']):g}) at {len(fi)} of "
+                        f"{len(freqs)} frequencies: tests/golden/config_{name}.npz",
+           "max_rel_err_R": err(R[fi], fx["R"]), "max_rel_err_L": err(L[fi], fx["L"])}
+    if X is not None:
+        rows = np.concatenate([np.arange(k * P, (k + 1) * P) for k in fi])
+        d = cf.compare(X[rows], nc, fx)
+        out["max_rel_err_current_density"] = d["curr_sketch"]
+        out["max_rel_err_potentials"] = d["phi_sketch"]
+        out["x_note"] = "relative 2-norm difference of x estimated by a 64-row Gaussian sketch (about +-25 %)"
+    return out
+
+
 # ---------------------------------------------------------------------------------------------- ours
-def run_ours(args, rank, world):
-    import torch
+class ConfigRunner:
+    """One configuration's device-resident sweep (geometry, RHS, buffers) and its timed steps."""
 
-    import __graft_entry__
+    def __init__(self, cid, args, world):
+        import torch
 
-    __graft_entry__.build()
-    from voxhenry_gb300 import _lib, executer, structure, vie
+        from voxhenry_gb300 import _lib, executer, structure
 
-    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
-    w, cfg = workload()
-    if args.mixed_precon != MIXED_PRECON:
-        cfg["gmres"]["schur_factor"]["mixed"] = "fp64"
-    prob = structure.problem_from_workload(w)
-    freqs = w.freqs
-    sw = executer.Sweep(prob, freqs, want_fp32=True)
-    g = sw.geom
-    lib = g.ctx._lib
-    stream = torch.cuda.ExternalStream(lib.vh_ctx_stream(g.ctx.handle))
-    F = len(freqs)
-    B = F * prob.num_ports
-    n = g.n
-    rhs = prob.rhs.astype(np.complex128)
-    b_host = np.ascontiguousarray(np.stack([rhs[:, p] for f in range(F) for p in range(prob.num_ports)]))
-    scale = np.ascontiguousarray(np.repeat(1j * 2 * np.pi * freqs * executer.MU0, prob.num_ports))
-    zsl = np.ascontiguousarray(np.repeat(sw.zslot, prob.num_ports).astype(np.int32))
-    tolv = np.full(B, TOL)
-    b_dev = torch.from_numpy(b_host.view(np.float64)).cuda()
-    x_dev = torch.empty_like(b_dev)
-    rhs_dev = torch.from_numpy(prob.rhs.astype(np.float64)).cuda()
-    ip = C.POINTER(C.c_int)
-    flag = np.zeros(B, dtype=np.int32)
-    relres = np.zeros(B)
-    iters = np.zeros(2 * B, dtype=np.int32)
-    nres = np.zeros(B, dtype=np.int32)
+        self.cid, self.args, self.world = cid, args, world
+        self.torch, self._lib, self.executer = torch, _lib, executer
+        self.w, self.cfg = workload(cid)
+        prob = structure.problem_from_workload(self.w)
+        self.prob = prob
+        self.freqs = self.w.freqs
+        self.sw = executer.Sweep(prob, self.freqs, want_fp32=True)
+        g = self.g = self.sw.geom
+        self.lib = g.ctx._lib
+        self.stream = torch.cuda.ExternalStream(self.lib.vh_ctx_stream(g.ctx.handle))
+        F, P = len(self.freqs), prob.num_ports
+        self.F, self.P, self.B, self.n = F, P, F * P, g.n
+        rhs = prob.rhs.astype(np.complex128)
+        self.b_host = np.ascontiguousarray(np.stack([rhs[:, p] for f in range(F) for p in range(P)]))
+        self.scale = np.ascontiguousarray(np.repeat(1j * 2 * np.pi * self.freqs * executer.MU0, P))
+        self.zsl = np.ascontiguousarray(np.repeat(self.sw.zslot, P).astype(np.int32))
+        self.b_dev = torch.from_numpy(self.b_host.view(np.float64)).cuda()
+        self.x_dev = torch.empty_like(self.b_dev)
+        self.rhs_dev = torch.from_numpy(prob.rhs.astype(np.float64)).cuda()
+        self.flag = np.zeros(self.B, dtype=np.int32)
+        self.relres = np.zeros(self.B)
+        self.iters = np.zeros(2 * self.B, dtype=np.int32)
+        self.nres = np.zeros(self.B, dtype=np.int32)
+        self.st_all = (1j * 2 * np.pi * self.freqs * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
+        # entries of the Schur factor (for the preconditioner's algorithmic bytes); also builds the
+        # symbolic analysis before the timed region, as the warm-up would
+        pc = g.precons(self.st_all[:1], self.sw.zslot[:1], kind=MIXED_PRECON)
+        self.nnz_l = int(pc[0].stats()["nnz_factor"])
+        pc[0].close()
+        self.share_rep = None
 
-    st_all = (1j * 2 * np.pi * freqs * executer.MU0)[:, None] * np.asarray(prob.st2)[None, :]
-    # entries of the Schur factor (for the preconditioner's algorithmic bytes); builds the symbolic
-    # analysis before the timed region, as the warm-up would
-    _pc = g.precons(st_all[:1], sw.zslot[:1], kind=args.mixed_precon)
-    nnz_l = int(_pc[0].stats()["nnz_factor"])
-    _pc[0].close()
+    def precon_kind(self, prec):
+        return self.args.mixed_precon if prec == "fp32" else "schur_invert"
 
-    def precon_kind(prec):
-        return args.mixed_precon if prec == "fp32" else "schur_invert"
+    def share_groups(self, tol):
+        ex = self.executer
+        return ex.factor_share_groups([ex.a_inv_classes(self.prob, f) for f in self.freqs], tol)
 
-    # factor sharing between neighbouring frequencies: reported as a separate line of the JSON unless
-    # --share-tol asks for it in the headline mixed path
-    def share_groups(tol):
-        return executer.factor_share_groups([executer.a_inv_classes(prob, f) for f in freqs], tol)
-
-    share_rep = np.arange(F)
-    if args.share_tol is not None:
-        share_rep = share_groups(args.share_tol)
-        cfg["factor_sharing"] = {"share_tol": args.share_tol, "factors_per_step": int(len(np.unique(share_rep)))}
-
-    def device_step(prec, tol=None, maxit=MAXIT, rep=None):
+    def device_step(self, prec, tol=TOL, maxit=MAXIT, rep=None):
         """One sweep with device-resident inputs: factors + batched solve + R, L."""
-        if rep is None:
-            rep = share_rep if prec == "fp32" else np.arange(F)
+        torch, _lib, g = self.torch, self._lib, self.g
+        F, P, B, n = self.F, self.P, self.B, self.n
+        rep = np.arange(F) if rep is None else rep
         reps = np.unique(rep)
-        made = g.precons(st_all[reps], sw.zslot[reps], kind=precon_kind(prec))
+        made = g.precons(self.st_all[reps], self.sw.zslot[reps], kind=self.precon_kind(prec))
         by_rep = dict(zip(reps.tolist(), made))
         pcs = [by_rep[int(r)] for r in rep]
-        parr = (C.c_void_p * B)(*[pcs[k // prob.num_ports].handle for k in range(B)])
-        tv = tolv if tol is None else np.full(B, tol)
-        st = lib.vh_gmres_device(g.handle, B, parr, C.c_void_p(b_dev.data_ptr()), _lib.cview(scale),
-                                 zsl.ctypes.data_as(ip), RESTART, _lib.dptr(tv), maxit, 0, _lib.PREC[prec],
-                                 C.c_void_p(x_dev.data_ptr()), flag.ctypes.data_as(ip), _lib.dptr(relres),
-                                 iters.ctypes.data_as(ip), None, 0, nres.ctypes.data_as(ip))
+        parr = (C.c_void_p * B)(*[pcs[k // P].handle for k in range(B)])
+        tv = np.full(B, tol)
+        ip = C.POINTER(C.c_int)
+        st = self.lib.vh_gmres_device(g.handle, B, parr, C.c_void_p(self.b_dev.data_ptr()), _lib.cview(self.scale),
+                                      self.zsl.ctypes.data_as(ip), RESTART, _lib.dptr(tv), maxit, 0, _lib.PREC[prec],
+                                      C.c_void_p(self.x_dev.data_ptr()), self.flag.ctypes.data_as(ip),
+                                      _lib.dptr(self.relres), self.iters.ctypes.data_as(ip), None, 0,
+                                      self.nres.ctypes.data_as(ip))
         _lib.check(st, g.ctx.handle)
-        with torch.cuda.stream(stream):
-            xc = torch.view_as_complex(x_dev.view(B, n, 2))
-            Y = torch.einsum("bn,np->bp", xc, rhs_dev.to(torch.complex128))   # Y(:, p) = sum rhs .* x
-            Yh = Y.cpu().numpy().reshape(F, prob.num_ports, prob.num_ports).transpose(0, 2, 1)
+        with torch.cuda.stream(self.stream):
+            xc = torch.view_as_complex(self.x_dev.view(B, n, 2))
+            Y = torch.einsum("bn,np->bp", xc, self.rhs_dev.to(torch.complex128))   # Y(:, p) = sum rhs .* x
+            Yh = Y.cpu().numpy().reshape(F, P, P).transpose(0, 2, 1)
         Z = np.linalg.inv(Yh)
         for p in made:
             p.close()
-        return np.abs(Z.real), np.abs(Z.imag) / (2 * np.pi * freqs)[:, None, None], iters[0::2].copy()
+        return np.abs(Z.real), np.abs(Z.imag) / (2 * np.pi * self.freqs)[:, None, None], self.iters[0::2].copy()
 
-    def timed(prec, steps, warm, profile=False, rep=None):
+    def x_host(self):
+        return self.x_dev.cpu().numpy().view(np.complex128).reshape(self.B, self.n)
+
+    def timed(self, prec, steps, warm, profile=False, rep=None, tol=TOL):
+        torch, lib = self.torch, self.lib
         for _ in range(warm):
-            device_step(prec, rep=rep)
-        if world > 1:
+            self.device_step(prec, rep=rep, tol=tol)
+        if self.world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         if profile:
-            _lib.check(lib.vh_ctx_profile(g.ctx.handle, 1), g.ctx.handle)
+            self._lib.check(lib.vh_ctx_profile(self.g.ctx.handle, 1), self.g.ctx.handle)
         l0 = lib.vh_launch_count()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.nvtx.range_push(f"timed_{prec}")
-        e0.record(stream)
+        e0.record(self.stream)
         t0 = time.perf_counter()
         out = None
         for _ in range(steps):
-            out = device_step(prec, rep=rep)
-        e1.record(stream)
+            out = self.device_step(prec, rep=rep, tol=tol)
+        e1.record(self.stream)
         torch.cuda.synchronize()
-        torch.cuda.nvtx.range_pop()
         wall = time.perf_counter() - t0
         launches = lib.vh_launch_count() - l0
         prof = None
@@ -253,161 +299,203 @@ def run_ours(args, rank, world):
             ms = np.zeros(7)
             calls = np.zeros(7, dtype=np.int64)
             units = np.zeros(7, dtype=np.int64)
-            _lib.check(lib.vh_ctx_profile_read(g.ctx.handle, _lib.dptr(ms), calls.ctypes.data_as(C.POINTER(C.c_int64)),
-                                               units.ctypes.data_as(C.POINTER(C.c_int64)), 7), g.ctx.handle)
-            _lib.check(lib.vh_ctx_profile(g.ctx.handle, 0), g.ctx.handle)
+            self._lib.check(lib.vh_ctx_profile_read(self.g.ctx.handle, self._lib.dptr(ms),
+                                                    calls.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                    units.ctypes.data_as(C.POINTER(C.c_int64)), 7), self.g.ctx.handle)
+            self._lib.check(lib.vh_ctx_profile(self.g.ctx.handle, 0), self.g.ctx.handle)
             prof = (ms, calls, units)
-        ev_ms = e0.elapsed_time(e1)
         # the host waits for the device inside every step, so device time == wall time of the region
-        t = max(ev_ms / 1e3, wall)
-        if world > 1:
+        t = max(e0.elapsed_time(e1) / 1e3, wall)
+        if self.world > 1:
             tt = torch.tensor([t], device="cuda")
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             t = float(tt.item())
         return t, out, launches, prof
 
-    if args.mixed_only:      # profiling aid: only the warm-up and timed mixed-precision steps
-        timed("fp32", args.steps, args.warmup)
-        return
-    # accuracy reference: the FP64 GPU path converged to 1e-12 (untimed); the FP64 GPU path matches
-    # the oracle to 1e-9 in the parity tests
-    R_t, L_t, _ = device_step("fp64", tol=1e-12, maxit=40)
-    clocks = ClockSampler(0)
-    # warm-up + timed, mixed precision (headline) with live section timing
-    clocks.start()
-    t_mixed, out_mixed, launches, prof = timed("fp32", args.steps, args.warmup, profile=True)
-    clk = clocks.stop()
-    # plain FP64 GPU path on the same workload
-    t_fp64, out_fp64, _, _ = timed("fp64", args.steps, args.warmup)
-    # the mixed path with one factor per group of neighbouring frequencies (A_inv within 1e-4)
-    shared = None
-    if args.share_tol is None:
-        rep_s = share_groups(SHARE_TOL)
-        t_sh, out_sh, _, _ = timed("fp32", args.steps, args.warmup, rep=rep_s)
-        shared = (rep_s, t_sh, out_sh)
-    # e2e: the host-buffer C ABI call a user makes (Sweep -> vh_gmres), copies inside the region
-    sw.pcs = None
-    sw.precon_kind = precon_kind("fp32")
-    for _ in range(args.warmup):
-        sw.prepare(share_tol=args.share_tol).solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_out = None
-    for _ in range(args.steps):
+    def rooflines(self, prof, step_ms_total):
+        """Roofline entries of the kernel groups of the mixed step (section times: CUDA events on the
+        library's stream), dominant first."""
+        ms, calls, units = prof
+        peak, peak_kind = measured_hbm_peak()
+        prob, wl = self.prob, CONFIGS[self.cid]["workload"]
+
+        def fft_roofline(sec, s, st, label, prof_name, note):
+            if calls[sec] == 0:
+                return None
+            avg_b = units[sec] / calls[sec]
+            per_rhs = fft_algorithmic_bytes_per_rhs(prob.idxS.size, prob.L, prob.M, prob.N, s, st, avg_b)
+            achieved = per_rhs * units[sec] / (ms[sec] / 1e3) / 1e9
+            traffic = profile_figure(prof_name, "dram_bytes_per_rhs_matvec")
+            return {"kernel": label, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                    "traffic": None if traffic is None else round(traffic * avg_b, 1),
+                    "traffic_source": f"profiles/{prof_name} (ncu, per RHS-matvec x RHS per launch)",
+                    "algorithmic_bytes_per_launch": round(per_rhs * avg_b, 1),
+                    "avg_rhs_per_launch": round(avg_b, 2), "launches": int(calls[sec]),
+                    "avg_launch_ms": round(ms[sec] / calls[sec], 4),
+                    "share_of_step_time": round(ms[sec] / step_ms_total, 4), "note": note}
+
+        r_df = fft_roofline(0, 16, 16, "FFT circulant matvec in double-float (refinement residuals, VH_PREC_DF: all 5 "
+                            "passes in pair arithmetic)", f"fft_matvec_df_{wl}.txt",
+                            "frac against HBM with the algorithmic bytes of the two-pass pruned model")
+        r_c64 = fft_roofline(1, 8, 4, "FFT circulant matvec, complex64 (inner GMRES matvecs; 5 passes, real/imaginary "
+                             "tensor: 4 bytes per component)", f"fft_matvec_c64_{wl}.txt",
+                             "frac against HBM with the algorithmic bytes of the two-pass pruned model")
+        r_p = None
+        if calls[4]:
+            apply_bytes = 2 * self.nnz_l * 8 + 16 * 4 * self.n
+            achieved = apply_bytes * units[4] / (ms[4] / 1e3) / 1e9
+            traffic = profile_figure(f"schur_precon_df_{wl}.txt", "dram_bytes_per_rhs_apply")
+            r_p = {"kernel": "Schur preconditioner apply (double-float triangular solves and the SpMVs around them)",
+                   "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                   "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                   "traffic": round(traffic * units[4] / calls[4], 1) if traffic else None,
+                   "traffic_source": f"profiles/schur_precon_df_{wl}.txt (ncu, per RHS-apply x RHS per launch)",
+                   "algorithmic_bytes_per_launch": round(apply_bytes * units[4] / calls[4], 1),
+                   "avg_rhs_per_launch": round(units[4] / calls[4], 2), "launches": int(calls[4]),
+                   "avg_launch_ms": round(ms[4] / calls[4], 4), "share_of_step_time": round(ms[4] / step_ms_total, 4),
+                   "note": "per RHS-apply: the pair factor read once per direction (2 x nnz(L) x 8 B) plus four "
+                           "complex128 vector passes; nnz(L) = %d" % self.nnz_l}
+        cands = [r for r in ((r_p, ms[4]), (r_c64, ms[1]), (r_df, ms[0])) if r[0] is not None]
+        cands.sort(key=lambda r: -r[1])
+        return [c[0] for c in cands]
+
+    def run(self, steps, warm, fp64_steps, profile=True, clocks=None):
+        """Timed mixed and FP64 sweeps plus accuracy against the oracle fixture."""
+        args = self.args
+        if clocks:
+            clocks.start()
+        t_m, out_m, launches, prof = self.timed("fp32", steps, warm, profile=profile)
+        clk = clocks.stop() if clocks else None
+        X_m = self.x_host()
+        t_d, out_d, _, _ = self.timed("fp64", fp64_steps, min(warm, 3))
+        X_d = self.x_host()
+        R_m, L_m, it_m = out_m
+        R_d, L_d, it_d = out_d
+        pts_m = steps * self.F * self.world
+        pts_d = fp64_steps * self.F * self.world
+        sections = None
+        roofs = []
+        if prof is not None:
+            ms, calls, units = prof
+            sections = {name: {"ms": round(float(ms[i]), 3), "calls": int(calls[i]), "rhs": int(units[i])}
+                        for i, name in enumerate(["fft_conv_df", "fft_conv_c64", "incidence_spmv", "schur_factor",
+                                                  "precon_apply", "krylov_vectors", "tensor"])}
+            roofs = self.rooflines(prof, 1e3 * t_m)
+        res = {
+            "workload": self.cfg["workload"], "value": round(pts_m / t_m, 4), "unit": UNIT,
+            "steps": steps, "warmup": warm, "ms_per_step": round(1e3 * t_m / steps, 3),
+            "fp64": {"value": round(pts_d / t_d, 4), "steps": fp64_steps, "ms_per_step": round(1e3 * t_d / fp64_steps, 3),
+                     "dtype": "f64 (complex128 FFT matvec, FP64 factor, solves and Krylov)"},
+            "mixed_over_fp64": round((pts_m / t_m) / (pts_d / t_d), 3),
+            "accuracy": {"mixed": fixture_accuracy(self.cid, self.freqs, R_m, L_m, X_m, self.prob.Ar.shape[1]),
+                         "fp64": fixture_accuracy(self.cid, self.freqs, R_d, L_d, X_d, self.prob.Ar.shape[1]),
+                         "bar": 1e-6,
+                         "gmres_iterations_mixed_total": int(it_m.sum()),
+                         "gmres_iterations_fp64_total": int(it_d.sum()),
+                         "iterations_note": "inner GMRES iterations summed over RHS (mixed: over refinement steps)"},
+            "gpu_launches": int(launches),
+        }
+        if sections is not None:
+            res["sections_ms"] = sections
+            res["matvecs_per_s"] = {
+                "complex64": round(sections["fft_conv_c64"]["rhs"] / max(1e-9, sections["fft_conv_c64"]["ms"] / 1e3), 1),
+                "double_float": round(sections["fft_conv_df"]["rhs"] / max(1e-9, sections["fft_conv_df"]["ms"] / 1e3), 1),
+                "note": "one RHS-matvec = the full operator of lse_matvect_mult.m on one vector (section timing of "
+                        "the mixed step)"}
+            res["roofline"] = roofs[0] if roofs else None
+            res["roofline_other"] = roofs[1:]
+        if clk is not None:
+            res["clocks"] = clk
+        own_tol = CONFIGS[self.cid].get("own_tol")
+        if own_tol is not None:   # the configuration's own GMRES settings (plain FP64)
+            t_o, out_o, _, _ = self.timed("fp64", fp64_steps, 1, tol=own_tol)
+            R_o, L_o, it_o = out_o
+            res["fp64_own_settings"] = {
+                "tol": own_tol, "restart": RESTART, "maxit": MAXIT, "value": round(pts_d / t_o, 4),
+                "ms_per_step": round(1e3 * t_o / fp64_steps, 3), "gmres_iterations_total": int(it_o.sum()),
+                "accuracy": fixture_accuracy(self.cid, self.freqs, R_o, L_o, self.x_host(), self.prob.Ar.shape[1])}
+        if args.share_tol is not None or self.cid == HEADLINE:
+            stol = SHARE_TOL if args.share_tol is None else args.share_tol
+            rep = self.share_groups(stol)
+            t_s, (R_s, L_s, it_s), _, _ = self.timed("fp32", steps, 1, rep=rep)
+            res["factor_sharing"] = {
+                "share_tol": stol, "factors_per_step": int(len(np.unique(rep))), "value": round(pts_m / t_s, 4),
+                "ms_per_step": round(1e3 * t_s / steps, 3), "gmres_iterations_total": int(it_s.sum()),
+                "accuracy": fixture_accuracy(self.cid, self.freqs, R_s, L_s),
+                "note": "mixed path with one Schur factor per group of neighbouring frequencies whose A_inv differs "
+                        "by at most share_tol (Sweep.prepare(share_tol)); the headline factors every frequency"}
+        return res
+
+    def e2e(self, steps, warm):
+        """The host-buffer C ABI call a user makes (Sweep -> vh_gmres), copies inside the region."""
+        sw = self.sw
         sw.pcs = None
-        # the previous result is released first, as a caller that keeps no earlier sweep does: its
-        # page-locked x block then returns to the host cache and is reused instead of pinning anew
-        e2e_out = None
-        e2e_out = sw.prepare(share_tol=args.share_tol).solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
-    t_e2e = time.perf_counter() - t0
+        sw.precon_kind = self.precon_kind("fp32")
+        for _ in range(warm):
+            sw.prepare().solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
+        self.torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = None
+        for _ in range(steps):
+            sw.pcs = None
+            # the previous result is released first, as a caller that keeps no earlier sweep does: its
+            # page-locked x block then returns to the host cache and is reused instead of pinning anew
+            out = None
+            out = sw.prepare().solve(restart=RESTART, tol=TOL, maxit=MAXIT, prec="fp32")
+        t = time.perf_counter() - t0
+        return {"value": round(steps * self.F * self.world / t, 4), "unit": UNIT,
+                "h2d_bytes_per_step": int(self.b_host.nbytes + self.scale.nbytes + 16 * self.B),
+                "d2h_bytes_per_step": int(self.b_host.nbytes),
+                "accuracy": fixture_accuracy(self.cid, self.freqs, out["R"], out["L"])}
 
-    R_m, L_m, it_m = out_mixed
-    R_d, L_d, it_d = out_fp64
+    def close(self):
+        self.sw.pcs = None
+        self.g.close()
 
-    def rl_err(R, L):
-        return float(np.max(np.abs(R - R_t) / np.abs(R_t))), float(np.max(np.abs(L - L_t) / np.abs(L_t)))
 
-    err_R, err_L = rl_err(R_m, L_m)
-    err_R64, err_L64 = rl_err(R_d, L_d)
-    err_e2e = max(rl_err(e2e_out["R"], e2e_out["L"]))
-    pts = args.steps * F * world
-    value = pts / t_mixed
-    # roofline of the FFT matvec kernel groups (section times: CUDA events on the library stream)
-    ms, calls, units = prof
-    peak, peak_kind = measured_hbm_peak()
-    sections = {name: {"ms": round(float(ms[i]), 3), "calls": int(calls[i]), "rhs": int(units[i])}
-                for i, name in enumerate(["fft_conv_df", "fft_conv_c64", "incidence_spmv", "schur_factor",
-                                          "precon_apply", "krylov_vectors", "tensor"])}
-    step_ms_total = 1e3 * t_mixed
-    dominant = max(sections, key=lambda k: sections[k]["ms"])
+def run_ours(args, rank, world):
+    import torch
 
-    def fft_roofline(sec, s, label, profile_name, note):
-        conv_ms, conv_calls, conv_rhs = ms[sec], calls[sec], units[sec]
-        if conv_calls == 0:
-            return None
-        avg_b = conv_rhs / conv_calls
-        bytes_per_rhs = fft_algorithmic_bytes_per_rhs(prob.idxS.size, prob.L, prob.M, prob.N, s, s, avg_b)
-        achieved = bytes_per_rhs * conv_rhs / (conv_ms / 1e3) / 1e9
-        traffic = conv_traffic_from_profile(profile_name)
-        return {"kernel": label, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "traffic": None if traffic is None else round(traffic * avg_b, 1),
-                "traffic_source": f"profiles/{profile_name} (ncu, 4-RHS launch, scaled per RHS)",
-                "algorithmic_bytes_per_launch": round(bytes_per_rhs * avg_b, 1),
-                "avg_rhs_per_launch": round(avg_b, 2), "launches": int(conv_calls),
-                "avg_launch_ms": round(conv_ms / conv_calls, 4),
-                "share_of_step_time": round(conv_ms / step_ms_total, 4), "note": note}
+    import __graft_entry__
 
-    roof64 = fft_roofline(0, 16, "FFT circulant matvec in double-float (refinement residuals, VH_PREC_DF: all 5 "
-                          "passes in pair arithmetic, pair storage between passes)", "fft_matvec_df_spiral.txt",
-                          "pair-arithmetic passes issue-bound on the FP32 pipes, the z-pass half of the call; "
-                          "frac is against HBM with the algorithmic bytes of the two-pass pruned model")
-    roof32 = fft_roofline(1, 8, "FFT circulant matvec, complex64 (inner GMRES matvecs; 5 passes)",
-                          "fft_matvec_c64_spiral.txt", "passes bound by shared-memory traffic and issue (Stockham "
-                          "stages in shared memory; the register z-pass issue-bound)")
-    # the preconditioner apply (double-float triangular solves and the SpMVs around them): per
-    # RHS-apply the pair-precision factor is read once in each direction and the complex128 vectors
-    # (input, output, the Schur part written and read) pass once
-    roofp = None
-    if calls[4]:
-        apply_bytes = 2 * nnz_l * 8 + 16 * 4 * n
-        achieved_p = apply_bytes * units[4] / (ms[4] / 1e3) / 1e9
-        traffic_p = conv_traffic_from_profile("schur_precon_df_spiral.txt", "dram_bytes_per_rhs_apply")
-        roofp = {"kernel": "Schur preconditioner apply (double-float triangular solves, level by level, and the "
-                           "SpMVs around them)", "bound": "hbm", "achieved": round(achieved_p, 1), "peak": peak,
-                 "unit": "GB/s", "frac": round(achieved_p / peak, 4),
-                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                 "traffic": round(traffic_p * units[4] / calls[4], 1) if traffic_p else None,
-                 "traffic_source": "profiles/schur_precon_df_spiral.txt (ncu, 12-RHS apply, per RHS)",
-                 "algorithmic_bytes_per_launch": round(apply_bytes * units[4] / calls[4], 1),
-                 "avg_rhs_per_launch": round(units[4] / calls[4], 2), "launches": int(calls[4]),
-                 "avg_launch_ms": round(ms[4] / calls[4], 4), "share_of_step_time": round(ms[4] / step_ms_total, 4),
-                 "note": "leaf level at 2.5-3 TB/s (partly issue-bound), upper levels latency chains; "
-                         "nnz(L) = %d pair entries" % nnz_l}
-    # the dominant kernel group of the step is `roofline`; the others follow
-    cands = [r for r in ((roofp, ms[4]), (roof32, ms[1]), (roof64, ms[0])) if r[0] is not None]
-    cands.sort(key=lambda r: -r[1])
-    roof = cands[0][0] if cands else None
-    roof_other = [r[0] for r in cands[1:]]
+    __graft_entry__.build()
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
+    fp64_steps = max(1, min(args.steps, args.fp64_steps))
+    head = ConfigRunner(HEADLINE, args, world)
+    if args.mixed_only:      # profiling aid: only the warm-up and timed mixed-precision steps
+        head.timed("fp32", args.steps, args.warmup)
+        return
+    res = head.run(args.steps, args.warmup, fp64_steps, clocks=ClockSampler(0))
+    e2e = head.e2e(args.steps, args.warmup)
+    cfg = head.cfg
     line = {
-        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(1e3 * t_mixed / args.steps, 3), "higher_is_better": True,
+        "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 FFT matvec / f64 Krylov, factor, refinement",
         "data": "synthetic (seeded geometry generator)", "config": cfg,
-        "fp64": {"value": round(pts / t_fp64, 4), "ms_per_step": round(1e3 * t_fp64 / args.steps, 3),
-                 "dtype": "f64 (complex128 FFT matvec)"},
-        "mixed_over_fp64": round(t_fp64 / t_mixed, 3),
-        "accuracy": {"reference": "FP64 GPU path converged to GMRES tol 1e-12 (matches the oracle to 1e-9 in tests)",
-                     "max_rel_err_R_mixed": err_R, "max_rel_err_L_mixed": err_L,
-                     "max_rel_err_R_fp64": err_R64, "max_rel_err_L_fp64": err_L64,
-                     "max_rel_err_RL_e2e": err_e2e, "bar": 1e-6,
-                     "gmres_iterations_mixed_total": int(it_m.sum()), "gmres_iterations_fp64_total": int(it_d.sum()),
-                     "iterations_note": "inner GMRES iterations summed over RHS (mixed: over refinement steps)"},
-        "e2e": {"value": round(args.steps * F * world / t_e2e, 4), "unit": UNIT,
-                "h2d_bytes_per_step": int(b_host.nbytes + scale.nbytes + 16 * B),
-                "d2h_bytes_per_step": int(b_host.nbytes)},
-        "gpu_launches": int(launches),
-        "sections_ms": sections, "dominant_section": dominant,
-        "roofline": roof, "roofline_other": roof_other, "clocks": clk,
+        "fp64": res["fp64"], "mixed_over_fp64": res["mixed_over_fp64"], "accuracy": res["accuracy"],
+        "e2e": e2e, "gpu_launches": res["gpu_launches"], "sections_ms": res.get("sections_ms"),
+        "roofline": res.get("roofline"), "roofline_other": res.get("roofline_other"), "clocks": res.get("clocks"),
+        "matvecs_per_s": res.get("matvecs_per_s"), "factor_sharing": res.get("factor_sharing"),
     }
-    if shared is not None:
-        rep_s, t_sh, (R_s, L_s, it_s) = shared
-        line["factor_sharing"] = {
-            "share_tol": SHARE_TOL, "factors_per_step": int(len(np.unique(rep_s))),
-            "value": round(pts / t_sh, 4), "ms_per_step": round(1e3 * t_sh / args.steps, 3),
-            "gmres_iterations_total": int(it_s.sum()), "max_rel_err_RL": max(rl_err(R_s, L_s)),
-            "note": "mixed path with one Schur factor per group of neighbouring frequencies whose A_inv differs "
-                    "by at most share_tol (Sweep.prepare(share_tol)); the headline value factors every frequency"}
-    # RHS-matvecs per second of the FFT operator, from the live section timing of the mixed step
-    line["matvecs_per_s"] = {
-        "complex64": round(sections["fft_conv_c64"]["rhs"] / max(1e-9, sections["fft_conv_c64"]["ms"] / 1e3), 1),
-        "double_float": round(sections["fft_conv_df"]["rhs"] / max(1e-9, sections["fft_conv_df"]["ms"] / 1e3), 1),
-        "note": "one RHS-matvec = the full operator of lse_matvect_mult.m on one vector; batched calls of ~11 "
-                "(complex64) and 32 (refinement residual) vectors"}
+    n_head, nnz_head, prob_head = head.n, head.nnz_l, head.prob
+    head.close()
+    del head
+    torch.cuda.empty_cache()
+    line["configs"] = {}
+    for cid in [c for c in args.configs.split(",") if c and c != HEADLINE]:
+        r = ConfigRunner(cid, args, world)
+        out = r.run(args.other_steps, args.warmup, fp64_steps)
+        out["config"] = r.cfg
+        line["configs"][cid] = out
+        r.close()
+        del r
+        torch.cuda.empty_cache()
     if args.serving_requests >= 0 and world == 1:
         line["serving"] = serving_run(args)
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(prob, freqs, sw)
+        line["cpu_baseline"] = cpu_sample(prob_head, HEADLINE, samples=1)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -434,81 +522,122 @@ def serving_run(args):
     return out
 
 
-def _oracle_system(prob):
-    """The oracle's System view of a Problem (same arrays; the setup was checked bit-exact)."""
+# ---------------------------------------------------------------------------------------------- CPU
+def _oracle_setup(cid):
+    """The oracle's own system and circulant tensor of a configuration (untimed set-up)."""
+    from oracle import circulant
     from oracle import structure as ostruct
 
-    nD = prob.L * prob.M * prob.N
-    idxS5 = np.concatenate([prob.idxS + k * nD for k in range(5)])
-    return ostruct.System(L=prob.L, M=prob.M, N=prob.N, dx=prob.dx, sigma_e=prob.sigma_e, lambdaL=prob.lambdaL,
-                          idxS=prob.idxS, idxS5=idxS5, all_panels_ids=None, num_nodes=prob.meta.get("num_nodes"),
-                          Ae_full=None, Ar=prob.Ar, rhs=prob.rhs, nodeid_4_grnd=None, nodeid_4_injectcurr=None,
-                          Ae_only_leaving=None, Ae_only_entering_bndry=None)
+    w, cfg = workload(cid)
+    S = ostruct.build_system(w.sigma_e, w.lambdaL, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, st2 = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
+    return w, cfg, S, fN, st2
 
 
-def cpu_baseline(prob, freqs, sw=None, fN_host=None):
-    """The oracle (NumPy/SciPy restatement, FFTs on all host cores) solving ONE frequency point."""
+def _oracle_iterations(cid, nfreq):
+    """The oracle's own GMRES iteration counts at every frequency of a configuration at the
+    benchmark tolerance (tests/golden/oracle_iterations.npz, written by the oracle), or None."""
+    p = os.path.join(ROOT, "tests", "golden", "oracle_iterations.npz")
+    try:
+        with np.load(p) as z:
+            it = z[CONFIGS[cid]["workload"]]
+    except (OSError, KeyError):
+        return None
+    return it if it.shape[0] == nfreq else None
+
+
+def oracle_point_sample(S, fN, st2, f, tol=TOL, iters=2):
+    """Times one bounded sample of the oracle's work at frequency f: the Schur factorisation of
+    lse_sparse_precon_prepare.m (SciPy splu) plus `iters` GMRES iterations of pgmres (each one FFT
+    matvec of lse_matvect_mult.m, one preconditioner apply and the Gram-Schmidt step).
+    Returns (seconds of the factor, seconds per iteration, total seconds)."""
     from oracle import solver
-    from voxhenry_gb300 import structure
 
-    if fN_host is None:
-        fN_host, st2 = structure.circulant_tensor(prob.L, prob.M, prob.N, prob.dx)
-    else:
-        fN_host, st2 = fN_host
-    S = _oracle_system(prob)
-    f = float(freqs[len(freqs) // 2])
     t0 = time.perf_counter()
-    out = solver.solve_frequencies(S, fN_host, st2, np.array([f]), restart=RESTART, tol=TOL, maxit=MAXIT)
-    t = time.perf_counter() - t0
-    return {"value": round(1.0 / t, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"1 of {len(freqs)} frequency points ({f:.3g} Hz) solved to convergence by the oracle "
-                      f"({out['iters'][0][2]} GMRES iterations, {t:.1f} s); FFTs threaded over all host cores"}
+    om = 2 * np.pi * f
+    z_real, z_imag = solver.z_arrays(S.sigma_e, S.lambdaL, om)
+    jwmu = 1j * om * solver.MU0
+    fN_f = jwmu * fN
+    pc = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, z_imag, S.idxS, jwmu * st2, S.Ar)
+    t1 = time.perf_counter()
+    A = lambda J: solver.lse_matvect_mult(J, fN_f, S.Ar, z_real, z_imag, S.dx, S.idxS5)
+    b = S.rhs[:, 0].astype(np.complex128)
+    r = pc.multiply(b)
+    solver.pgmres_iter(A, np.zeros_like(b), r, iters, pc.multiply, None, 0.0)
+    t2 = time.perf_counter()
+    return t1 - t0, (t2 - t1) / iters, t2 - t0
 
 
-# ---------------------------------------------------------------------------------------------- reference
+def cpu_sample(prob, cid, samples=1, setup=None):
+    """The oracle (NumPy/SciPy restatement, FFTs on all host cores) on a bounded sample of the
+    workload: the factorisation and two GMRES iterations at one frequency point, extrapolated to
+    the point with the oracle's own iteration count there."""
+    w, cfg, S, fN, st2 = setup or _oracle_setup(cid)
+    its = _oracle_iterations(cid, len(w.freqs))
+    k = len(w.freqs) - 1 if its is None else int(np.argmax(its))
+    tf, ti, tt = oracle_point_sample(S, fN, st2, w.freqs[k])
+    n_it = its[k] if its is not None else None
+    per_point = tf + ti * (n_it if n_it is not None else 10)
+    return {"value": round(1.0 / per_point, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"oracle at {w.freqs[k]:.3g} Hz of the headline workload: Schur factorisation ({tf:.1f} s) and 2 "
+                      f"GMRES iterations ({ti:.1f} s each) timed, extrapolated to the point with the oracle's own "
+                      f"{n_it if n_it is not None else 'assumed 10'} iterations there (the frequency of most "
+                      f"iterations); FFTs threaded over all host cores"}
+
+
 def run_reference(args, rank, world):
+    """The reference arm: the oracle on the headline workload, each step a bounded sample at one
+    frequency (the factorisation plus two GMRES iterations), rotating over the sweep's frequencies;
+    the point time extrapolates with the oracle's own iteration count at that frequency."""
     if rank != 0:
         return
-    from oracle import circulant, solver
-    from oracle import structure as ostruct
-
-    w, cfg = workload()
-    S = ostruct.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
-    fN, st2 = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
-    freqs = w.freqs
-    jwmu = 1j * 2 * np.pi * freqs[0] * solver.MU0
-    z_real, _ = solver.z_arrays(w.sigma_e, None, 2 * np.pi * freqs[0])
-    x = S.rhs[:, 0].astype(np.complex128)
-    for _ in range(args.warmup):      # warm-up: one matvec each (FFT plans, page-in)
-        solver.lse_matvect_mult(x, jwmu * fN, S.Ar, z_real, None, S.dx, S.idxS5)
-    n_timed = max(1, min(args.steps, 2))
-    sel = [freqs[(len(freqs) // 2 + i * 7) % len(freqs)] for i in range(n_timed)]
+    w, cfg, S, fN, st2 = _oracle_setup(HEADLINE)
+    F = len(w.freqs)
+    its = _oracle_iterations(HEADLINE, F)
+    if its is None:
+        print(json.dumps({"impl": "reference", "unavailable": "oracle iteration table "
+                          "tests/golden/oracle_iterations.npz missing for the headline workload"}), flush=True)
+        return
+    order = [(k * 5) % F for k in range(max(args.steps, F))]   # visits every frequency within F steps
+    for k in range(args.warmup):
+        oracle_point_sample(S, fN, st2, w.freqs[order[k % F]], iters=1)
+    t_steps, t_points = [], []
     t0 = time.perf_counter()
-    out = solver.solve_frequencies(S, fN, st2, np.array(sel), restart=RESTART, tol=TOL, maxit=MAXIT)
-    t = time.perf_counter() - t0
-    value = n_timed / t
-    sample = (f"{n_timed} of {len(freqs)} frequency points solved to convergence "
-              f"(GMRES iterations {[it[2] for it in out['iters']]}, {t:.1f} s)")
+    for s in range(args.steps):
+        k = order[s]
+        tf, ti, tt = oracle_point_sample(S, fN, st2, w.freqs[k])
+        t_steps.append(tt)
+        t_points.append(tf + ti * its[k])
+    wall = time.perf_counter() - t0
+    value = len(t_points) / sum(t_points)
+    sample = (f"each step: the oracle's Schur factorisation and 2 GMRES iterations at one of the {F} frequencies "
+              f"(rotating: {sorted(set(order[:args.steps]))}), timed; a frequency point = factorisation + the oracle's "
+              f"own iteration count there x the per-iteration time (tests/golden/oracle_iterations.npz, GMRES tol "
+              f"{TOL:g}, restart {RESTART}); value = points / sum of their times; ms_per_step = the timed sample")
     line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(1e3 * t / n_timed, 1), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * wall / args.steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded geometry generator)",
             "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                              "sample": sample},
-            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "per_point_seconds": {f"{w.freqs[order[s]]:.4g}": round(t, 2) for s, t in enumerate(t_points)}}
     print(json.dumps(line), flush=True)
 
 
 def run_probe(args):
-    """Kernel probe for profilers: a few calls of one operator of the workload's geometry (B RHS)."""
+    """Kernel probe for profilers: a few calls of one operator of a workload's geometry (B RHS)."""
     import torch
 
     import __graft_entry__
 
     __graft_entry__.build()
-    from voxhenry_gb300 import _lib, executer, structure
+    from voxhenry_gb300 import _lib, executer, geometry, structure
 
-    w, _ = workload()
+    if args.probe_workload == "ring_small":   # the ring's kernels on a 256x256x16 grid (radius 75 um)
+        w = geometry.ring(L=256, M=256, N=16, radius=75.0)
+    else:
+        w, _ = workload(args.probe_workload)
     prob = structure.problem_from_workload(w)
     sw = executer.Sweep(prob, w.freqs, want_fp32=True)
     g = sw.geom
@@ -550,14 +679,19 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe", choices=["conv32", "conv64", "convdf", "precon", "gmres"], default=None,
                     help="profiling aid: run a few calls of one operator instead of the benchmark")
+    ap.add_argument("--probe-workload", default="C2", choices=list(CONFIGS) + ["ring_small"])
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: run only the warm-up and timed mixed-precision sweeps, print nothing")
+    ap.add_argument("--configs", default="C1,C2,C3",
+                    help="configurations reported beside the headline (comma-separated; empty: none)")
+    ap.add_argument("--other-steps", type=int, default=3, help="timed steps of the other configurations")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 path (at most --steps)")
     ap.add_argument("--serving-requests", type=int, default=0,
                     help="serving configuration: requests of the seeded stream to serve (0: the first ~30 s of "
                          "service; -1: skip)")
     ap.add_argument("--share-tol", type=float, default=None,
-                    help="share one Schur factor between neighbouring frequencies whose A_inv differs by at most "
-                         "this (mixed path); off by default")
+                    help="also report every configuration with one Schur factor per group of neighbouring "
+                         "frequencies whose A_inv differs by at most this (mixed path)")
     ap.add_argument("--probe-rhs", type=int, default=4)
     ap.add_argument("--probe-iters", type=int, default=3)
     ap.add_argument("--probe-restart", type=int, default=20)

@@ -114,8 +114,10 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
                            const int* zslot, vh_prec prec);
 
 /* ---- allocation-free matvec (no counterpart in the reference) -----------------------------------
- * The operator of vh_matvec_device, same arguments and results, enqueued on the context stream, but
- * the call allocates no device memory (no cudaMalloc / cudaFree, no allocating library routine).
+ * The operator of vh_matvec_device, same arguments and results for VH_PREC_FP64 and VH_PREC_FP32,
+ * enqueued on the context stream, but the call allocates no device memory (no cudaMalloc / cudaFree,
+ * no allocating library routine).  VH_PREC_DF is rejected with VH_ERR_BAD_ARG: its first product
+ * builds a pair copy of the tensor, an allocation.
  * For callers that cannot allocate at call time: a host whose device memory is all handed to its own
  * pool allocator (a framework's caching allocator under a memory cap), and a host whose solve loop
  * must not stall, since cudaMalloc / cudaFree synchronise the whole device and so serialise the work
@@ -128,7 +130,8 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
  *     scratch: order them on the device (one context, or events between the streams).
  *   - The first call on a device does the set-up (it looks up the scratch array's device address and
  *     fills a table of unit scales, then synchronises the context stream); make that first call
- *     before any stream capture.
+ *     before any stream capture.  The addresses are kept for the life of the process: do not use the
+ *     library across a cudaDeviceReset (or a reset of the primary context).
  *   - zslot: as vh_matvec_device (NULL: slot 0); every slot named must already be set.           */
 #define VH_MATVEC_NOALLOC_SCRATCH_BYTES (16u << 20)
 vh_status vh_matvec_device_noalloc(vh_geom* g, int B, const void* x_dev, void* y_dev, const void* scale_dev,

@@ -1,8 +1,9 @@
 """Extract compact golden fixtures from the reference's published result files.
 
-Run in a container where the reference tree is mounted (default
-/root/reference); the fixtures it writes are committed next to it so that
-tests can run where the reference is absent.
+    python tests/golden/make_golden.py <reference tree>      (or VOXHENRY_REFERENCE=<tree>)
+
+Run where the reference tree is present; the fixtures it writes are committed
+next to it so that tests can run where the reference is absent.
 
 Sources (paths within the reference project):
   results_numex1_straight_conductor/data_R_jL_mat.mat   R + jL at 41 frequencies
@@ -39,7 +40,7 @@ def csc_digest(A) -> str:
     return h.hexdigest()
 
 
-def main(ref: str = "/root/reference") -> None:
+def main(ref: str) -> None:
     out = {}
     g = sio.loadmat(os.path.join(ref, "results_numex1_straight_conductor/data_R_jL_mat.mat"))
     out["numex1_freq"] = g["freq_all"].ravel().astype(np.float64)
@@ -74,4 +75,7 @@ def main(ref: str = "/root/reference") -> None:
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VOXHENRY_REFERENCE")
+    if not tree:
+        sys.exit("usage: make_golden.py <reference tree> (or set VOXHENRY_REFERENCE)")
+    main(tree)

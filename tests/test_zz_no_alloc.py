@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-12     # single FP64 matvec, relative 2-norm
 FP32_TOL = 2e-6      # complex64 FFT convolution, relative 2-norm
 SCRATCH_BYTES = 16 << 20
+VH_ERR_BAD_ARG = 1
 VH_ERR_UNSUPPORTED = 3
 
 
@@ -108,3 +109,63 @@ def test_noalloc_rejects_grid_beyond_scratch(env):
     assert st == VH_ERR_UNSUPPORTED
     assert b"scratch" in lib.vh_last_error(g.ctx.handle)
     check_twice(env, g, X, None, None, "fp32", FP32_TOL)
+
+
+def test_noalloc_matches_the_oracle(env):
+    """FP64 allocation-free products against the oracle's lse_matvect_mult (lse_matvect_mult.m:1-140)
+    on the same geometry: the oracle's own circulant tensor, panel numbering and Ae."""
+    from oracle import circulant, solver, structure
+
+    geometry, vie = env[3], env[5]
+    w = geometry.random_blob((9, 6, 5), fill=0.65, seed=21)
+    S = structure.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, _ = circulant.generate_circulant_tensor(w.dx, 1.0, S.L, S.M, S.N)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 2 * np.pi * 1e9)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS)
+    rng = np.random.default_rng(23)
+    X = rng.standard_normal((2, S.n)) + 1j * rng.standard_normal((2, S.n))
+    jwmu = 1j * 2 * np.pi * np.array([1e6, 2e10]) * solver.MU0
+    for _ in range(2):
+        st, got = run(env, g.ctx._lib.vh_matvec_device_noalloc, g, X, jwmu, None, "fp64")
+        env[1].check(st, g.ctx.handle)
+        for b in range(2):
+            ref = solver.lse_matvect_mult(X[b], jwmu[b] * fN, S.Ar, z_real, None, S.dx, S.idxS5)
+            assert rel(got[b], ref) < FP64_TOL
+
+
+def test_noalloc_allocates_nothing_on_a_new_geometry(env):
+    """The first product on a fresh geometry, before any regular product could size its scratch, leaves
+    the device's free memory unchanged (the regular path would grow ~30 L M N complex values per RHS)."""
+    torch, geometry = env[0], env[3]
+    # a geometry of the same shape first: loads the kernels these grids use (lazy module loading takes
+    # device memory for code) and sets up the fixed arrays
+    warm, _ = make_geometry(env, geometry.random_blob((30, 20, 12), fill=0.6, seed=2))
+    rng = np.random.default_rng(4)
+    Xw = rng.standard_normal((2, warm.n)) + 1j * rng.standard_normal((2, warm.n))
+    for prec in ("fp64", "fp32"):
+        env[1].check(run(env, warm.ctx._lib.vh_matvec_device_noalloc, warm, Xw, None, None, prec)[0], warm.ctx.handle)
+    g, _ = make_geometry(env, geometry.random_blob((30, 20, 12), fill=0.6, seed=3))
+    lib = g.ctx._lib
+    B = 6
+    X = rng.standard_normal((B, g.n)) + 1j * rng.standard_normal((B, g.n))
+    x = torch.from_numpy(np.ascontiguousarray(X).view(np.float64)).cuda()
+    y = torch.empty_like(x)
+    for prec in ("fp64", "fp32"):
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        st = lib.vh_matvec_device_noalloc(g.handle, B, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), None, None,
+                                          env[1].PREC[prec])
+        g.ctx.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        env[1].check(st, g.ctx.handle)
+        assert free1 == free0, (prec, free0 - free1)
+        assert np.all(np.isfinite(y.cpu().numpy()))
+
+
+def test_noalloc_rejects_double_float(env):
+    """VH_PREC_DF builds a pair copy of the tensor (an allocation): VH_ERR_BAD_ARG."""
+    geometry = env[3]
+    g, _ = make_geometry(env, geometry.random_blob((8, 6, 5), fill=0.6, seed=6))
+    X = np.ones((1, g.n), dtype=np.complex128)
+    st, _ = run(env, g.ctx._lib.vh_matvec_device_noalloc, g, X, None, None, "df")
+    assert st == VH_ERR_BAD_ARG

@@ -13,6 +13,10 @@
 //   - right-hand sides are grouped by z slot, so no gathered z buffer is needed.
 // Nothing must start at zero: every scratch element a pass reads was written by an earlier pass.
 // The arrays are shared by every context on a device, so calls whose GPU work overlaps race.
+// VH_PREC_DF is not taken (VH_ERR_BAD_ARG): its first product builds the pair tensor, an allocation.
+// The device addresses are looked up once per device and kept for the life of the process; after a
+// cudaDeviceReset (or a reset of the primary context) they are stale, so the library must not be used
+// across one.
 #include <cstdio>
 #include <mutex>
 
@@ -117,7 +121,8 @@ extern "C" vh_status vh_matvec_device_noalloc(vh_geom* g, int B, const void* x_d
   vh_ctx* ctx = g->ctx;
   try {
     VH_REQUIRE(B >= 1 && x_dev && y_dev && x_dev != y_dev, ERR_BAD_ARG, "bad matvec arguments");
-    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32, ERR_BAD_ARG, "bad precision");
+    VH_REQUIRE(prec == VH_PREC_FP64 || prec == VH_PREC_FP32, ERR_BAD_ARG,
+               "the allocation-free matvec takes VH_PREC_FP64 or VH_PREC_FP32 (VH_PREC_DF builds a pair tensor)");
     VH_CUDA_TRY(cudaSetDevice(ctx->device));
     matvec_noalloc(g, B, static_cast<const double2*>(x_dev), static_cast<double2*>(y_dev),
                    static_cast<const double2*>(scale_dev), zslot, (Prec)prec);
@@ -125,6 +130,9 @@ extern "C" vh_status vh_matvec_device_noalloc(vh_geom* g, int B, const void* x_d
   } catch (const Error& e) {
     ctx->last_error = e.msg;
     return (vh_status)e.st;
+  } catch (const std::bad_alloc&) {   // host allocation (error text, z-slot checks), as every entry point
+    ctx->last_error = "host allocation failed";
+    return VH_ERR_OOM;
   } catch (const std::exception& e) {
     ctx->last_error = e.what();
     return VH_ERR_CUDA;
