@@ -252,6 +252,89 @@ __global__ void k_pass_y(const cplx<T>* __restrict__ src, int src_rows, int nin,
   tile_store(d + kx0, X, r + out_off * tx, tx, nout, cv);
 }
 
+// pass 2 / 4 for Y = 256, 512, 1024 in registers: Y = R1 R2 (R2 = 32 for 512 and 1024, 16 for 256),
+// a CTA takes NC consecutive kx columns of one plane (NC = 128 bytes of row: 16 complex64 values, 8
+// complex128 or double-float values).  Row n = j + R2 m, output k = k1 + R1 k2:
+//   step 1: thread (c, j) gathers x[j + R2 m], m < R1 (rows outside the input window are zero and not
+//           read), transforms over m (R1 points: A_j[k1]), multiplies by w_Y^(j k1) and stores the
+//           products in shared memory;
+//   step 2: thread (c, k1) transforms them over j (R2 points): X[k1 + R1 k2]; rows outside the output
+//           window are not stored.
+// One shared-memory exchange per transform (the ping-pong stages of k_pass_y take log8 Y of them).
+template <typename C, int DIR, int R1, int R2, int NC>
+__global__ void __launch_bounds__(NC * R2)
+    k_pass_y_reg(const C* __restrict__ src, int src_rows, int nin, C* __restrict__ dst, int dst_rows, int nout, int X,
+                 const C* __restrict__ twg, int in_off, int out_off) {
+  constexpr int Y = R1 * R2, NT = NC * R2;
+  static_assert(R1 <= R2, "step 2 runs R1 of the R2 thread rows");
+  extern __shared__ __align__(16) unsigned char yr_raw[];
+  C* tw = reinterpret_cast<C*>(yr_raw);   // tw[i] = exp(-2 pi i i / Y)
+  C* T = tw + Y;                            // T[(k1 * R2 + j) * NC + c]
+  for (int i = threadIdx.x; i < Y; i += NT) tw[i] = twg[i];
+  const int c = threadIdx.x % NC;
+  const int kx0 = blockIdx.x * NC;
+  const bool col_ok = kx0 + c < X;
+  const int64_t plane = blockIdx.y;
+  const C* s = src + plane * src_rows * (int64_t)X + kx0 + c;
+  C* d = dst + plane * dst_rows * (int64_t)X + kx0 + c;
+  __syncthreads();
+  {
+    const int j = threadIdx.x / NC;
+    C v[R1];
+#pragma unroll
+    for (int m = 0; m < R1; ++m) {
+      const int r = j + R2 * m - in_off;
+      v[m] = (col_ok && r >= 0 && r < nin) ? s[(int64_t)r * X] : czero<C>();
+    }
+    dif_pruned<Y, R1, R1, DIR>(v, tw);   // v[p] = A_j[bitrev(p)]
+#pragma unroll
+    for (int p = 0; p < R1; ++p) {
+      const int k1 = bit_reverse<ilog2c(R1)>(p);
+      const C w = tw[j * k1];
+      T[(k1 * R2 + j) * NC + c] = DIR < 0 ? cmul(v[p], w) : cmulc(v[p], w);
+    }
+  }
+  __syncthreads();
+  for (int k1 = threadIdx.x / NC; k1 < R1; k1 += NT / NC) {
+    C v[R2];
+#pragma unroll
+    for (int j = 0; j < R2; ++j) v[j] = T[(k1 * R2 + j) * NC + c];
+    dif_pruned<Y, R2, R2, DIR>(v, tw);   // v[p] = X[k1 + R1 bitrev(p)]
+#pragma unroll
+    for (int p = 0; p < R2; ++p) {
+      const int k = k1 + R1 * bit_reverse<ilog2c(R2)>(p) - out_off;
+      if (col_ok && k >= 0 && k < nout) d[(int64_t)k * X] = v[p];
+    }
+  }
+}
+
+template <typename C, int DIR, int R1, int R2>
+static void launch_pass_y_reg(const C* src, int src_rows, int nin, C* dst, int dst_rows, int nout, int X,
+                              unsigned planes, const C* tw, int in_off, int out_off, cudaStream_t st) {
+  constexpr int NC = 128 / (int)sizeof(C);
+  constexpr size_t sm = (size_t)R1 * R2 * (NC + 1) * sizeof(C);
+  static_assert(sm <= 227 * 1024, "y-pass shared memory");
+  VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y_reg<C, DIR, R1, R2, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sm));
+  dim3 grid((unsigned)ceil_div(X, NC), planes);
+  k_pass_y_reg<C, DIR, R1, R2, NC><<<grid, NC * R2, sm, st>>>(src, src_rows, nin, dst, dst_rows, nout, X, tw, in_off,
+                                                              out_off);
+  count_launch();
+  VH_CUDA_TRY(cudaGetLastError());
+}
+
+// the register y-pass when Y is 256, 512 or 1024; false otherwise
+template <int DIR, typename C>
+static bool pass_y_reg(int Y, const C* src, int src_rows, int nin, C* dst, int dst_rows, int nout, int X,
+                       unsigned planes, const C* tw, int in_off, int out_off, cudaStream_t st) {
+  switch (Y) {
+    case 256: launch_pass_y_reg<C, DIR, 16, 16>(src, src_rows, nin, dst, dst_rows, nout, X, planes, tw, in_off, out_off, st); return true;
+    case 512: launch_pass_y_reg<C, DIR, 16, 32>(src, src_rows, nin, dst, dst_rows, nout, X, planes, tw, in_off, out_off, st); return true;
+    case 1024: launch_pass_y_reg<C, DIR, 32, 32>(src, src_rows, nin, dst, dst_rows, nout, X, planes, tw, in_off, out_off, st); return true;
+    default: return false;
+  }
+}
+
 // The 13 distinct products of the 5 current spectra with the 7 tensor components at one point
 // (lse_matvect_mult.m:57-86), in place: (Jx, Jy, Jz, J2D, J3D) -> their operator images.
 template <typename C>
@@ -341,12 +424,20 @@ __global__ void k_zpass(cplx<T>* __restrict__ Bf, const cplx<T>* __restrict__ te
   }
 }
 
-// pass 3 for Z = 8, 16, 32: one thread transforms one column of one component in registers.  The
-// nz voxel rows enter the transform at rows 0.. (circular convolution is shift invariant), so the
-// forward transform reads only NZ >= nz leading rows and the inverse forms only the first NZ rows
-// (pruned at compile time).  Block: 5 warps (warp = component, lane = kx column) over 32 columns of
-// one ky row; the five spectra of a point meet in shared memory for the tensor product.
-constexpr int kZregCols = 32;
+// pass 3 for Z = 8, 16, 32, 64: the z transform of each column in registers, two threads per
+// column.  The nz voxel rows enter the transform at rows 0.. (circular convolution is shift
+// invariant), so the forward transform reads only NZ >= nz leading rows and the inverse forms only
+// the first NZ rows (pruned at compile time).  NZ <= Z / 2, so the first decimation-in-frequency
+// stage only copies (lower half) or twiddles (upper half) the inputs: lane half h = 0 takes the
+// lower half, h = 1 the upper, and each runs the remaining Z/2-point transform alone.  The last
+// decimation-in-time stage of the inverse needs both halves at each output row: the two lanes of a
+// column (lane and lane ^ 16) trade half of their rows by shuffle and each forms half of the outputs.
+// The operations and their order are those of the full-column transform (dif_pruned / dit_pruned
+// of length Z), so the results are the same.
+// Block: 5 warps (warp = component) over 16 columns of one ky row (lane = column + 16 h); the five
+// spectra of a point meet in shared memory for the tensor product, and the block's tensor values
+// (the same for every RHS of the batch) are staged in shared memory once.
+constexpr int kZregCols = 16;
 
 // storage <-> arithmetic type of the z-pass (identity, or complex128 storage with double-float
 // arithmetic)
@@ -359,90 +450,110 @@ __device__ __forceinline__ double2 zstore(dcomplex v, double2) { return to_d(v);
 __device__ __forceinline__ dcomplex zload(dcomplex v, dcomplex) { return v; }
 __device__ __forceinline__ dcomplex zstore(dcomplex v, dcomplex) { return v; }
 
+// a complex value from lane ^ m
+__device__ __forceinline__ float2 shfl_xor_c(float2 v, int m) {
+  v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
+  v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+  return v;
+}
+__device__ __forceinline__ double2 shfl_xor_c(double2 v, int m) {
+  v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
+  v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+  return v;
+}
+__device__ __forceinline__ dcomplex shfl_xor_c(dcomplex v, int m) {
+  v.x.hi = __shfl_xor_sync(0xffffffffu, v.x.hi, m);
+  v.x.lo = __shfl_xor_sync(0xffffffffu, v.x.lo, m);
+  v.y.hi = __shfl_xor_sync(0xffffffffu, v.y.hi, m);
+  v.y.lo = __shfl_xor_sync(0xffffffffu, v.y.lo, m);
+  return v;
+}
+
+template <typename T, int Z, typename GT>
+__host__ __device__ constexpr size_t zpass_reg_smem() {
+  return (size_t)(Z + 5 * Z * kZregCols) * sizeof(cplx<T>) + (size_t)Z * 7 * kZregCols * sizeof(GT);
+}
+
 template <typename T, int Z, int NZ, typename ST = cplx<T>, typename GT = cplx<T>>
-__global__ void __launch_bounds__(5 * kZregCols)
+__global__ void __launch_bounds__(5 * 32)
     k_zpass_reg(ST* __restrict__ Bf, const GT* __restrict__ tens, int nz, int Y, int X, int nrhs,
                 const cplx<T>* __restrict__ twg) {
   using C = cplx<T>;
-  constexpr int BITS = Z == 8 ? 3 : (Z == 16 ? 4 : 5);
-  static_assert(Z == 8 || Z == 16 || Z == 32, "register z-pass lengths");
+  constexpr int H = Z / 2;
+  constexpr int HN = NZ / 2;                 // output rows formed by each lane of a column
+  constexpr int BITS = ilog2c(Z);
+  constexpr int NC = kZregCols;
+  static_assert(Z == 8 || Z == 16 || Z == 32 || Z == 64, "register z-pass lengths");
+  static_assert(NZ >= 2 && NZ <= H, "pruned rows");
+  constexpr bool kRI = sizeof(GT) < sizeof(C);   // real/imaginary tensor: one T per component
   extern __shared__ __align__(16) unsigned char zr_raw[];
   C* tw = reinterpret_cast<C*>(zr_raw);
-  C* S = tw + Z;   // S[(c * Z + p) * 32 + lane]: component c, transform position p
+  C* S = tw + Z;                                             // S[(c * Z + p) * NC + col]
+  GT* G = reinterpret_cast<GT*>(S + 5 * Z * NC);             // G[(p * 7 + k) * NC + col]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int col = lane & (NC - 1);
+  const bool hi = lane >= NC;
   for (int i = threadIdx.x; i < Z; i += blockDim.x) tw[i] = twg[i];
   const int ky = blockIdx.y;
-  const int kx = blockIdx.x * kZregCols + lane;
+  const int kx0 = blockIdx.x * NC;
+  // the tensor values of the block's points, position p holding kz = bitrev(p)
+  for (int i = threadIdx.x; i < Z * 7 * NC; i += blockDim.x) {
+    const int c = i % NC, k = (i / NC) % 7, p = i / (7 * NC);
+    const int kz = bit_reverse<BITS>(p);
+    G[i] = (kx0 + c < X) ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx0 + c] : GT{};
+  }
+  const int kx = kx0 + col;
   const bool col_ok = kx < X;
   const int64_t plane = (int64_t)Y * X;       // one z row of one component
   const int64_t comp = (int64_t)nz * plane;   // one component of one RHS
-  // the tensor values of this thread's positions p = warp + 5 q, loaded once for all RHS when
-  // they fit in registers (they are the same for every RHS of the batch)
-  constexpr int Q = (Z + 4) / 5;
-  constexpr bool kRI = sizeof(GT) < sizeof(C);   // real/imaginary tensor: one T per component
-  constexpr bool kHoist = sizeof(GT) * 7 * Q <= 256;
-  GT gq[kHoist ? Q : 1][7];
-  if constexpr (kHoist) {
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int p = warp + 5 * q;
-      const int kz = bit_reverse<BITS>(p < Z ? p : 0);
-#pragma unroll
-      for (int k = 0; k < 7; ++k)
-        gq[q][k] = (col_ok && p < Z) ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : GT{};
-    }
-  }
   __syncthreads();
   for (int b = 0; b < nrhs; ++b) {
-    ST* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X + kx;
+    ST* base = Bf + ((int64_t)b * 5 + warp) * comp + (int64_t)ky * X + kx;
     {
-      C v[Z];
+      C v[H];
 #pragma unroll
-      for (int i = 0; i < Z; ++i) v[i] = czero<C>();
+      for (int n = 0; n < H; ++n) v[n] = czero<C>();
 #pragma unroll
-      for (int i = 0; i < NZ; ++i)
-        if (i < nz && col_ok) v[i] = zload(base[warp * comp + i * plane], C());
-      dif_pruned<Z, Z, NZ, -1>(v, tw);
+      for (int n = 0; n < NZ; ++n)
+        if (n < nz && col_ok) v[n] = zload(base[n * plane], C());
+      // first decimation-in-frequency stage (upper input half zero): the upper output half is the
+      // twiddled input
 #pragma unroll
-      for (int p = 0; p < Z; ++p) S[(warp * Z + p) * kZregCols + lane] = v[p];
+      for (int n = 0; n < NZ; ++n)
+        if (hi) v[n] = tw_mul<Z, Z, -1>(v[n], n, tw);
+      dif_pruned<Z, H, NZ, -1>(v, tw);
+#pragma unroll
+      for (int q = 0; q < H; ++q) S[(warp * Z + (hi ? H : 0) + q) * NC + col] = v[q];
     }
     __syncthreads();
-    if constexpr (kHoist) {
+    for (int i = threadIdx.x; i < Z * NC; i += blockDim.x) {
+      const int p = i / NC, c = i % NC;
+      GT g[7];
 #pragma unroll
-      for (int qi = 0; qi < Q; ++qi) {
-        const int p = warp + 5 * qi;
-        if (p < Z) {
-          C* q = S + p * kZregCols + lane;
-          constexpr int cs = Z * kZregCols;
-          if constexpr (kRI)
-            tensor_apply_ri(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
-          else
-            tensor_apply(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
-        }
-      }
-    } else {
-      for (int p = warp; p < Z; p += 5) {   // position p holds kz = bitrev(p)
-        const int kz = bit_reverse<BITS>(p);
-        GT g[7];
-#pragma unroll
-        for (int k = 0; k < 7; ++k) g[k] = col_ok ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : GT{};
-        C* q = S + p * kZregCols + lane;
-        constexpr int cs = Z * kZregCols;
-        if constexpr (kRI)
-          tensor_apply_ri(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
-        else
-          tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
-      }
+      for (int k = 0; k < 7; ++k) g[k] = G[(p * 7 + k) * NC + c];
+      C* q = S + p * NC + c;
+      constexpr int cs = Z * NC;
+      if constexpr (kRI)
+        tensor_apply_ri(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+      else
+        tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
     }
     __syncthreads();
     {
-      C v[Z];
+      C v[H];
 #pragma unroll
-      for (int p = 0; p < Z; ++p) v[p] = S[(warp * Z + p) * kZregCols + lane];
-      dit_pruned<Z, Z, NZ, +1>(v, tw);
+      for (int q = 0; q < H; ++q) v[q] = S[(warp * Z + (hi ? H : 0) + q) * NC + col];
+      dit_pruned<Z, H, NZ, +1>(v, tw);
+      // last decimation-in-time stage, rows k < NZ: out[k] = X0[k] + w^k X1[k] (X0: lower half,
+      // X1: upper); the lower lane forms rows 0..HN-1, the upper lane rows HN..NZ-1
 #pragma unroll
-      for (int i = 0; i < NZ; ++i)
-        if (i < nz && col_ok) base[warp * comp + i * plane] = zstore(v[i], ST());
+      for (int i = 0; i < HN; ++i) {
+        const C mine = hi ? v[HN + i] : v[i];
+        const C other = shfl_xor_c(hi ? v[i] : v[HN + i], NC);   // X0[HN + i] to the upper, X1[i] to the lower
+        const C o = hi ? cadd(other, tw_mul<Z, Z, +1>(mine, HN + i, tw)) : cadd(mine, tw_mul<Z, Z, +1>(other, i, tw));
+        const int k = (hi ? HN : 0) + i;
+        if (k < nz && col_ok) base[k * plane] = zstore(o, ST());
+      }
     }
     __syncthreads();   // S is rewritten by the next RHS
   }
@@ -451,17 +562,19 @@ __global__ void __launch_bounds__(5 * kZregCols)
 template <typename T, int Z, int NZ, typename ST, typename GT>
 static void launch_zpass_reg(ST* Bf, const GT* tens, int nz, int Y, int X, int B, const cplx<T>* tw,
                              cudaStream_t st) {
-  const size_t sm = (size_t)(Z + 5 * Z * kZregCols) * sizeof(cplx<T>);
+  constexpr size_t sm = zpass_reg_smem<T, Z, GT>();
+  static_assert(sm <= 227 * 1024, "z-pass shared memory");
   VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass_reg<T, Z, NZ, ST, GT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)sm));
   dim3 grid((unsigned)ceil_div(X, kZregCols), (unsigned)Y);
-  k_zpass_reg<T, Z, NZ, ST, GT><<<grid, 5 * kZregCols, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
+  k_zpass_reg<T, Z, NZ, ST, GT><<<grid, 5 * 32, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
   count_launch();
   VH_CUDA_TRY(cudaGetLastError());
 }
 
-// true when the register z-pass handles this length (Z = 8, 16, 32; nz <= Z / 2 always holds);
-// T is the arithmetic type, ST the storage type of the spectra
+// true when the register z-pass handles this length (Z = 8, 16, 32, and 64 outside the
+// double-float product; nz <= Z / 2 always holds); T is the arithmetic type, ST the storage type of
+// the spectra
 template <typename T, typename ST = cplx<T>, typename GT = cplx<T>>
 static bool zpass_reg(int Z, int nz, ST* Bf, const GT* tens, int Y, int X, int B, const cplx<T>* tw,
                       cudaStream_t st) {
@@ -477,8 +590,19 @@ static bool zpass_reg(int Z, int nz, ST* Bf, const GT* tens, int Y, int X, int B
     case 3204: launch_zpass_reg<T, 32, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
     case 3208: launch_zpass_reg<T, 32, 8>(Bf, tens, nz, Y, X, B, tw, st); return true;
     case 3216: launch_zpass_reg<T, 32, 16>(Bf, tens, nz, Y, X, B, tw, st); return true;
-    default: return false;
+    default: break;
   }
+  if constexpr (!std::is_same<T, dfloat>::value) {
+    switch (Z * 100 + nzb) {
+      case 6402: launch_zpass_reg<T, 64, 2>(Bf, tens, nz, Y, X, B, tw, st); return true;
+      case 6404: launch_zpass_reg<T, 64, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
+      case 6408: launch_zpass_reg<T, 64, 8>(Bf, tens, nz, Y, X, B, tw, st); return true;
+      case 6416: launch_zpass_reg<T, 64, 16>(Bf, tens, nz, Y, X, B, tw, st); return true;
+      case 6432: launch_zpass_reg<T, 64, 32>(Bf, tens, nz, Y, X, B, tw, st); return true;
+      default: break;
+    }
+  }
+  return false;
 }
 
 // pass 5: inverse x-FFT, crop, diagonal term, scatter.
@@ -610,7 +734,8 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 2
-  {
+  const bool y_reg = pass_y_reg<-1>(Y, A, ny, ny, Bf, Y, Y, X, (unsigned)(5 * nz * B), twp[1], y0, 0, st);
+  if (!y_reg) {
     const int tx = y_lines_per_cta(Y, X, dbl);
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
@@ -637,7 +762,9 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 4
-  {
+  if (y_reg) {
+    pass_y_reg<+1>(Y, Bf, Y, Y, A, ny, ny, X, (unsigned)(5 * nz * B), twp[1], 0, y0, st);
+  } else {
     const int tx = y_lines_per_cta(Y, X, dbl);
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
