@@ -171,7 +171,7 @@ vh_status vh_precon_apply_device(vh_geom* g, int B, vh_precon* const* pcs, const
  *      or fpgmres(A, b, restart, tol, maxit, R1)                             (fpgmres.m:58)
  *      for B right-hand sides at once, A = lse_matvect_mult of geometry g with per-RHS scale/zslot,
  *      the preconditioner pcs[b] (NULL: none) on the left (flexible = 0) or right (flexible = 1).
- *      x0 = 0.  b, x: HOST B x n complex.  tol: B values.  Outputs per RHS: flag (0 converged),
+ *      x0 = 0 (vh_gmres_x0 below takes one).  b, x: HOST B x n complex.  tol: B values.  Outputs per RHS: flag (0 converged),
  *      relres = |b - A x| / |b|, iter = [inner iterations of the last cycle, outer cycles] (2 ints),
  *      resvec (first resvec_len entries, row b at b*resvec_len), nres = its full length.
  *      prec = VH_PREC_FP32: mixed precision -- FP64 iterative refinement around left-preconditioned
@@ -188,6 +188,17 @@ vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, co
 vh_status vh_gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const void* b_dev, const double* scale,
                           const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
                           void* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres);
+/* [x,flag,relres,iter,resvec] = pgmres(A, b, restart, tol, maxit, L1, [], [], [], x0)   (pgmres.m:70)
+ * with an initial guess: as vh_gmres / vh_gmres_device, starting from x0 (B x n complex, HOST for
+ * vh_gmres_x0, DEVICE for vh_gmres_device_x0; NULL: zero).  The first residual is b - A x0 (pgmres.m:111-113);
+ * the mixed-precision solver forms it with the double-float product and refines from x0.             */
+vh_status vh_gmres_x0(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
+                      int restart, const double* tol, int maxit, int flexible, vh_prec prec, const double* x0,
+                      double* x, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres);
+vh_status vh_gmres_device_x0(vh_geom* g, int B, vh_precon* const* pcs, const void* b_dev, const double* scale,
+                             const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
+                             const void* x0_dev, void* x_dev, int* flag, double* relres, int* iter, double* resvec,
+                             int resvec_len, int* nres);
 
 /* ---- instrumentation (no counterpart in the reference, which times with tic/toc) --------------
  * vh_ctx_stream: the CUDA stream (cudaStream_t) all work of the context is enqueued on.

@@ -501,3 +501,101 @@ def test_ring_full_size_mixed_vs_fp64(lib):
     assert np.all(mixed["flag"] == 0) and np.all(ref["relres"] < 1e-10)
     for key in ("R", "L"):
         np.testing.assert_allclose(mixed[key], ref[key], rtol=1e-6)
+
+
+def superconducting_bar():
+    """A bar whose first half is a superconductor (London depth 0.1 um, normal-fluid sigma as the
+    copper), so that z is complex and depends on omega (VoxHenry_executer.m:236-259)."""
+    from voxhenry_gb300 import geometry
+
+    w = geometry.bar(L=16, M=5, N=4, dx=0.5e-6)
+    lam = np.zeros(w.sigma_e.shape, order="F")
+    lam[:8] = 1e-7
+    w.lambdaL = lam
+    return w
+
+
+@pytest.mark.parametrize("f", [1e6, 2e10])
+def test_precon_superconductor_matches_oracle(lib, f):
+    """lse_sparse_precon_prepare's z_real + z_imag branch (prepare.m:42-46) on the device."""
+    vie, ex = lib
+    w = superconducting_bar()
+    S, P = problem_of(w)
+    om = 2 * np.pi * f
+    jwmu = 1j * om * solver.MU0
+    z_real, z_imag = solver.z_arrays(w.sigma_e, w.lambdaL, om)
+    assert np.abs(z_imag).max() > 0
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, z_imag, S.idxS, jwmu * P.st2, S.Ar)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, z_imag, S.dx, S.idxS)
+    pc = g.precon(jwmu * P.st2)
+    X = np.random.default_rng(31).standard_normal((2, S.n)) + 1j * np.random.default_rng(32).standard_normal((2, S.n))
+    Y = vie.apply_precons(g, [pc, pc], X)
+    for k in range(2):
+        assert rel(Y[k], ref.multiply(X[k])) < PRECON_TOL
+
+
+def test_superconductor_sweep_matches_oracle(lib):
+    """A sweep with one omega-dependent z slot per frequency (VoxHenry_executer.m:236-259) through the
+    factor, the FFT matvec and GMRES: FP64 R, L and x within 1e-9 of the oracle at 100 MHz and 20 GHz,
+    mixed precision within 1e-6.  At 1 kHz the superconducting half is a near-short (|z| ~ 1e-8 of
+    copper's), A_inv spans ten decades and the oracle's own true relative residual stops at ~1e-5 even
+    at GMRES tol 1e-14: there two exact factorisations of S (this build's Cholesky, the oracle's SuperLU)
+    lead to solutions ~1e-8 apart, and R, L are compared to 1e-6."""
+    vie, ex = lib
+    w = superconducting_bar()
+    S, P = problem_of(w)
+    freqs = np.array([1e3, 1e8, 2e10])
+    ref = solver.solve_frequencies(S, P.fN_all2, P.st2, freqs, restart=50, tol=1e-12, keep_x=True)
+    sw = ex.Sweep(P, freqs)
+    assert sw.super and list(sw.zslot) == [0, 1, 2]
+    out = sw.prepare().solve(restart=50, tol=1e-12, maxit=10)
+    for k, bound in enumerate((1e-6, 1e-9, 1e-9)):
+        assert_port_matrix_close(out["R"][k:k + 1], ref["R"][k:k + 1], bound)
+        assert_port_matrix_close(out["L"][k:k + 1], ref["L"][k:k + 1], bound)
+    for k in (1, 2):
+        assert rel(out["x"][k], ref["x"][k]) < 1e-9
+    # mixed precision refines on the true residual, which the 1 kHz near-short cannot bring to 1e-10
+    swm = ex.Sweep(P, freqs[1:], precon="schur_invert_df")
+    outm = swm.prepare().solve(restart=50, tol=1e-10, maxit=10, prec="fp32")
+    assert np.all(outm["flag"] == 0)
+    assert_port_matrix_close(outm["R"], ref["R"][1:], 1e-6)
+    assert_port_matrix_close(outm["L"], ref["L"][1:], 1e-6)
+    for k in range(2):
+        assert rel(outm["x"][k], ref["x"][k + 1]) < 1e-6
+
+
+def test_pgmres_initial_guess_and_right_preconditioner(lib, blob):
+    """pgmres(A, b, restart, tol, maxit, L1, [], [], [], x0) and pgmres(..., [], [], R1) (pgmres.m:70)
+    against the oracle's pgmres with the same arguments; the mixed solver refines from x0 too."""
+    vie, ex = lib
+    w, S, P = blob
+    f = 2.5e9
+    om = 2 * np.pi * f
+    jwmu = 1j * om * solver.MU0
+    fN = jwmu * P.fN_all2
+    st = jwmu * P.st2
+    z_real, z_imag = solver.z_arrays(w.sigma_e, None, om)
+    ref = solver.SparsePrecon("schur_invert").prepare(S.dx, z_real, z_imag, S.idxS, st, S.Ar)
+    vie.lse_sparse_precon_prepare(S.dx, z_real, z_imag, S.idxS, st, S.nodeid_4_grnd, S.nodeid_4_injectcurr, S.Ar)
+    A = vie.matvec_handle(fN, S.Ar, z_real, z_imag, S.dx, S.idxS5)
+    Aref = lambda J: solver.lse_matvect_mult(J, fN, S.Ar, z_real, z_imag, S.dx, S.idxS5)
+    b = S.rhs[:, 0].astype(complex)
+    rng = np.random.default_rng(41)
+    x0 = 1e-3 * (rng.standard_normal(S.n) + 1j * rng.standard_normal(S.n))
+    xg, flag, relres, it, resvec = vie.pgmres(A, b, 100, 1e-12, 10, vie.precon_handle(), x0=x0)
+    xo, flag_o, relres_o, it_o, resvec_o = solver.pgmres(Aref, b, 100, 1e-12, 10, ref.multiply, x0=x0)
+    assert rel(xg, xo) < 1e-9
+    np.testing.assert_allclose(resvec[0], resvec_o[0], rtol=1e-9)   # |M^-1 (b - A x0)| / |M^-1 b|
+    assert flag == flag_o and relres < 1e-10
+    # right preconditioning (R1): the flexible solver with a fixed preconditioner
+    xr, flag_r, relres_r, it_r, resvec_r = vie.pgmres(A, b, 100, 1e-11, 10, None, None, vie.precon_handle())
+    xor, *_ = solver.pgmres(Aref, b, 100, 1e-11, 10, None, ref.multiply)
+    assert rel(xr, xor) < 1e-9 and flag_r == 0
+    # the mixed-precision solver from x0 (a geometry with the complex64 tensor, the batched form)
+    g = vie.Geometry(P.fN_all2, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)
+    pc = g.precon(st, kind="schur_invert_df")
+    out = g.solve(b[None], pcs=[pc], scale=jwmu, restart=50, tol=1e-10, maxit=10, prec="fp32", x0=x0[None])
+    assert out["flag"][0] == 0 and out["relres"][0] <= 1e-10
+    assert rel(out["x"][0], xo) < 1e-8
+    with pytest.raises(NotImplementedError):
+        vie.pgmres(A, b, 100, 1e-12, 10, vie.precon_handle(), None, vie.precon_handle())

@@ -65,6 +65,10 @@ SIGNATURES = {
     "vh_launch_count": (C.c_int64, []),
     "vh_gmres": (C.c_int, [_p, C.c_int, C.POINTER(_p), _dp, _dp, _ip, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp,
                            _ip, _dp, _ip, _dp, C.c_int, _ip]),
+    "vh_gmres_x0": (C.c_int, [_p, C.c_int, C.POINTER(_p), _dp, _dp, _ip, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp,
+                              _dp, _ip, _dp, _ip, _dp, C.c_int, _ip]),
+    "vh_gmres_device_x0": (C.c_int, [_p, C.c_int, C.POINTER(_p), _p, _dp, _ip, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
+                                     _p, _p, _ip, _dp, _ip, _dp, C.c_int, _ip]),
 }
 
 _lib = None

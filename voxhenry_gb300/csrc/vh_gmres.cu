@@ -805,7 +805,7 @@ void schur_gmres_solve(vh_geom* g, int B, double* const* ainv, double* const* sd
 //   that pgmres monitors);  else solve A d = r with GMRES (complex64 FFT, FP64 Krylov), x += d.
 void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2* b, const double2* scale_h,
                         const int* zslot_h, const double* tol, int m, int maxit, double inner_tol, int max_refine,
-                        double2* x, GmresOut& out, std::vector<int>& refine_steps) {
+                        double2* x, GmresOut& out, std::vector<int>& refine_steps, bool has_x0) {
   cudaStream_t st = g->ctx->stream;
   const int64_t n = g->n;
   DevBuf<double2> R, S, D, Wc, Rc;
@@ -847,16 +847,26 @@ void solve_mixed_device(vh_geom* g, int B, vh_precon* const* pcs, const double2*
   out.relres.assign(B, 0.0);
   out.resvec.assign(B, {});
   refine_steps.assign(B, 0);
-  VH_CUDA_TRY(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(double2), st));
+  if (!has_x0) VH_CUDA_TRY(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(double2), st));
   // |M^-1 b|
   M(all, b, S.p);
   std::vector<double> mb = row_norms(S.p, n, all, n, d_rows, partr, nrm, st);
   const std::vector<double> bnorm = row_norms(b, n, all, n, d_rows, partr, nrm, st);
   std::vector<int> active = all;
-  VH_CUDA_TRY(cudaMemcpyAsync(R.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-  std::vector<double> sn = mb;      // |M^-1 r| with x = 0
-  std::vector<double> rn = bnorm;   // |r| with x = 0
-  for (int i = 0; i < B; ++i) out.resvec[i].push_back(1.0);
+  std::vector<double> sn = mb;      // |M^-1 r|
+  std::vector<double> rn = bnorm;   // |r|
+  if (has_x0) {   // r = b - A x0 (double-float product, as every refinement residual) and M^-1 r
+    Aprec(all, x, Wc.p, PREC_DF);
+    k_sub<<<grid1((int64_t)B * n), 256, 0, st>>>(b, Wc.p, R.p, (int64_t)B * n);
+    count_launch();
+    VH_CUDA_TRY(cudaGetLastError());
+    M(all, R.p, S.p);
+    sn = row_norms(S.p, n, all, n, d_rows, partr, nrm, st);
+    rn = row_norms(R.p, n, all, n, d_rows, partr, nrm, st);
+  } else {
+    VH_CUDA_TRY(cudaMemcpyAsync(R.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  }
+  for (int i = 0; i < B; ++i) out.resvec[i].push_back(rn[i] / bnorm[i]);
   for (int step = 0; step < max_refine && !active.empty(); ++step) {
     const int na = (int)active.size();
     // compact r of the active RHS and solve A d = r in reduced precision
@@ -997,7 +1007,8 @@ vh_status guarded_g(vh_ctx* ctx, F&& f) {
 namespace {
 void gmres_dispatch(vh_geom* g, int B, vh_precon* const* pcs, const double2* b_dev, const double* scale,
                     const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
-                    double2* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+                    const double2* x0_dev, double2* x_dev, int* flag, double* relres, int* iter, double* resvec,
+                    int resvec_len, int* nres) {
   VH_REQUIRE(B >= 1 && b_dev && x_dev && tol, ERR_BAD_ARG, "bad gmres arguments");
   if (prec == VH_PREC_FP32 && pcs)
     for (int i = 0; i < B; ++i)
@@ -1006,12 +1017,20 @@ void gmres_dispatch(vh_geom* g, int B, vh_precon* const* pcs, const double2* b_d
   VH_REQUIRE(!(flexible && prec == VH_PREC_FP32), ERR_UNSUPPORTED, "mixed precision uses the left-preconditioned form");
   PoolScope pool_scope(&g->ctx->pool);
   cudaStream_t st = g->ctx->stream;
-  VH_CUDA_TRY(cudaMemsetAsync(x_dev, 0, (size_t)B * g->n * sizeof(double2), st));
+  // x0 (pgmres.m:70): the solve starts from it; none means zero
+  if (x0_dev) {
+    if (x0_dev != x_dev)
+      VH_CUDA_TRY(cudaMemcpyAsync(x_dev, x0_dev, (size_t)B * g->n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  } else {
+    VH_CUDA_TRY(cudaMemsetAsync(x_dev, 0, (size_t)B * g->n * sizeof(double2), st));
+  }
   GmresOut o;
   std::vector<int> steps;
   if (prec == VH_PREC_FP32)
-    // inner tolerance 1e-5: above the complex64 floor, and two FP64 checks reach 1e-9..1e-10
-    solve_mixed_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, 1e-5, 20, x_dev, o, steps);
+    // inner tolerance 1e-5: above the complex64 floor, and two FP64 checks reach 1e-9..1e-10 (tighter
+    // inner tolerances were measured to take more inner iterations in total, not fewer)
+    solve_mixed_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, 1e-5, 20, x_dev, o, steps,
+                       x0_dev != nullptr);
   else
     gmres_device(g, B, pcs, b_dev, (const double2*)scale, zslot, tol, restart, maxit, flexible != 0, PREC_FP64, x_dev, o);
   VH_CUDA_TRY(cudaStreamSynchronize(st));
@@ -1031,20 +1050,28 @@ void gmres_dispatch(vh_geom* g, int B, vh_precon* const* pcs, const double2* b_d
 
 extern "C" {
 
-vh_status vh_gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const void* b_dev, const double* scale,
-                          const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
-                          void* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+vh_status vh_gmres_device_x0(vh_geom* g, int B, vh_precon* const* pcs, const void* b_dev, const double* scale,
+                             const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
+                             const void* x0_dev, void* x_dev, int* flag, double* relres, int* iter, double* resvec,
+                             int resvec_len, int* nres) {
   if (!g) return VH_ERR_BAD_ARG;
   return guarded_g(g->ctx, [&] {
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     gmres_dispatch(g, B, pcs, (const double2*)b_dev, scale, zslot, restart, tol, maxit, flexible, prec,
-                   (double2*)x_dev, flag, relres, iter, resvec, resvec_len, nres);
+                   (const double2*)x0_dev, (double2*)x_dev, flag, relres, iter, resvec, resvec_len, nres);
   });
 }
 
-vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
-                   int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
-                   double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+vh_status vh_gmres_device(vh_geom* g, int B, vh_precon* const* pcs, const void* b_dev, const double* scale,
+                          const int* zslot, int restart, const double* tol, int maxit, int flexible, vh_prec prec,
+                          void* x_dev, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+  return vh_gmres_device_x0(g, B, pcs, b_dev, scale, zslot, restart, tol, maxit, flexible, prec, nullptr, x_dev, flag,
+                            relres, iter, resvec, resvec_len, nres);
+}
+
+vh_status vh_gmres_x0(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
+                      int restart, const double* tol, int maxit, int flexible, vh_prec prec, const double* x0,
+                      double* x, int* flag, double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
   if (!g) return VH_ERR_BAD_ARG;
   return guarded_g(g->ctx, [&] {
     VH_REQUIRE(B >= 1 && b && x && tol, ERR_BAD_ARG, "bad gmres arguments");
@@ -1056,11 +1083,19 @@ vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, co
     db.ensure((size_t)B * n);
     dx.ensure((size_t)B * n);
     VH_CUDA_TRY(cudaMemcpyAsync(db.p, b, (size_t)B * n * sizeof(double2), cudaMemcpyHostToDevice, st));
-    gmres_dispatch(g, B, pcs, db.p, scale, zslot, restart, tol, maxit, flexible, prec, dx.p, flag, relres, iter,
-                   resvec, resvec_len, nres);
+    if (x0) VH_CUDA_TRY(cudaMemcpyAsync(dx.p, x0, (size_t)B * n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    gmres_dispatch(g, B, pcs, db.p, scale, zslot, restart, tol, maxit, flexible, prec, x0 ? dx.p : nullptr, dx.p, flag,
+                   relres, iter, resvec, resvec_len, nres);
     VH_CUDA_TRY(cudaMemcpyAsync(x, dx.p, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VH_CUDA_TRY(cudaStreamSynchronize(st));
   });
+}
+
+vh_status vh_gmres(vh_geom* g, int B, vh_precon* const* pcs, const double* b, const double* scale, const int* zslot,
+                   int restart, const double* tol, int maxit, int flexible, vh_prec prec, double* x, int* flag,
+                   double* relres, int* iter, double* resvec, int resvec_len, int* nres) {
+  return vh_gmres_x0(g, B, pcs, b, scale, zslot, restart, tol, maxit, flexible, prec, nullptr, x, flag, relres, iter,
+                     resvec, resvec_len, nres);
 }
 
 }  // extern "C"

@@ -157,8 +157,9 @@ class Geometry:
         return [Precon._from_handle(self, C.c_void_p(h), kind) for h in hs]
 
     def solve(self, b, pcs=None, scale=None, zslot=None, restart=50, tol=1e-8, maxit=10, flexible=False,
-              prec="fp64", resvec_len=None):
-        """Batched pgmres / fpgmres (x0 = 0).  b: (B, n).  Returns dict(x, flag, relres, iter, resvec)."""
+              prec="fp64", resvec_len=None, x0=None):
+        """Batched pgmres / fpgmres from x0 (None: zero).  b, x0: (B, n).  Returns dict(x, flag, relres,
+        iter, resvec)."""
         bb = _lib.as_c128(np.atleast_2d(b))
         B = bb.shape[0]
         if bb.shape[1] != self.n:
@@ -179,11 +180,15 @@ class Geometry:
         if pcs is not None:
             parr = (C.c_void_p * B)(*[p.handle for p in pcs])
         ip = C.POINTER(C.c_int)
-        st = self.ctx._lib.vh_gmres(self.handle, B, parr, _lib.cview(bb), _lib.cview(s) if s is not None else None,
-                                    zs.ctypes.data_as(ip) if zs is not None else None, int(restart),
-                                    _lib.dptr(tolv), int(maxit), int(bool(flexible)), _lib.PREC[prec],
-                                    _lib.cview(x), flag.ctypes.data_as(ip), _lib.dptr(relres), it.ctypes.data_as(ip),
-                                    _lib.dptr(resvec), rl, nres.ctypes.data_as(ip))
+        x0c = None
+        if x0 is not None and np.count_nonzero(x0):
+            x0c = _lib.as_c128(np.broadcast_to(np.asarray(x0, dtype=np.complex128), bb.shape))
+        st = self.ctx._lib.vh_gmres_x0(self.handle, B, parr, _lib.cview(bb), _lib.cview(s) if s is not None else None,
+                                       zs.ctypes.data_as(ip) if zs is not None else None, int(restart),
+                                       _lib.dptr(tolv), int(maxit), int(bool(flexible)), _lib.PREC[prec],
+                                       _lib.cview(x0c) if x0c is not None else None, _lib.cview(x),
+                                       flag.ctypes.data_as(ip), _lib.dptr(relres), it.ctypes.data_as(ip),
+                                       _lib.dptr(resvec), rl, nres.ctypes.data_as(ip))
         _lib.check(st, self.ctx.handle)
         rv = resvec.reshape(B, rl)
         return {"x": x, "flag": flag, "relres": relres, "iter": it.reshape(B, 2),
@@ -442,29 +447,40 @@ def _resolve_precon(op, geom):
 
 def _krylov(A, b, restart, tol, maxit, P, flexible, x0, prec):
     if not isinstance(A, MatvecHandle):
-        raise TypeError("the GPU pgmres takes the operator as matvec_handle(...) (lse_matvect_mult's arguments)")
-    if x0 is not None and np.count_nonzero(x0):
-        raise NotImplementedError("a nonzero initial guess is not supported on the GPU path")
+        # iterchk.m:16-43 also takes a matrix A (and matrix preconditioners, applied as L1 \ x): the
+        # GPU solver is built for the VIE operator of lse_matvect_mult and its Schur preconditioner only
+        raise TypeError("the GPU pgmres takes the operator as matvec_handle(...) (lse_matvect_mult's arguments); "
+                        "matrix operators (iterchk.m:16-43) are not supported")
     g = A.geom
     pc = _resolve_precon(P, g)
-    out = g.solve(np.asarray(b).ravel()[None, :], pcs=None if pc is None else [pc], restart=restart, tol=tol,
-                  maxit=maxit, flexible=flexible, prec=prec if prec else A.prec)
+    b = np.asarray(b).ravel()
+    x0v = None if x0 is None else np.asarray(x0, dtype=np.complex128).ravel()
+    if x0v is not None and x0v.size != b.size:
+        raise ValueError("x0 must have the length of b")
+    out = g.solve(b[None, :], pcs=None if pc is None else [pc], restart=restart, tol=tol, maxit=maxit,
+                  flexible=flexible, prec=prec if prec else A.prec, x0=None if x0v is None else x0v[None, :])
     it = out["iter"][0]
     return out["x"][0], int(out["flag"][0]), float(out["relres"][0]), (int(it[0]), int(it[1])), out["resvec"][0]
 
 
 def pgmres(A, b, restart=50, tol=1e-3, maxit=10, L1=None, L2=None, R1=None, R2=None, x0=None, prec=None):
-    """[x, flag, relres, iter, resvec] = pgmres(A, b, restart, tol, maxit, L1)  (pgmres.m:70).
+    """[x, flag, relres, iter, resvec] = pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)  (pgmres.m:70).
 
-    A: matvec_handle(...); L1: precon_handle() or lse_sparse_precon_multiply (left preconditioner).
-    Second preconditioners (L2, R1, R2) are not used by VoxHenry_executer and are not supported."""
-    if L2 is not None or R1 is not None or R2 is not None:
-        raise NotImplementedError("only the left preconditioner L1 is supported")
+    A: matvec_handle(...).  One preconditioner, precon_handle() or lse_sparse_precon_multiply: on the left
+    as L1 (the executer's form, VoxHenry_executer.m:294-295), or on the right as R1 (right-preconditioned
+    GMRES: the flexible solver with a fixed preconditioner, whose iterates are the same).  x0: initial
+    guess (None or zeros: x0 = 0).  A second preconditioner (L1 with L2, R1 or R2) is not supported:
+    the executer never passes one."""
+    given = [k for k, v in (("L1", L1), ("L2", L2), ("R1", R1), ("R2", R2)) if v is not None]
+    if len(given) > 1 or given in (["L2"], ["R2"]):
+        raise NotImplementedError(f"one preconditioner, L1 or R1, is supported (got {', '.join(given)})")
+    if given == ["R1"]:
+        return _krylov(A, b, restart, tol, maxit, R1, True, x0, prec)
     return _krylov(A, b, restart, tol, maxit, L1, False, x0, prec)
 
 
 def fpgmres(A, b, restart=50, tol=1e-3, maxit=10, R1=None, R2=None, x0=None):
-    """[x, flag, relres, iter, resvec] = fpgmres(A, b, restart, tol, maxit, R1)  (fpgmres.m:58)."""
+    """[x, flag, relres, iter, resvec] = fpgmres(A, b, restart, tol, maxit, R1, R2, x0)  (fpgmres.m:58)."""
     if R2 is not None:
-        raise NotImplementedError("only one right preconditioner is supported")
+        raise NotImplementedError("one right preconditioner (R1) is supported")
     return _krylov(A, b, restart, tol, maxit, R1, True, x0, "fp64")
