@@ -501,24 +501,53 @@ def run_ours(args, rank, world):
 
 
 def serving_run(args):
-    """The serving configuration: the seeded 2000-request stream served in arrival order on this GPU
-    (all of it with --serving-requests 2000; by default the first requests up to ~30 s of service),
-    latencies under Poisson arrivals at 80 % of the measured capacity."""
-    import torch
-
+    """The serving configuration (continuous batching, voxhenry_gb300.serving.Server) on the seeded
+    2000-request stream: a calibration sample served at saturation on one slot and on the server's
+    slots (the speed-up of overlapping requests on the device), then the stream's next requests arriving
+    as a seeded Poisson process at 80 % of the measured capacity, replayed on the wall clock: p50/p99
+    latency = completion - arrival."""
     from voxhenry_gb300 import serving
 
-    n = args.serving_requests or 2000
-    reqs = serving.request_stream(n)
-    free, _ = torch.cuda.mem_get_info()
-    served = serving.serve(reqs, budget_bytes=int(0.8 * free), max_seconds=None if args.serving_requests else 30.0,
-                           min_requests=8)
-    out = serving.summarize(served)
-    k = out["requests"]
-    out["sample"] = (f"the first {k} requests of the seeded 2000-request stream (bars, wires, square spirals; "
-                     f"{int(served['freq_points'].sum())} frequency points), mixed precision at GMRES tol 1e-9; "
-                     "latency = FIFO queueing under seeded Poisson arrivals + measured service (setup, factors, "
-                     "solve, R and L)")
+    slots = args.serving_slots
+    n_cal = args.serving_calibration
+    n = args.serving_requests
+    reqs = serving.request_stream(n_cal + n)
+    cal, stream = reqs[:n_cal], reqs[n_cal:]
+    out = {"slots": slots}
+    srv1 = serving.Server(slots=1)
+    t0 = time.perf_counter()
+    srv1.run(cal)
+    t1 = time.perf_counter() - t0
+    srv1.close()
+    srv = serving.Server(slots=slots)
+    t0 = time.perf_counter()
+    rk = srv.run(cal)
+    tk = time.perf_counter() - t0
+    pts = sum(r.freq_points for r in rk)
+    out["saturation"] = {"requests": n_cal, "freq_points": int(pts),
+                         "one_slot_s": round(t1, 3), f"{slots}_slots_s": round(tk, 3),
+                         "freq_points_per_s_one_slot": round(pts / t1, 3),
+                         "freq_points_per_s": round(pts / tk, 3), "speedup": round(t1 / tk, 3),
+                         "max_in_flight": srv.max_in_flight,
+                         "all_converged": serving.summarize_run(rk)["all_converged"]}
+    rate = 0.8 * n_cal / tk        # requests per second at 80 % of the measured capacity
+    arr = serving.poisson_arrivals(len(stream), rate)
+    t0 = time.perf_counter()
+    rs = srv.run(stream, arr)
+    wall = time.perf_counter() - t0
+    srv.close()
+    summ = serving.summarize_run(rs, wall)
+    summ.update({"arrival_rate_per_s": round(rate, 3), "offered_load": 0.8, "wall_s": round(wall, 2),
+                 "max_in_flight": srv.max_in_flight})
+    out["poisson"] = summ
+    out["p50_latency_s"] = summ["p50_latency_s"]
+    out["p99_latency_s"] = summ["p99_latency_s"]
+    out["freq_points_per_s"] = summ["freq_points_per_s"]
+    out["sample"] = (f"requests {n_cal}..{n_cal + n - 1} of the seeded 2000-request stream (bars, wires, square "
+                     f"spirals; {summ['freq_points']} frequency points) arriving as a seeded Poisson process at 80 % of "
+                     f"the capacity measured on requests 0..{n_cal - 1}, replayed on the wall clock; mixed precision at "
+                     f"GMRES tol 1e-9; {slots} slots (library contexts, one CUDA stream each) admitted first come first "
+                     "served by device-memory footprint; latency = completion - arrival")
     return out
 
 
@@ -686,9 +715,12 @@ def main():
                     help="configurations reported beside the headline (comma-separated; empty: none)")
     ap.add_argument("--other-steps", type=int, default=3, help="timed steps of the other configurations")
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 path (at most --steps)")
-    ap.add_argument("--serving-requests", type=int, default=0,
-                    help="serving configuration: requests of the seeded stream to serve (0: the first ~30 s of "
-                         "service; -1: skip)")
+    ap.add_argument("--serving-requests", type=int, default=200,
+                    help="serving configuration: requests of the seeded stream replayed with Poisson arrivals "
+                         "(-1: skip the serving configuration)")
+    ap.add_argument("--serving-calibration", type=int, default=40,
+                    help="serving configuration: requests served at saturation to measure the capacity")
+    ap.add_argument("--serving-slots", type=int, default=3, help="serving configuration: requests in flight")
     ap.add_argument("--share-tol", type=float, default=None,
                     help="also report every configuration with one Schur factor per group of neighbouring "
                          "frequencies whose A_inv differs by at most this (mixed path)")

@@ -75,6 +75,13 @@ vh_status vh_ctx_create(int device, vh_ctx** out);
 void vh_ctx_destroy(vh_ctx* ctx);
 const char* vh_last_error(const vh_ctx* ctx);
 vh_status vh_ctx_synchronize(vh_ctx* ctx);
+/* device memory of the context's block cache (no counterpart in the reference): solver buffers and
+ * factors are drawn from a per-context cache instead of cudaMalloc / cudaFree per call (both cost
+ * milliseconds at these sizes and synchronise the device).  vh_ctx_memory: bytes handed out and bytes
+ * cached; vh_ctx_trim: waits for the context's stream and frees the cached blocks (a server hands them
+ * back before another context needs the memory).                                                   */
+vh_status vh_ctx_memory(vh_ctx* ctx, int64_t* in_use, int64_t* cached);
+vh_status vh_ctx_trim(vh_ctx* ctx);
 
 /* ---- geometry: the fixed arguments of lse_matvect_mult (lse_matvect_mult.m:1) ------------------
  * fN_all      : circulant tensor spectrum, complex (2L, 2M, 2N, 7) column-major.  The drop-in passes

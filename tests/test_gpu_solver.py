@@ -418,25 +418,42 @@ def test_factor_sharing_across_frequencies(lib):
     assert np.all(it <= it_ref + 1)
 
 
-def test_serving_small_requests(lib):
-    """The serving loop (voxhenry_gb300.serving) on the smallest requests of the seeded stream:
-    every request converges, and a request's R and L equal a direct sweep of its workload."""
-    vie, ex = lib
-    import torch
+def test_serving_alone_and_in_the_mix(lib):
+    """Continuous batching (voxhenry_gb300.serving.Server) on small requests of the seeded stream:
+    served one at a time on one slot, then all at once on three slots whose work overlaps on the
+    device.  Every request converges; each request's R and L in the mix equal its R and L alone within
+    1e-6 (the mixed-precision bar); a request for a geometry a slot holds reuses it; and a direct
+    FP64 sweep of the first request agrees within 1e-6."""
+    import dataclasses
 
+    vie, ex = lib
     from voxhenry_gb300 import serving, structure
 
-    reqs = [r for r in serving.request_stream(60) if r.workload.sigma_e.size < 6e4][:3]
-    free, _ = torch.cuda.mem_get_info()
-    served = serving.serve(reqs, budget_bytes=int(0.5 * free))
-    assert served["converged"].all() and len(served["service_s"]) == len(reqs)
-    assert np.all(served["service_s"] > 0)
+    reqs = [r for r in serving.request_stream(80) if r.workload.sigma_e.size < 6e4][:6]
+    srv1 = serving.Server(slots=1)
+    alone = srv1.run(reqs)
+    srv1.close()
+    srv3 = serving.Server(slots=3)
+    mix = srv3.run(reqs)
+    assert srv3.max_in_flight == 3
+    for a, m in zip(alone, mix):
+        assert a.error is None and m.error is None, (a.error, m.error)
+        assert np.all(a.flags == 0) and np.all(m.flags == 0)
+        assert_port_matrix_close(m.R, a.R, 1e-6)
+        assert_port_matrix_close(m.L, a.L, 1e-6)
+    # the same geometry again, with other frequencies: the slot that solved it keeps it resident
+    last = mix[-1]
+    w_last = reqs[-1].workload
+    again = serving.Request(1000, "repeat", dataclasses.replace(w_last, freqs=w_last.freqs[::-1].copy()))
+    rec = srv3.run([again])[0]
+    assert rec.reused_geometry and rec.slot == last.slot and np.all(rec.flags == 0)
+    assert_port_matrix_close(rec.R[::-1], last.R, 1e-6)
+    srv3.close()
     w = reqs[0].workload
     P = structure.problem_from_workload(w)
-    a = ex.Sweep(P, w.freqs, precon="schur_invert_df").prepare().solve(restart=50, tol=1e-9, maxit=10, prec="fp32")
     b = ex.Sweep(P, w.freqs).prepare().solve(restart=50, tol=1e-12, maxit=20)
-    assert_port_matrix_close(a["R"], b["R"], 1e-6)
-    assert_port_matrix_close(a["L"], b["L"], 1e-6)
+    assert_port_matrix_close(alone[0].R, b["R"], 1e-6)
+    assert_port_matrix_close(alone[0].L, b["L"], 1e-6)
 
 
 def test_padded_grid_matches_oracle(lib):

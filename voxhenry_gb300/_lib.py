@@ -32,6 +32,8 @@ SIGNATURES = {
     "vh_ctx_destroy": (None, [_p]),
     "vh_last_error": (C.c_char_p, [_p]),
     "vh_ctx_synchronize": (C.c_int, [_p]),
+    "vh_ctx_memory": (C.c_int, [_p, _i64p, _i64p]),
+    "vh_ctx_trim": (C.c_int, [_p]),
     "vh_geom_create": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int64, _i64p, C.c_int64,
                                  _i64p, _i64p, _dp, _dp, _dp, C.c_int, C.POINTER(_p)]),
     "vh_geom_destroy": (None, [_p]),

@@ -220,6 +220,24 @@ vh_status vh_ctx_synchronize(vh_ctx* ctx) {
   return guarded(ctx, [&] { VH_CUDA_TRY(cudaStreamSynchronize(ctx->stream)); });
 }
 
+vh_status vh_ctx_trim(vh_ctx* ctx) {
+  if (!ctx) return VH_ERR_BAD_ARG;
+  return guarded(ctx, [&] {
+    VH_CUDA_TRY(cudaSetDevice(ctx->device));
+    VH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));   // cached blocks may still be read by queued work
+    ctx->pool.trim();
+  });
+}
+
+vh_status vh_ctx_memory(vh_ctx* ctx, int64_t* in_use, int64_t* cached) {
+  if (!ctx) return VH_ERR_BAD_ARG;
+  size_t u = 0, c = 0;
+  ctx->pool.usage(u, c);
+  if (in_use) *in_use = (int64_t)u;
+  if (cached) *cached = (int64_t)c;
+  return VH_OK;
+}
+
 vh_status vh_geom_create(vh_ctx* ctx, int L, int M, int N, double dx, const double* fN_all, int64_t nv,
                          const int64_t* idxS, int64_t num_node, const int64_t* Ae_jc, const int64_t* Ae_ir,
                          const double* Ae_pr, const double* z_real, const double* z_imag, int want_fp32,

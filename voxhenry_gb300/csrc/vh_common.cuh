@@ -140,6 +140,14 @@ class DevicePool {
     std::lock_guard<std::mutex> lock(mu_);
     trim_locked();
   }
+  // bytes handed out and bytes held in the cache
+  void usage(size_t& in_use, size_t& cached) {
+    std::lock_guard<std::mutex> lock(mu_);
+    in_use = 0;
+    cached = 0;
+    for (auto& kv : used_) in_use += kv.second;
+    for (auto& kv : free_) cached += kv.first;
+  }
   ~DevicePool() {
     trim_locked();
     for (auto& kv : used_) cudaFree(kv.first);

@@ -89,16 +89,16 @@ def factor_share_groups(a_invs, share_tol: float) -> np.ndarray:
 class Sweep:
     """Device-resident job: geometry (tensor, Ae, z slots) plus one factor per frequency."""
 
-    def __init__(self, prob: Problem, freqs, want_fp32=True, precon="schur_invert"):
+    def __init__(self, prob: Problem, freqs, want_fp32=True, precon="schur_invert", ctx=None):
         self.prob = prob
         self.freqs = np.asarray(freqs, dtype=np.float64)
         t0 = time.perf_counter()
         z0, zi0 = z_arrays(prob.sigma_e, prob.lambdaL, 2 * np.pi * self.freqs[0])
         if prob.fN_all2 is None:     # tensor generated on the device (lse_generate_circulant_tensor)
             self.geom, prob.st2 = vie.Geometry.generated(prob.L, prob.M, prob.N, prob.dx, prob.Ar, z0, zi0, prob.idxS,
-                                                         want_fp32=want_fp32)
+                                                         want_fp32=want_fp32, ctx=ctx)
         else:
-            self.geom = vie.Geometry(prob.fN_all2, prob.Ar, z0, zi0, prob.dx, prob.idxS, want_fp32=want_fp32)
+            self.geom = vie.Geometry(prob.fN_all2, prob.Ar, z0, zi0, prob.dx, prob.idxS, want_fp32=want_fp32, ctx=ctx)
         self.super = prob.lambdaL is not None
         self.zslot = np.zeros(len(self.freqs), dtype=np.int32)
         if self.super:                                   # omega-dependent z: one slot per frequency
@@ -110,6 +110,21 @@ class Sweep:
         self.precon_kind = precon
         self.pcs = None
         self.t_factor = 0.0
+
+    def set_frequencies(self, freqs):
+        """Solves another frequency list on the same resident geometry (tensor, Ae, symbolic analysis);
+        superconductors get their z slots for the new frequencies."""
+        self.freqs = np.asarray(freqs, dtype=np.float64)
+        self.zslot = np.zeros(len(self.freqs), dtype=np.int32)
+        if self.super:
+            for i, f in enumerate(self.freqs):
+                zr, zi = z_arrays(self.prob.sigma_e, self.prob.lambdaL, 2 * np.pi * f)
+                self.geom.set_z(i, zr, zi)
+                self.zslot[i] = i
+        self.pcs = None
+        self.__dict__.pop("_b_host", None)
+        self.__dict__.pop("_share_groups", None)
+        return self
 
     def prepare(self, share_tol: float | None = None):
         """lse_sparse_precon_prepare for every frequency (VoxHenry_executer.m:273).

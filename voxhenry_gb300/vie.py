@@ -29,6 +29,16 @@ class Context:
     def synchronize(self):
         _lib.check(self._lib.vh_ctx_synchronize(self.handle), self.handle)
 
+    def memory(self):
+        """(bytes handed out, bytes cached) of the context's device block cache."""
+        u, c = C.c_int64(), C.c_int64()
+        _lib.check(self._lib.vh_ctx_memory(self.handle, C.byref(u), C.byref(c)), self.handle)
+        return u.value, c.value
+
+    def trim(self):
+        """Frees the cached device blocks (after the context's queued work)."""
+        _lib.check(self._lib.vh_ctx_trim(self.handle), self.handle)
+
     def close(self):
         if self.handle:
             self._lib.vh_ctx_destroy(self.handle)
