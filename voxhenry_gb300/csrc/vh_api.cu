@@ -215,6 +215,87 @@ void vh_ctx_destroy(vh_ctx* ctx) { vh::ctx_release(ctx); }
 
 const char* vh_last_error(const vh_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
+vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int max_rhs) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded(g->ctx, [&] {
+    VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && y_variant >= 0 && y_variant <= 2 && max_rhs >= 0,
+               ERR_BAD_ARG, "bad tuning");
+    VH_REQUIRE(g->has_conv, ERR_BAD_ARG, "geometry was created without a circulant tensor");
+    const int Y = g->conv.Y;
+    VH_REQUIRE(y_variant != 1 || Y == 256 || Y == 512 || Y == 1024, ERR_UNSUPPORTED,
+               "the register y-pass takes padded y lengths 256, 512 and 1024");
+    g->conv.tune[prec] = ConvTuning{y_variant, max_rhs};
+  });
+}
+
+vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* max_rhs, double* ms_per_rhs) {
+  if (!g) return VH_ERR_BAD_ARG;
+  return guarded(g->ctx, [&] {
+    VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && B >= 1, ERR_BAD_ARG, "bad tuning arguments");
+    VH_REQUIRE(g->has_conv && g->nv > 0, ERR_BAD_ARG, "geometry without a circulant tensor or voxels");
+    VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    cudaStream_t st = g->ctx->stream;
+    DevicePool& pool = g->ctx->pool;
+    const size_t bytes = (size_t)B * g->n * sizeof(double2);
+    double2* x = static_cast<double2*>(pool.get(bytes));
+    double2* y = static_cast<double2*>(pool.get(bytes));
+    ensure_ones(g, B);
+    // the timing does not depend on the values: a constant byte pattern (finite, nonzero doubles)
+    VH_CUDA_TRY(cudaMemsetAsync(x, 0x3f, bytes, st));
+    ConvPlan& p = g->conv;
+    const Prec pr = (Prec)prec;
+    std::vector<ConvTuning> cands;
+    const bool reg_ok = p.Y == 256 || p.Y == 512 || p.Y == 1024;
+    for (int yv : {1, 2}) {
+      if (yv == 1 && !reg_ok) continue;
+      cands.push_back(ConvTuning{yv, 0});
+      for (int w : {16, 8, 4})
+        if (w < B) cands.push_back(ConvTuning{yv, w});
+    }
+    cudaEvent_t e0, e1;
+    VH_CUDA_TRY(cudaEventCreate(&e0));
+    VH_CUDA_TRY(cudaEventCreate(&e1));
+    ConvTuning best{};
+    float best_ms = 0.0f;
+    const ConvTuning saved = p.tune[pr];
+    try {
+      for (const ConvTuning& c : cands) {
+        p.tune[pr] = c;
+        conv_apply(p, pr, B, x, g->n, y, g->n, g->ones, g->zslots[0], 0, st);   // warm-up, sizes the scratch
+        float ms = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+          VH_CUDA_TRY(cudaEventRecord(e0, st));
+          conv_apply(p, pr, B, x, g->n, y, g->n, g->ones, g->zslots[0], 0, st);
+          VH_CUDA_TRY(cudaEventRecord(e1, st));
+          VH_CUDA_TRY(cudaEventSynchronize(e1));
+          float t = 0.0f;
+          VH_CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
+          ms = std::min(ms, t);
+        }
+        if (best_ms == 0.0f || ms < best_ms) {
+          best_ms = ms;
+          best = c;
+        }
+      }
+    } catch (...) {
+      p.tune[pr] = saved;
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      pool.put(x);
+      pool.put(y);
+      throw;
+    }
+    p.tune[pr] = best;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    pool.put(x);
+    pool.put(y);
+    if (y_variant) *y_variant = best.y_variant;
+    if (max_rhs) *max_rhs = best.max_rhs;
+    if (ms_per_rhs) *ms_per_rhs = best_ms / B;
+  });
+}
+
 vh_status vh_ctx_synchronize(vh_ctx* ctx) {
   if (!ctx) return VH_ERR_BAD_ARG;
   return guarded(ctx, [&] { VH_CUDA_TRY(cudaStreamSynchronize(ctx->stream)); });

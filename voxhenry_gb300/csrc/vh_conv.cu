@@ -344,14 +344,24 @@ void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaSt
 
 void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
                 const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st) {
-  conv_plan_reserve(p, B, prec);
+  const ConvTuning& t = p.tune[prec];
+  const int w = (t.max_rhs > 0 && t.max_rhs < B) ? t.max_rhs : B;   // right-hand sides per launch sequence
+  conv_plan_reserve(p, w, prec);
   if (prec == PREC_DF && conv_df_supported(p)) ensure_df_tensor(p, st);
-  if (prec == PREC_FP32)
-    conv_apply_c64(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
-  else if (prec == PREC_DF && conv_df_supported(p))
-    conv_apply_df(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
-  else
-    conv_apply_t<double>(p, B, x, ldx, y, ldy, scale, zdiag, zstride, st);
+  p.y_variant_now = t.y_variant;
+  for (int b0 = 0; b0 < B; b0 += w) {
+    const int nb = std::min(w, B - b0);
+    const double2* xb = x + (int64_t)b0 * ldx;
+    double2* yb = y + (int64_t)b0 * ldy;
+    const double2* zb = zdiag + (int64_t)b0 * zstride;
+    if (prec == PREC_FP32)
+      conv_apply_c64(p, nb, xb, ldx, yb, ldy, scale + b0, zb, zstride, st);
+    else if (prec == PREC_DF && conv_df_supported(p))
+      conv_apply_df(p, nb, xb, ldx, yb, ldy, scale + b0, zb, zstride, st);
+    else
+      conv_apply_t<double>(p, nb, xb, ldx, yb, ldy, scale + b0, zb, zstride, st);
+  }
+  p.y_variant_now = 0;
 }
 
 void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t& b_per_rhs) {
@@ -367,6 +377,7 @@ void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, i
   size_t a1, b1;
   conv_scratch_bytes(p, prec, a1, b1);
   ConvPlan q = p;   // shallow view of the plan with the caller's scratch; owns nothing
+  q.y_variant_now = 0;   // the automatic pass choice
   q.scratchA = scratchA;
   q.scratchB = scratchB;
   q.scratch_bytes_A = a1 * B;

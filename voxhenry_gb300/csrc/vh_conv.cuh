@@ -15,6 +15,16 @@ enum Prec { PREC_FP64 = 0, PREC_FP32 = 1, PREC_DF = 2 };
 // Factor n into the radices the FFT supports; false if n has another prime factor.
 bool fft_factor(int n, FftDesc& d);
 
+// Launch choices of the FFT convolution at one precision, set by the autotuner (vh_conv_tune) or from
+// its cache (vh_conv_set_tuning): the y-pass (0 automatic = the register pass where Y is 256, 512 or
+// 1024; 1 the register pass; 2 the shared-memory Stockham pass) and the right-hand sides per launch
+// sequence (0: the whole batch; else chunks of at most max_rhs, which keeps the spectra of a chunk
+// smaller at the price of reading the tensor once per chunk).
+struct ConvTuning {
+  int y_variant = 0;
+  int max_rhs = 0;
+};
+
 struct ConvPlan {
   int L = 0, M = 0, N = 0;   // voxel grid
   int X = 0, Y = 0, Z = 0;   // padded grid (2L, 2M, 2N)
@@ -46,6 +56,8 @@ struct ConvPlan {
   void* scratchA = nullptr;
   void* scratchB = nullptr;
   size_t scratch_bytes_A = 0, scratch_bytes_B = 0;
+  ConvTuning tune[3];          // per Prec
+  int y_variant_now = 0;       // the y-pass of the launch sequence being issued (ConvTuning::y_variant)
 
   int64_t points() const { return (int64_t)X * Y * Z; }
   int64_t lmn() const { return (int64_t)L * M * N; }

@@ -734,7 +734,8 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 2
-  const bool y_reg = pass_y_reg<-1>(Y, A, ny, ny, Bf, Y, Y, X, (unsigned)(5 * nz * B), twp[1], y0, 0, st);
+  const bool y_reg =
+      p.y_variant_now != 2 && pass_y_reg<-1>(Y, A, ny, ny, Bf, Y, Y, X, (unsigned)(5 * nz * B), twp[1], y0, 0, st);
   if (!y_reg) {
     const int tx = y_lines_per_cta(Y, X, dbl);
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);

@@ -126,6 +126,16 @@ class Sweep:
         self.__dict__.pop("_share_groups", None)
         return self
 
+    def tune(self, precs=("fp32", "df"), path: str | None = None, retune: bool = False) -> dict:
+        """Autotunes the FFT convolution for this sweep's batch (all frequencies x ports) at each
+        precision (voxhenry_gb300.autotune; cached on disk)."""
+        from . import autotune
+
+        B = len(self.freqs) * self.prob.num_ports
+        grid = (self.prob.L, self.prob.M, self.prob.N)
+        box = autotune.box_of(self.prob)
+        return {p: autotune.tune(self.geom, p, B, grid, box, path=path, retune=retune) for p in precs}
+
     def prepare(self, share_tol: float | None = None):
         """lse_sparse_precon_prepare for every frequency (VoxHenry_executer.m:273).
 
