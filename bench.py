@@ -213,6 +213,11 @@ class ConfigRunner:
         self.freqs = self.w.freqs
         self.sw = executer.Sweep(prob, self.freqs, want_fp32=True)
         g = self.g = self.sw.geom
+        if not getattr(args, "no_tune", False):   # the mixed path's FFT products (cached on disk)
+            t0 = time.perf_counter()
+            tuned = self.sw.tune(precs=("fp32", "df"))
+            self.cfg["autotune"] = {p: {k: v for k, v in c.items()} for p, c in tuned.items()}
+            self.cfg["autotune"]["seconds"] = round(time.perf_counter() - t0, 2)
         self.lib = g.ctx._lib
         self.stream = torch.cuda.ExternalStream(self.lib.vh_ctx_stream(g.ctx.handle))
         F, P = len(self.freqs), prob.num_ports
@@ -715,10 +720,10 @@ def main():
                     help="configurations reported beside the headline (comma-separated; empty: none)")
     ap.add_argument("--other-steps", type=int, default=3, help="timed steps of the other configurations")
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 path (at most --steps)")
-    ap.add_argument("--serving-requests", type=int, default=200,
+    ap.add_argument("--serving-requests", type=int, default=48,
                     help="serving configuration: requests of the seeded stream replayed with Poisson arrivals "
                          "(-1: skip the serving configuration)")
-    ap.add_argument("--serving-calibration", type=int, default=40,
+    ap.add_argument("--serving-calibration", type=int, default=12,
                     help="serving configuration: requests served at saturation to measure the capacity")
     ap.add_argument("--serving-slots", type=int, default=3, help="serving configuration: requests in flight")
     ap.add_argument("--share-tol", type=float, default=None,
@@ -733,6 +738,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the FFT convolution's default launch choices")
     ap.add_argument("--mixed-precon", default=MIXED_PRECON, choices=["schur_invert_df", "schur_invert"],
                     help="Schur factor arithmetic of the mixed-precision path")
     args = ap.parse_args()

@@ -123,14 +123,16 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
 /* ---- autotuning of the FFT convolution (no counterpart in the reference) -----------------------
  * vh_conv_tune times the launch choices of the geometry's FFT convolution at precision `prec` for a
  * batch of B right-hand sides with CUDA events on the context stream (one warm-up and the best of
- * three products each; inputs are a constant pattern, the timing does not depend on the values),
+ * two products each; inputs are a constant pattern, the timing does not depend on the values),
  * keeps the fastest in the geometry and returns it: y_variant (1 the register y-pass for padded y
- * lengths 256, 512, 1024; 2 the shared-memory Stockham pass) and max_rhs (right-hand sides per
+ * lengths 256, 512, 1024; 2 the shared-memory Stockham pass), z_variant (1 the two-lane register
+ * z-pass; 2 one thread per column, for padded z lengths up to 32) and max_rhs (right-hand sides per
  * launch sequence; 0: the whole batch), and its milliseconds per RHS-matvec.  vh_conv_set_tuning
- * sets a choice without timing (a cached one); y_variant 0 and max_rhs 0 restore the defaults.  The
- * products of every choice agree within the precision's rounding.                                 */
-vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* max_rhs, double* ms_per_rhs);
-vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int max_rhs);
+ * sets a choice without timing (a cached one); zeros restore the defaults.  The products of every
+ * choice agree within the precision's rounding.                                                     */
+vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_variant, int* max_rhs,
+                       double* ms_per_rhs);
+vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_variant, int max_rhs);
 
 /* ---- allocation-free matvec (no counterpart in the reference) -----------------------------------
  * The operator of vh_matvec_device, same arguments and results for VH_PREC_FP64 and VH_PREC_FP32,

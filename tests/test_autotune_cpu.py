@@ -23,13 +23,13 @@ def test_tune_times_once_then_uses_the_cache(tmp_path):
 
     def timer(geom, prec, B):
         calls.append((prec, B))
-        return {"y_variant": 2, "max_rhs": 8, "ms_per_rhs": 0.5}
+        return {"y_variant": 2, "z_variant": 1, "max_rhs": 8, "ms_per_rhs": 0.5}
 
     g = FakeGeom()
     a = autotune.tune(g, "fp32", 12, (64, 16, 16), (16, 16), path=path, timer=timer)
     assert a["cached"] is False and calls == [("fp32", 12)]
     b = autotune.tune(g, "fp32", 16, (64, 16, 16), (16, 16), path=path, timer=timer)   # same bucket
-    assert b["cached"] is True and len(calls) == 1 and g.tuning == ("fp32", 2, 8)
+    assert b["cached"] is True and len(calls) == 1 and g.tuning == ("fp32", 2, 1, 8)
     autotune.tune(g, "fp32", 12, (64, 16, 16), (16, 16), path=path, timer=timer, retune=True)
     assert len(calls) == 2
     d = json.load(open(path))

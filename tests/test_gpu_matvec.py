@@ -202,8 +202,9 @@ def test_matvec_df_takes_the_double_float_passes(vie, shape, zr):
 @pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL), ("df", DF_TOL)])
 def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     """Each launch choice the autotuner can make (vh_conv_set_tuning: the register or the Stockham
-    y-pass, the whole batch or chunks of 4 right-hand sides) gives the FP64 product of the default
-    within the precision's tolerance; vh_conv_tune picks one of them and leaves it set."""
+    y-pass, the two-lane or the one-thread-per-column z-pass, the whole batch or chunks of 4
+    right-hand sides) gives the FP64 product of the default within the precision's tolerance;
+    vh_conv_tune picks one of them and leaves it set."""
     import ctypes as C
 
     from voxhenry_gb300 import _lib, executer, geometry, structure
@@ -219,14 +220,16 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     ref = g.matvec(X, scale=scale, prec="fp64")
     lib = g.ctx._lib
     for yv in (1, 2):
-        for mr in (0, 4):
-            _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], yv, mr), g.ctx.handle)
-            got = g.matvec(X, scale=scale, prec=prec)
-            for b in range(B):
-                assert rel(got[b], ref[b]) < tol, (yv, mr, b)
-    yv, mr, ms = C.c_int(), C.c_int(), C.c_double()
-    _lib.check(lib.vh_conv_tune(g.handle, _lib.PREC[prec], B, C.byref(yv), C.byref(mr), C.byref(ms)), g.ctx.handle)
-    assert yv.value in (1, 2) and mr.value in (0, 4) and ms.value > 0
+        for zv in (1, 2):
+            for mr in (0, 4):
+                _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], yv, zv, mr), g.ctx.handle)
+                got = g.matvec(X, scale=scale, prec=prec)
+                for b in range(B):
+                    assert rel(got[b], ref[b]) < tol, (yv, zv, mr, b)
+    yv, zv, mr, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+    _lib.check(lib.vh_conv_tune(g.handle, _lib.PREC[prec], B, C.byref(yv), C.byref(zv), C.byref(mr), C.byref(ms)),
+               g.ctx.handle)
+    assert yv.value in (1, 2) and zv.value in (1, 2) and mr.value in (0, 4) and ms.value > 0
     got = g.matvec(X, scale=scale, prec=prec)
     assert max(rel(got[b], ref[b]) for b in range(B)) < tol
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], 0, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], 0, 0, 0), g.ctx.handle)

@@ -12,6 +12,20 @@ namespace vh {
 static std::atomic<int64_t> g_launches{0};
 int64_t launches_total() { return g_launches.load(std::memory_order_relaxed); }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int max_dyn_smem_optin() {
+  static std::atomic<int> cache[64];   // per device; 0 = not looked up yet
+  int dev = 0;
+  VH_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64) {
+    const int v = cache[dev].load(std::memory_order_relaxed);
+    if (v) return v;
+  }
+  int v = 0;
+  VH_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (dev >= 0 && dev < 64) cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
 }  // namespace vh
 
 namespace {
@@ -215,20 +229,22 @@ void vh_ctx_destroy(vh_ctx* ctx) { vh::ctx_release(ctx); }
 
 const char* vh_last_error(const vh_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
-vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int max_rhs) {
+vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_variant, int max_rhs) {
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
-    VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && y_variant >= 0 && y_variant <= 2 && max_rhs >= 0,
+    VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && y_variant >= 0 && y_variant <= 2 && z_variant >= 0 &&
+                   z_variant <= 2 && max_rhs >= 0,
                ERR_BAD_ARG, "bad tuning");
     VH_REQUIRE(g->has_conv, ERR_BAD_ARG, "geometry was created without a circulant tensor");
     const int Y = g->conv.Y;
     VH_REQUIRE(y_variant != 1 || Y == 256 || Y == 512 || Y == 1024, ERR_UNSUPPORTED,
                "the register y-pass takes padded y lengths 256, 512 and 1024");
-    g->conv.tune[prec] = ConvTuning{y_variant, max_rhs};
+    g->conv.tune[prec] = ConvTuning{y_variant, max_rhs, z_variant};
   });
 }
 
-vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* max_rhs, double* ms_per_rhs) {
+vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_variant, int* max_rhs,
+                       double* ms_per_rhs) {
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
     VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && B >= 1, ERR_BAD_ARG, "bad tuning arguments");
@@ -246,11 +262,15 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* max
     const Prec pr = (Prec)prec;
     std::vector<ConvTuning> cands;
     const bool reg_ok = p.Y == 256 || p.Y == 512 || p.Y == 1024;
+    const bool col_ok = p.Z <= 32;   // the one-thread-per-column z-pass takes Z = 8, 16, 32
     for (int yv : {1, 2}) {
       if (yv == 1 && !reg_ok) continue;
-      cands.push_back(ConvTuning{yv, 0});
-      for (int w : {16, 8, 4})
-        if (w < B) cands.push_back(ConvTuning{yv, w});
+      for (int zv : {1, 2}) {
+        if (zv == 2 && !col_ok) continue;
+        cands.push_back(ConvTuning{yv, 0, zv});
+        for (int w : {8, 4})
+          if (w < B) cands.push_back(ConvTuning{yv, w, zv});
+      }
     }
     cudaEvent_t e0, e1;
     VH_CUDA_TRY(cudaEventCreate(&e0));
@@ -263,7 +283,7 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* max
         p.tune[pr] = c;
         conv_apply(p, pr, B, x, g->n, y, g->n, g->ones, g->zslots[0], 0, st);   // warm-up, sizes the scratch
         float ms = 1e30f;
-        for (int rep = 0; rep < 3; ++rep) {
+        for (int rep = 0; rep < 2; ++rep) {
           VH_CUDA_TRY(cudaEventRecord(e0, st));
           conv_apply(p, pr, B, x, g->n, y, g->n, g->ones, g->zslots[0], 0, st);
           VH_CUDA_TRY(cudaEventRecord(e1, st));
@@ -291,6 +311,7 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* max
     pool.put(x);
     pool.put(y);
     if (y_variant) *y_variant = best.y_variant;
+    if (z_variant) *z_variant = best.z_variant;
     if (max_rhs) *max_rhs = best.max_rhs;
     if (ms_per_rhs) *ms_per_rhs = best_ms / B;
   });

@@ -457,7 +457,7 @@ static int fused_threads(int max_nf) { return max_nf <= 64 ? 32 : (max_nf <= 96 
 template <typename T, int NT>
 static void launch_front_nt(const int32_t* lev, unsigned count, unsigned nz, size_t sm, const CholSymbolic& s,
                             T* const* Wp, int* d_err, cudaStream_t st) {
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_front<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  allow_dyn_smem(k_chol_front<T, NT>, sm);
   k_chol_front<T, NT><<<dim3(count, 1, nz), NT, sm, st>>>(lev, s.d_fronts, s.d_relmap, Wp, d_err);
   count_launch();
   VH_CUDA_TRY(cudaGetLastError());
@@ -1159,17 +1159,17 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
     }
   }
   VH_REQUIRE(sm_w[0] <= kWideStageMax, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
-  if (sm_f[0]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_f[0]));
-  if (sm_f[1]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_f[1]));
-  if (sm_b[0]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b[0]));
-  if (sm_b[1]) VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b[1]));
+  if (sm_f[0]) allow_dyn_smem(k_chol_fsolve<T, false>, sm_f[0]);
+  if (sm_f[1]) allow_dyn_smem(k_chol_fsolve<T, true>, sm_f[1]);
+  if (sm_b[0]) allow_dyn_smem(k_chol_bsolve<T, false>, sm_b[0]);
+  if (sm_b[1]) allow_dyn_smem(k_chol_bsolve<T, true>, sm_b[1]);
   if (sm_w[0]) {
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[0]));
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[0]));
+    allow_dyn_smem(k_chol_fsolve_wide<T, false>, sm_w[0]);
+    allow_dyn_smem(k_chol_bsolve_wide<T, false>, sm_w[0]);
   }
   if (sm_w[1]) {
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_fsolve_wide<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[1]));
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_chol_bsolve_wide<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_w[1]));
+    allow_dyn_smem(k_chol_fsolve_wide<T, true>, sm_w[1]);
+    allow_dyn_smem(k_chol_bsolve_wide<T, true>, sm_w[1]);
   }
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();

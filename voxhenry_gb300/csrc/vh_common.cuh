@@ -163,6 +163,20 @@ class DevicePool {
   std::unordered_map<void*, size_t> used_;
 };
 
+// ---------------------------------------------------------------- dynamic shared memory
+// The largest dynamic shared memory a block may opt in to on the current device.
+int max_dyn_smem_optin();
+// Lets `kernel` launch with `bytes` of dynamic shared memory.  The limit is a per-kernel, process-wide
+// attribute shared by every host thread and context, so it is set to the device's opt-in maximum, the
+// same value for every caller, and not to `bytes`: a thread launching the kernel with more than
+// another thread's size then never meets a limit that thread just lowered.
+template <typename K>
+void allow_dyn_smem(K* kernel, size_t bytes) {
+  const int mx = max_dyn_smem_optin();
+  VH_REQUIRE(bytes <= (size_t)mx, ERR_UNSUPPORTED, "a kernel needs more shared memory than the device offers");
+  VH_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+}
+
 // ---------------------------------------------------------------- instrumentation
 // Kernels launched by this library (every launch site calls count_launch()).
 int64_t launches_total();

@@ -332,7 +332,7 @@ void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaSt
       tx = std::max(1, std::min(16, 4096 / n));
     }
     const size_t sm = (size_t)(n + 2 * n * tx) * sizeof(double2);
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_fft_axis_inplace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_dyn_smem(k_fft_axis_inplace, sm);
     dim3 grid((unsigned)ceil_div(inner, tx), (unsigned)planes);
     k_fft_axis_inplace<<<grid, kPassThreads, sm, st>>>(data, inner, fd, tw, tx, contiguous);
     count_launch();
@@ -349,6 +349,7 @@ void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, do
   conv_plan_reserve(p, w, prec);
   if (prec == PREC_DF && conv_df_supported(p)) ensure_df_tensor(p, st);
   p.y_variant_now = t.y_variant;
+  p.z_variant_now = t.z_variant;
   for (int b0 = 0; b0 < B; b0 += w) {
     const int nb = std::min(w, B - b0);
     const double2* xb = x + (int64_t)b0 * ldx;
@@ -362,6 +363,7 @@ void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, do
       conv_apply_t<double>(p, nb, xb, ldx, yb, ldy, scale + b0, zb, zstride, st);
   }
   p.y_variant_now = 0;
+  p.z_variant_now = 0;
 }
 
 void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t& b_per_rhs) {
@@ -377,7 +379,8 @@ void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, i
   size_t a1, b1;
   conv_scratch_bytes(p, prec, a1, b1);
   ConvPlan q = p;   // shallow view of the plan with the caller's scratch; owns nothing
-  q.y_variant_now = 0;   // the automatic pass choice
+  q.y_variant_now = 0;   // the automatic pass choices
+  q.z_variant_now = 0;
   q.scratchA = scratchA;
   q.scratchB = scratchB;
   q.scratch_bytes_A = a1 * B;

@@ -17,12 +17,13 @@ bool fft_factor(int n, FftDesc& d);
 
 // Launch choices of the FFT convolution at one precision, set by the autotuner (vh_conv_tune) or from
 // its cache (vh_conv_set_tuning): the y-pass (0 automatic = the register pass where Y is 256, 512 or
-// 1024; 1 the register pass; 2 the shared-memory Stockham pass) and the right-hand sides per launch
-// sequence (0: the whole batch; else chunks of at most max_rhs, which keeps the spectra of a chunk
-// smaller at the price of reading the tensor once per chunk).
+// 1024; 1 the register pass; 2 the shared-memory Stockham pass), the z-pass (z_variant) and the
+// right-hand sides per launch sequence (0: the whole batch; else chunks of at most max_rhs, which
+// keeps the spectra of a chunk smaller at the price of reading the tensor once per chunk).
 struct ConvTuning {
   int y_variant = 0;
   int max_rhs = 0;
+  int z_variant = 0;   // 0 automatic = 1 the two-lane register z-pass; 2 one thread per column (Z <= 32)
 };
 
 struct ConvPlan {
@@ -57,7 +58,8 @@ struct ConvPlan {
   void* scratchB = nullptr;
   size_t scratch_bytes_A = 0, scratch_bytes_B = 0;
   ConvTuning tune[3];          // per Prec
-  int y_variant_now = 0;       // the y-pass of the launch sequence being issued (ConvTuning::y_variant)
+  int y_variant_now = 0;       // the y- and z-passes of the launch sequence being issued (ConvTuning)
+  int z_variant_now = 0;
 
   int64_t points() const { return (int64_t)X * Y * Z; }
   int64_t lmn() const { return (int64_t)L * M * N; }

@@ -5,9 +5,9 @@
 
 namespace vh {
 
-bool zpass_df(int Z, int nz, dcomplex* Bf, const dfloat* tens_ri, int Y, int X, int B, const dcomplex* tw,
-              cudaStream_t st) {
-  return zpass_reg<dfloat>(Z, nz, Bf, tens_ri, Y, X, B, tw, st);
+bool zpass_df(int z_variant, int Z, int nz, dcomplex* Bf, const dfloat* tens_ri, int Y, int X, int B,
+              const dcomplex* tw, cudaStream_t st) {
+  return zpass_any<dfloat>(z_variant, Z, nz, Bf, tens_ri, Y, X, B, tw, st);
 }
 
 }  // namespace vh

@@ -314,8 +314,7 @@ static void launch_pass_y_reg(const C* src, int src_rows, int nin, C* dst, int d
   constexpr int NC = 128 / (int)sizeof(C);
   constexpr size_t sm = (size_t)R1 * R2 * (NC + 1) * sizeof(C);
   static_assert(sm <= 227 * 1024, "y-pass shared memory");
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y_reg<C, DIR, R1, R2, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sm));
+  allow_dyn_smem(k_pass_y_reg<C, DIR, R1, R2, NC>, sm);
   dim3 grid((unsigned)ceil_div(X, NC), planes);
   k_pass_y_reg<C, DIR, R1, R2, NC><<<grid, NC * R2, sm, st>>>(src, src_rows, nin, dst, dst_rows, nout, X, tw, in_off,
                                                               out_off);
@@ -564,10 +563,116 @@ static void launch_zpass_reg(ST* Bf, const GT* tens, int nz, int Y, int X, int B
                              cudaStream_t st) {
   constexpr size_t sm = zpass_reg_smem<T, Z, GT>();
   static_assert(sm <= 227 * 1024, "z-pass shared memory");
-  VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass_reg<T, Z, NZ, ST, GT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sm));
+  allow_dyn_smem(k_zpass_reg<T, Z, NZ, ST, GT>, sm);
   dim3 grid((unsigned)ceil_div(X, kZregCols), (unsigned)Y);
   k_zpass_reg<T, Z, NZ, ST, GT><<<grid, 5 * 32, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
+  count_launch();
+  VH_CUDA_TRY(cudaGetLastError());
+}
+
+// pass 3 alternative for Z = 8, 16, 32 (the autotuner's z_variant 2): one thread transforms a whole
+// column of one component in registers (the same pruned transforms), 5 warps over 32 columns of one
+// ky row, the thread's tensor values held in registers for all RHS when they fit.  It keeps more
+// columns per block and fewer exchanges than the two-lane pass, and pays for it in registers as Z
+// grows (255 at Z = 32).
+constexpr int kZcolCols = 32;
+
+template <typename T, int Z, int NZ, typename ST = cplx<T>, typename GT = cplx<T>>
+__global__ void __launch_bounds__(5 * kZcolCols)
+    k_zpass_col(ST* __restrict__ Bf, const GT* __restrict__ tens, int nz, int Y, int X, int nrhs,
+                const cplx<T>* __restrict__ twg) {
+  using C = cplx<T>;
+  constexpr int BITS = Z == 8 ? 3 : (Z == 16 ? 4 : 5);
+  static_assert(Z == 8 || Z == 16 || Z == 32, "register z-pass lengths");
+  extern __shared__ __align__(16) unsigned char zr_raw[];
+  C* tw = reinterpret_cast<C*>(zr_raw);
+  C* S = tw + Z;   // S[(c * Z + p) * 32 + lane]: component c, transform position p
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < Z; i += blockDim.x) tw[i] = twg[i];
+  const int ky = blockIdx.y;
+  const int kx = blockIdx.x * kZcolCols + lane;
+  const bool col_ok = kx < X;
+  const int64_t plane = (int64_t)Y * X;       // one z row of one component
+  const int64_t comp = (int64_t)nz * plane;   // one component of one RHS
+  // the tensor values of this thread's positions p = warp + 5 q, loaded once for all RHS when
+  // they fit in registers (they are the same for every RHS of the batch)
+  constexpr int Q = (Z + 4) / 5;
+  constexpr bool kRI = sizeof(GT) < sizeof(C);   // real/imaginary tensor: one T per component
+  constexpr bool kHoist = sizeof(GT) * 7 * Q <= 256;
+  GT gq[kHoist ? Q : 1][7];
+  if constexpr (kHoist) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int p = warp + 5 * q;
+      const int kz = bit_reverse<BITS>(p < Z ? p : 0);
+#pragma unroll
+      for (int k = 0; k < 7; ++k)
+        gq[q][k] = (col_ok && p < Z) ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : GT{};
+    }
+  }
+  __syncthreads();
+  for (int b = 0; b < nrhs; ++b) {
+    ST* base = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X + kx;
+    {
+      C v[Z];
+#pragma unroll
+      for (int i = 0; i < Z; ++i) v[i] = czero<C>();
+#pragma unroll
+      for (int i = 0; i < NZ; ++i)
+        if (i < nz && col_ok) v[i] = zload(base[warp * comp + i * plane], C());
+      dif_pruned<Z, Z, NZ, -1>(v, tw);
+#pragma unroll
+      for (int p = 0; p < Z; ++p) S[(warp * Z + p) * kZcolCols + lane] = v[p];
+    }
+    __syncthreads();
+    if constexpr (kHoist) {
+#pragma unroll
+      for (int qi = 0; qi < Q; ++qi) {
+        const int p = warp + 5 * qi;
+        if (p < Z) {
+          C* q = S + p * kZcolCols + lane;
+          constexpr int cs = Z * kZcolCols;
+          if constexpr (kRI)
+            tensor_apply_ri(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+          else
+            tensor_apply(gq[qi], q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+        }
+      }
+    } else {
+      for (int p = warp; p < Z; p += 5) {   // position p holds kz = bitrev(p)
+        const int kz = bit_reverse<BITS>(p);
+        GT g[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) g[k] = col_ok ? tens[(((int64_t)ky * Z + kz) * 7 + k) * X + kx] : GT{};
+        C* q = S + p * kZcolCols + lane;
+        constexpr int cs = Z * kZcolCols;
+        if constexpr (kRI)
+          tensor_apply_ri(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+        else
+          tensor_apply(g, q[0], q[cs], q[2 * cs], q[3 * cs], q[4 * cs]);
+      }
+    }
+    __syncthreads();
+    {
+      C v[Z];
+#pragma unroll
+      for (int p = 0; p < Z; ++p) v[p] = S[(warp * Z + p) * kZcolCols + lane];
+      dit_pruned<Z, Z, NZ, +1>(v, tw);
+#pragma unroll
+      for (int i = 0; i < NZ; ++i)
+        if (i < nz && col_ok) base[warp * comp + i * plane] = zstore(v[i], ST());
+    }
+    __syncthreads();   // S is rewritten by the next RHS
+  }
+}
+
+template <typename T, int Z, int NZ, typename ST, typename GT>
+static void launch_zpass_col(ST* Bf, const GT* tens, int nz, int Y, int X, int B, const cplx<T>* tw,
+                             cudaStream_t st) {
+  const size_t sm = (size_t)(Z + 5 * Z * kZcolCols) * sizeof(cplx<T>);
+  allow_dyn_smem(k_zpass_col<T, Z, NZ, ST, GT>, sm);
+  dim3 grid((unsigned)ceil_div(X, kZcolCols), (unsigned)Y);
+  k_zpass_col<T, Z, NZ, ST, GT><<<grid, 5 * kZcolCols, sm, st>>>(Bf, tens, nz, Y, X, B, tw);
   count_launch();
   VH_CUDA_TRY(cudaGetLastError());
 }
@@ -603,6 +708,35 @@ static bool zpass_reg(int Z, int nz, ST* Bf, const GT* tens, int Y, int X, int B
     }
   }
   return false;
+}
+
+// the one-thread-per-column z-pass for Z = 8, 16, 32; false otherwise
+template <typename T, typename ST = cplx<T>, typename GT = cplx<T>>
+static bool zpass_col(int Z, int nz, ST* Bf, const GT* tens, int Y, int X, int B, const cplx<T>* tw,
+                      cudaStream_t st) {
+  int nzb = 2;
+  while (nzb < nz) nzb *= 2;
+  switch (Z * 100 + nzb) {
+    case 802: launch_zpass_col<T, 8, 2>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 804: launch_zpass_col<T, 8, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 1602: launch_zpass_col<T, 16, 2>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 1604: launch_zpass_col<T, 16, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 1608: launch_zpass_col<T, 16, 8>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3202: launch_zpass_col<T, 32, 2>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3204: launch_zpass_col<T, 32, 4>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3208: launch_zpass_col<T, 32, 8>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    case 3216: launch_zpass_col<T, 32, 16>(Bf, tens, nz, Y, X, B, tw, st); return true;
+    default: return false;
+  }
+}
+
+// the z-pass of the launch choice: the one-thread-per-column pass when z_variant is 2 and it takes the
+// length, else the two-lane register pass
+template <typename T, typename ST = cplx<T>, typename GT = cplx<T>>
+static bool zpass_any(int z_variant, int Z, int nz, ST* Bf, const GT* tens, int Y, int X, int B, const cplx<T>* tw,
+                      cudaStream_t st) {
+  if (z_variant == 2 && zpass_col<T, ST, GT>(Z, nz, Bf, tens, Y, X, B, tw, st)) return true;
+  return zpass_reg<T, ST, GT>(Z, nz, Bf, tens, Y, X, B, tw, st);
 }
 
 // pass 5: inverse x-FFT, crop, diagonal term, scatter.
@@ -672,8 +806,8 @@ __global__ void k_inv_x(const cplx<T>* __restrict__ A, const int32_t* __restrict
 }
 
 // the register z-pass in double-float arithmetic on pair storage (vh_conv_df_z.cu)
-bool zpass_df(int Z, int nz, dcomplex* Bf, const dfloat* tens_ri, int Y, int X, int B, const dcomplex* tw,
-              cudaStream_t st);
+bool zpass_df(int z_variant, int Z, int nz, dcomplex* Bf, const dfloat* tens_ri, int Y, int X, int B,
+              const dcomplex* tw, cudaStream_t st);
 
 // true when the double-float product handles the plan: a real/imaginary spectrum, x and y lengths and
 // line counts with compile-time stages and a register z-pass length (else the complex128 product)
@@ -728,7 +862,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const int64_t lines = (int64_t)ny * nz * 5 * B;
     const size_t sm = (size_t)(X + 2 * xpad_len<C>(X * nl)) * sizeof(C) + nl * sizeof(XLine);
     const unsigned grid = (unsigned)ceil_div(lines, nl);
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_fwd_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_dyn_smem(k_fwd_x<T>, sm);
     k_fwd_x<T><<<grid, kPassThreads, sm, st>>>(x, ldx, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, A, p.fx, twp[0], nl);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
@@ -740,7 +874,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const int tx = y_lines_per_cta(Y, X, dbl);
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_dyn_smem(k_pass_y<T, -1>, sm);
     k_pass_y<T, -1><<<grid, kPassThreads, sm, st>>>(A, ny, ny, Bf, Y, Y, X, p.fy, twp[1], tx, y0, 0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
@@ -748,16 +882,17 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   // pass 3 (complex64: the real/imaginary tensor when the spectrum has that form)
   bool z_done = false;
   if constexpr (std::is_same<T, float>::value) {
-    if (p.tens32ri) z_done = zpass_reg<float>(Z, nz, Bf, static_cast<const float*>(p.tens32ri), Y, X, B, twp[2], st);
+    if (p.tens32ri)
+      z_done = zpass_any<float>(p.z_variant_now, Z, nz, Bf, static_cast<const float*>(p.tens32ri), Y, X, B, twp[2], st);
   }
   if constexpr (std::is_same<T, dfloat>::value) {
-    z_done = zpass_df(Z, nz, Bf, static_cast<const dfloat*>(p.tensdf), Y, X, B, twp[2], st);
+    z_done = zpass_df(p.z_variant_now, Z, nz, Bf, static_cast<const dfloat*>(p.tensdf), Y, X, B, twp[2], st);
     VH_REQUIRE(z_done, ERR_UNSUPPORTED, "double-float z-pass length");
-  } else if (!z_done && !zpass_reg<T>(Z, nz, Bf, tens, Y, X, B, twp[2], st)) {
+  } else if (!z_done && !zpass_any<T>(p.z_variant_now, Z, nz, Bf, tens, Y, X, B, twp[2], st)) {
     const int tx = z_lines_per_cta(Z, X);
     const size_t sm = (size_t)(Z + 2 * Z * 5 * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)Y);
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_zpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_dyn_smem(k_zpass<T>, sm);
     k_zpass<T><<<grid, Z * tx, sm, st>>>(Bf, tens, z0, nz, Y, X, B, p.fz, twp[2], tx);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
@@ -769,7 +904,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const int tx = y_lines_per_cta(Y, X, dbl);
     const size_t sm = (size_t)(Y + 2 * Y * tx) * sizeof(C);
     dim3 grid((unsigned)ceil_div(X, tx), (unsigned)(5 * nz * B));
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_pass_y<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_dyn_smem(k_pass_y<T, +1>, sm);
     k_pass_y<T, +1><<<grid, kPassThreads, sm, st>>>(Bf, Y, Y, A, ny, ny, X, p.fy, twp[1], tx, 0, y0);
     count_launch();
     VH_CUDA_TRY(cudaGetLastError());
@@ -780,7 +915,7 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     const int64_t lines = (int64_t)ny * nz * 5 * B;
     const size_t sm = (size_t)(X + 2 * xpad_len<C>(X * nl)) * sizeof(C) + nl * (sizeof(XLine) + sizeof(float2));
     const unsigned grid = (unsigned)ceil_div(lines, nl);
-    VH_CUDA_TRY(cudaFuncSetAttribute(k_inv_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_dyn_smem(k_inv_x<T>, sm);
     k_inv_x<T><<<grid, kPassThreads, sm, st>>>(A, p.vmap, L, M, y0, ny, z0, nz, p.nv, lines, x, ldx, y, ldy, scale, zdiag,
                                       zstride, 1.0 / p.dx, p.fx, twp[0], nl);
     count_launch();
