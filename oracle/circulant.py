@@ -15,7 +15,13 @@ are reproduced below.
 """
 from __future__ import annotations
 
+import os
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
+import scipy.fft as sfft
+
+WORKERS = os.cpu_count() or 1   # the host cores (the reference's MATLAB is multithreaded)
 
 # src_lin_vie/K_near_interactions_1mm.txt (rows: offsets (1,1,1),(1,2,1),(1,2,2),(2,1,1),(2,2,1),(2,2,2);
 # columns: pulse-pulse, linear(x)-pulse, linear(x)-linear(x') for a 1 mm voxel)
@@ -165,9 +171,12 @@ def green_tensor(dx: float, L: int, M: int, N: int, ko: float = 1.0, chunk: int 
     mx, my, mz = np.meshgrid(np.arange(L), np.arange(M), np.arange(N), indexing="ij")
     offs = np.stack([mx.ravel(order="F"), my.ravel(order="F"), mz.ravel(order="F")], axis=1)
     flat = G.reshape(L * M * N, 7, order="F")
-    for s in range(0, offs.shape[0], chunk):
-        o = offs[s:s + chunk]
-        flat[s:s + chunk] = volume_volume_batch(W, pts, KO_GRFN, o * dx, dx)
+
+    def far_chunk(s):   # numpy releases the GIL inside the array operations: chunks run on all cores
+        flat[s:s + chunk] = volume_volume_batch(W, pts, KO_GRFN, offs[s:s + chunk] * dx, dx)
+
+    with ThreadPoolExecutor(max_workers=WORKERS) as ex:
+        list(ex.map(far_chunk, range(0, offs.shape[0], chunk)))
     G = flat.reshape(L, M, N, 7, order="F")
     # medium interactions, 5^6 Gauss-Legendre (:79-310)
     W5, pts5 = weights_points(5, 6)
@@ -227,5 +236,5 @@ def generate_circulant_tensor(dx: float, ko: float, L: int, M: int, N: int, fl_n
     Gp = circulant_embed(G)
     if fl_no_fft:
         return Gp, st
-    fN = np.fft.fftn(Gp, axes=(0, 1, 2))     # fft_operator.m
+    fN = sfft.fftn(Gp, axes=(0, 1, 2), workers=WORKERS)     # fft_operator.m
     return np.asfortranarray(fN), st

@@ -12,6 +12,7 @@ Restates:
 from __future__ import annotations
 
 import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import scipy.fft as sfft
@@ -23,6 +24,45 @@ WORKERS = os.cpu_count() or 1   # FFTs threaded over the host cores (MATLAB's ff
 DIAG_SCALE = np.array([1.0, 1.0, 1.0, 1.0 / 6.0, 1.0 / 2.0])   # lse_matvect_mult.m:99-103
 
 
+def _tensor_products(G, F):
+    """The five output spectra of lse_matvect_mult.m:57-93 from the five input spectra F and the seven
+    tensor components G, element by element in the reference's order of operations; ranges of the
+    grid run on all host cores (numpy releases the GIL inside the array operations)."""
+    shape = F[0].shape
+    n = F[0].size
+    Gf = [g.reshape(-1, order="F") for g in G]
+    Ff = [f.reshape(-1, order="F") for f in F]
+    out = [np.empty(n, dtype=np.complex128) for _ in range(5)]
+
+    def part(a, b):
+        g = [x[a:b] for x in Gf]
+        f = [x[a:b] for x in Ff]
+        J1 = g[0] * f[0]
+        J4 = -g[1] * f[0]
+        J5 = J4.copy()
+        J2 = g[0] * f[1]
+        J4 = J4 - g[2] * f[1]
+        J5 = J5 + g[2] * f[1]
+        J3 = g[0] * f[2]
+        J5 = J5 - g[4] * f[2]
+        J1 = J1 + g[1] * f[3]
+        J2 = J2 + g[2] * f[3]
+        J4 = J4 + g[3] * f[3]
+        J5 = J5 + g[5] * f[3]
+        J1 = J1 + g[1] * f[4]
+        J2 = J2 - g[2] * f[4]
+        J3 = J3 + g[4] * f[4]
+        J4 = J4 + g[5] * f[4]
+        J5 = J5 + g[6] * f[4]
+        for o, J in zip(out, (J1, J2, J3, J4, J5)):
+            o[a:b] = J
+
+    step = max(1 << 16, -(-n // (4 * WORKERS)))
+    with ThreadPoolExecutor(max_workers=WORKERS) as ex:
+        list(ex.map(lambda a: part(a, min(n, a + step)), range(0, n, step)))
+    return [o.reshape(shape, order="F") for o in out]
+
+
 def lse_matvect_mult(JIn0, fN_all, Ae, z_real, z_imag, dx, idx):
     """lse_matvect_mult.m:1-140 (fl_precon_type != 'schur_invert_original')."""
     num_node, num_curr = Ae.shape
@@ -31,31 +71,11 @@ def lse_matvect_mult(JIn0, fN_all, Ae, z_real, z_imag, dx, idx):
     JIn = np.zeros(L * M * N * 5, dtype=np.complex128)
     JIn[idx - 1] = JIn0[:num_curr]
     JIn = JIn.reshape(L, M, N, 5, order="F")
-    f = lambda c: sfft.fftn(JIn[:, :, :, c], s=(LfN, MfN, NfN), workers=WORKERS)
+    F = [sfft.fftn(JIn[:, :, :, c], s=(LfN, MfN, NfN), workers=WORKERS) for c in range(5)]
     G = [fN_all[:, :, :, k] for k in range(7)]
-    fJ = f(0)
-    J1 = G[0] * fJ
-    J4 = -G[1] * fJ
-    J5 = J4.copy()
-    fJ = f(1)
-    J2 = G[0] * fJ
-    J4 = J4 - G[2] * fJ
-    J5 = J5 + G[2] * fJ
-    fJ = f(2)
-    J3 = G[0] * fJ
-    J5 = J5 - G[4] * fJ
-    fJ = f(3)
-    J1 = J1 + G[1] * fJ
-    J2 = J2 + G[2] * fJ
-    J4 = J4 + G[3] * fJ
-    J5 = J5 + G[5] * fJ
-    fJ = f(4)
-    J1 = J1 + G[1] * fJ
-    J2 = J2 - G[2] * fJ
-    J3 = J3 + G[4] * fJ
-    J4 = J4 + G[5] * fJ
-    J5 = J5 + G[6] * fJ
-    outs = [sfft.ifftn(J, workers=WORKERS) for J in (J1, J2, J3, J4, J5)]
+    Js = _tensor_products(G, F)
+    del F
+    outs = [sfft.ifftn(J, workers=WORKERS) for J in Js]
     zz = z_real if z_imag is None else (z_real + z_imag)
     JOut = np.zeros((L, M, N, 5), dtype=np.complex128, order="F")
     with np.errstate(invalid="ignore"):
