@@ -67,7 +67,9 @@ def test_bar_fixture_reproduces_with_the_oracle():
     np.testing.assert_allclose(out["L"], fx["L"][sel], rtol=1e-12)
     d = cf.compare(np.stack(out["x"]), int(fx["nc"]), {k: v[sel] if k.endswith(("sample", "blocks", "norm", "sketch"))
                                                       else v for k, v in fx.items()})
-    assert d["curr_sketch"] < 1e-12 and d["phi_sketch"] < 1e-12, d
+    # x to 1e-10: the fixtures' tensor spectrum came from one FFT implementation, the oracle's from the
+    # multithreaded SciPy one, whose roundings differ at ~1e-12 after a 44-iteration solve
+    assert d["curr_sketch"] < 1e-10 and d["phi_sketch"] < 1e-10, d
 
 
 def test_sketch_estimates_the_relative_difference():
