@@ -241,6 +241,12 @@ vh_status vh_panel_ids(int L, int M, int N, int64_t nv, const int64_t* idxS, int
 /* Ae = lse_compute_Ae_matrix(idxS, all_panels_ids, num_nodes) (lse_compute_Ae_matrix.m:1) as CSC:
  *   jc: 5nv+1, ir (0-based rows) and pr: 16 nv entries each; no device needed.                  */
 vh_status vh_incidence(int64_t nv, const int64_t* all_panels_ids, int64_t* Ae_jc, int64_t* Ae_ir, double* Ae_pr);
+/* Both of the above on the context's device, in one call (the per-request setup of a serving loop):
+ *   all_panels_ids and num_nodes as vh_panel_ids; Ae_jc/Ae_ir/Ae_pr as vh_incidence, or all three NULL
+ *   to skip Ae.  Host buffers; ids are built by prefix sums along each axis's scan order and equal the
+ *   sequential numbering of lse_generate_panelIDs.m:25-172 exactly.  Grids up to 2^31 cells.       */
+vh_status vh_setup_device(vh_ctx* ctx, int L, int M, int N, int64_t nv, const int64_t* idxS, int64_t* all_panels_ids,
+                          int64_t* num_nodes, int64_t* Ae_jc, int64_t* Ae_ir, double* Ae_pr);
 /* [fN_all, st_sparse_precon] = lse_generate_circulant_tensor(dx, 1, L, M, N, 0)
  *   (lse_generate_circulant_tensor.m:1), computed on the device; fN_all (HOST, may be NULL):
  *   complex (2L, 2M, 2N, 7) column-major; st_sparse_precon (HOST, may be NULL): 3 complex.       */

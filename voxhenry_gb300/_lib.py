@@ -60,6 +60,8 @@ SIGNATURES = {
                                            _i64p, _i64p, _dp, _dp, _dp, C.c_int, _dp, C.POINTER(_p)]),
     "vh_panel_ids": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, _i64p, _i64p, _i64p]),
     "vh_incidence": (C.c_int, [C.c_int64, _i64p, _i64p, _i64p, _dp]),
+    "vh_setup_device": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_int64, _i64p, _i64p, _i64p, _i64p, _i64p,
+                                  _dp]),
     "vh_circulant_tensor": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp]),
     "vh_gmres_device": (C.c_int, [_p, C.c_int, C.POINTER(_p), _p, _dp, _ip, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
                                   _p, _ip, _dp, _ip, _dp, C.c_int, _ip]),

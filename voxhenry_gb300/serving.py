@@ -244,7 +244,7 @@ def solve_request(slot: Slot, req: Request, rec: Served, budget: int, prec="fp32
         rec.reused_geometry = True
     else:
         slot.drop()
-        slot.prob = structure.problem_from_workload(w)
+        slot.prob = structure.problem_from_workload(w, ctx=slot.ctx)
     need = footprint_bytes(slot.prob, nf, restart)   # host-only symbolic analysis (vh_schur_analyze)
     if reserve is not None:
         reserve(need)

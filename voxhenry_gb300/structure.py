@@ -48,6 +48,29 @@ def incidence(all_panels_ids, num_nodes) -> sp.csc_matrix:
     return sp.csc_matrix((pr, ir, jc), shape=(num_nodes, 5 * nv))
 
 
+def setup_device(ctx, idxS, L, M, N, with_incidence=True):
+    """Panel ids, num_nodes and (optionally) Ae built on the context's device (vh_setup_device):
+    the same numbers as panel_ids() and incidence()."""
+    lib = _lib.load()
+    idx = np.ascontiguousarray(idxS, dtype=np.int64)
+    nv = idx.size
+    ap = np.zeros(6 * nv, dtype=np.int64)
+    nn = C.c_int64()
+    if with_incidence:
+        jc = np.zeros(5 * nv + 1, dtype=np.int64)
+        ir = np.zeros(16 * nv, dtype=np.int64)
+        pr = np.zeros(16 * nv)
+        bufs = (_lib.i64ptr(jc), _lib.i64ptr(ir), _lib.dptr(pr))
+    else:
+        bufs = (None, None, None)
+    _lib.check(lib.vh_setup_device(ctx.handle, L, M, N, nv, _lib.i64ptr(idx), _lib.i64ptr(ap), C.byref(nn),
+                                   *bufs), ctx.handle)
+    apid = ap.reshape(6, nv).T.copy()
+    if not with_incidence:
+        return apid, nn.value, None
+    return apid, nn.value, sp.csc_matrix((pr, ir, jc), shape=(nn.value, 5 * nv))
+
+
 def _node_ids(idxS, shape, apid, rows):
     L, M, N = shape
     rows = np.asarray(rows, dtype=np.int64).reshape(-1, 4)
@@ -72,9 +95,10 @@ def smooth7(n: int) -> int:
         m += 1
 
 
-def build_problem(sigma_e, lambdaL, dx, pnt_lft, pnt_rght, pnt_well_cond=None, tensor=None, meta=None):
+def build_problem(sigma_e, lambdaL, dx, pnt_lft, pnt_rght, pnt_well_cond=None, tensor=None, meta=None, ctx=None):
     """Inputs of the solve loop.  tensor: (fN_all2, st2) host arrays, or None to leave the tensor to
-    the device (Problem.fN_all2 = None; Sweep then generates it in place).
+    the device (Problem.fN_all2 = None; Sweep then generates it in place).  ctx: a vie.Context to
+    number the panels and build Ae on its device (vh_setup_device), else the host builders.
 
     With the tensor left to the device, a grid whose padded FFT lengths 2L, 2M, 2N have a prime factor
     above 7 is extended with empty voxels at its high ends to the next lengths that do not: the
@@ -94,8 +118,11 @@ def build_problem(sigma_e, lambdaL, dx, pnt_lft, pnt_rght, pnt_well_cond=None, t
         sigma_e = grown
         L, M, N = shape
     idxS = nonempty_voxels(sigma_e, lambdaL)
-    apid, num_nodes = panel_ids(idxS, L, M, N)
-    Ae = incidence(apid, num_nodes)
+    if ctx is not None:
+        apid, num_nodes, Ae = setup_device(ctx, idxS, L, M, N)
+    else:
+        apid, num_nodes = panel_ids(idxS, L, M, N)
+        Ae = incidence(apid, num_nodes)
     nc = Ae.shape[1]
     P = len(pnt_lft)
     rhs = np.zeros((num_nodes + nc, P))
@@ -124,9 +151,9 @@ def build_problem(sigma_e, lambdaL, dx, pnt_lft, pnt_rght, pnt_well_cond=None, t
     return Problem(L, M, N, float(dx), sigma_e, lambdaL, idxS, Ar, rhs, fN, st, meta=m)
 
 
-def problem_from_workload(w, tensor=None) -> Problem:
+def problem_from_workload(w, tensor=None, ctx=None) -> Problem:
     return build_problem(w.sigma_e, w.lambdaL, w.dx, w.pnt_lft, w.pnt_rght, tensor=tensor,
-                         meta={"name": w.name})
+                         meta={"name": w.name}, ctx=ctx)
 
 
 def circulant_tensor(L, M, N, dx, ctx=None):
