@@ -556,8 +556,8 @@ def test_superconductor_sweep_matches_oracle(lib):
     factor, the FFT matvec and GMRES: FP64 R, L and x within 1e-9 of the oracle at 100 MHz and 20 GHz,
     mixed precision within 1e-6.  At 1 kHz the superconducting half is a near-short (|z| ~ 1e-8 of
     copper's), A_inv spans ten decades and the oracle's own true relative residual stops at ~1e-5 even
-    at GMRES tol 1e-14: there two exact factorisations of S (this build's Cholesky, the oracle's SuperLU)
-    lead to solutions ~1e-8 apart, and R, L are compared to 1e-6."""
+    at GMRES tol 1e-14: there any change of rounding (two exact factorisations of S, two FFTs) moves the
+    solution by up to that floor, and R, L are compared to 1e-4."""
     vie, ex = lib
     w = superconducting_bar()
     S, P = problem_of(w)
@@ -566,7 +566,7 @@ def test_superconductor_sweep_matches_oracle(lib):
     sw = ex.Sweep(P, freqs)
     assert sw.super and list(sw.zslot) == [0, 1, 2]
     out = sw.prepare().solve(restart=50, tol=1e-12, maxit=10)
-    for k, bound in enumerate((1e-6, 1e-9, 1e-9)):
+    for k, bound in enumerate((1e-4, 1e-9, 1e-9)):
         assert_port_matrix_close(out["R"][k:k + 1], ref["R"][k:k + 1], bound)
         assert_port_matrix_close(out["L"][k:k + 1], ref["L"][k:k + 1], bound)
     for k in (1, 2):
