@@ -54,9 +54,20 @@ def make(name: str) -> None:
            "t_setup": np.float64(t_setup)}
     out, X, it, rr, t = solve(S, fN, st2, freqs, cf.TOL_REF, cf.MAXIT_REF)
     res.update(Y=out["Y"], Z=out["Z"], R=out["R"], L=out["L"], iters=it, relres=rr, t_solve=np.float64(t))
-    res.update({"x_" + k: v for k, v in cf.fingerprint(X, S.nc).items()})
+    fp = cf.fingerprint(X, S.nc)
+    res.update({"x_" + k: v for k, v in fp.items()})
     print(f"{name}: n={S.n} setup {t_setup:.1f} s, {len(freqs)} freqs x {S.rhs.shape[1]} ports to tol "
           f"{cf.TOL_REF:g} in {t:.1f} s, iterations {it.ravel().tolist()}", flush=True)
+    # sensitivity: the same points solved to tol 1e-12
+    o2, X2, it2, rr2, t2 = solve(S, fN, st2, freqs, cf.TOL_SENS, cf.MAXIT_REF)
+    P = S.rhs.shape[1]
+    rel_port = lambda a, b: np.array([np.abs(a[k] - b[k]).max() / np.abs(b[k]).max() for k in range(b.shape[0])])
+    res["sens_R"] = rel_port(o2["R"], out["R"])
+    res["sens_L"] = rel_port(o2["L"], out["L"])
+    d = cf.compare(X2, S.nc, {"x_" + k: v for k, v in fp.items()})
+    res["sens_x"] = np.float64(max(d["curr_sketch"], d["phi_sketch"]))
+    print(f"{name}: sensitivity (tol {cf.TOL_SENS:g} vs {cf.TOL_REF:g}) R {res['sens_R'].tolist()} "
+          f"L {res['sens_L'].tolist()} x {float(res['sens_x']):.2e} ({t2:.1f} s)", flush=True)
     if "config_tol" in spec:   # the configuration's own GMRES settings (restart 50, maxit 10)
         tc = spec["config_tol"]
         out, X, it, rr, t = solve(S, fN, st2, freqs, tc, 10)

@@ -1,11 +1,16 @@
 """GPU parity on the four benchmark configurations against the oracle's committed fixtures.
 
 The oracle (the FP64 restatement of the reference path) solved each configuration's seeded
-synthetic workload to GMRES tol 1e-12 (tests/golden/make_config_fixtures.py).  Here the GPU solves
-the same frequencies through the batched sweep (executer.Sweep -> vh_gmres) and is held to:
-  * the plain FP64 path at tol 1e-12: R, L and the current density x within 1e-9 relative;
+synthetic workload to GMRES tol 1e-14, and once more to 1e-12 to measure how much each point's
+R, L and x are left undetermined by its conditioning (tests/golden/make_config_fixtures.py).  Here
+the GPU solves the same frequencies through the batched sweep (executer.Sweep -> vh_gmres) and is
+held to:
+  * the plain FP64 path at tol 1e-12: R, L and the current density x within 1e-9 or, where a point
+    is more sensitive, within 10 times the oracle's own change between its two solves (the spiral's
+    20 GHz resistance moves by 1.1e-8 between them, a small real part of a mostly inductive
+    impedance, and its x by up to 6e-9);
   * the mixed-precision path (complex64 FFT matvec inside FP64 refinement, double-float Schur
-    factor) at the benchmark's tol 1e-9: R, L and x within 1e-6 relative;
+    factor) at the benchmark's tol 1e-10: R, L and x within 1e-6;
   * the straight bar at its own settings (tol 1e-8, restart 50, maxit 10): the oracle's iteration
     counts, R and L within 1e-9 of the oracle's at the same settings, and x within 1e-8 (both
     iterates stop at the same step short of convergence, where rounding differences of the two
@@ -61,7 +66,7 @@ def sweep_of(lib, name):
 
 
 def rel_port(a, b):
-    return max(np.abs(a[k] - b[k]).max() / np.abs(b[k]).max() for k in range(b.shape[0]))
+    return np.array([np.abs(a[k] - b[k]).max() / np.abs(b[k]).max() for k in range(b.shape[0])])
 
 
 def check_x(out, fx, nc, bound, prefix="x_"):
@@ -78,13 +83,13 @@ def test_fp64_matches_oracle(lib, name):
     fx, sw = sweep_of(lib, name)
     sw.precon_kind = "schur_invert"
     sw.pcs = None
-    out = sw.prepare().solve(restart=cf.RESTART, tol=cf.TOL_REF, maxit=cf.MAXIT_REF, prec="fp64")
+    out = sw.prepare().solve(restart=cf.RESTART, tol=cf.TOL_SENS, maxit=cf.MAXIT_REF, prec="fp64")
     # the stop is on the preconditioned residual; the true one may end a few times above tol (flag 1),
     # as the oracle's does
-    assert np.all(out["relres"] < 100 * cf.TOL_REF), out["relres"]
-    assert rel_port(out["R"], fx["R"]) < FP64_TOL
-    assert rel_port(out["L"], fx["L"]) < FP64_TOL
-    check_x(out, fx, int(fx["nc"]), FP64_TOL)
+    assert np.all(out["relres"] < 100 * cf.TOL_SENS), out["relres"]
+    assert np.all(rel_port(out["R"], fx["R"]) < cf.bound(fx, "R", FP64_TOL)), (rel_port(out["R"], fx["R"]), fx["sens_R"])
+    assert np.all(rel_port(out["L"], fx["L"]) < cf.bound(fx, "L", FP64_TOL)), (rel_port(out["L"], fx["L"]), fx["sens_L"])
+    check_x(out, fx, int(fx["nc"]), max(FP64_TOL, 10 * float(fx["sens_x"])))
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -92,10 +97,10 @@ def test_mixed_matches_oracle(lib, name):
     fx, sw = sweep_of(lib, name)
     sw.precon_kind = "schur_invert_df"
     sw.pcs = None
-    out = sw.prepare().solve(restart=50, tol=1e-9, maxit=10, prec="fp32")
+    out = sw.prepare().solve(restart=50, tol=1e-10, maxit=10, prec="fp32")
     assert np.all(out["flag"] == 0), out["relres"]
-    assert rel_port(out["R"], fx["R"]) < MIXED_TOL
-    assert rel_port(out["L"], fx["L"]) < MIXED_TOL
+    assert np.all(rel_port(out["R"], fx["R"]) < cf.bound(fx, "R", MIXED_TOL))
+    assert np.all(rel_port(out["L"], fx["L"]) < cf.bound(fx, "L", MIXED_TOL))
     check_x(out, fx, int(fx["nc"]), MIXED_TOL)
 
 
@@ -108,8 +113,8 @@ def test_bar_own_settings_match_oracle(lib):
     out = sw.prepare().solve(restart=50, tol=float(fx["cfg_tol"]), maxit=10, prec="fp64")
     inner = out["iter"][:, 0] + (out["iter"][:, 1] - 1) * 50
     np.testing.assert_array_equal(inner, fx["cfg_iters"].ravel())
-    assert rel_port(out["R"], fx["cfg_R"]) < FP64_TOL
-    assert rel_port(out["L"], fx["cfg_L"]) < FP64_TOL
+    assert np.all(rel_port(out["R"], fx["cfg_R"]) < FP64_TOL)
+    assert np.all(rel_port(out["L"], fx["cfg_L"]) < FP64_TOL)
     check_x(out, fx, int(fx["nc"]), OWN_SETTINGS_X_TOL, prefix="cfgx_")
 
 
