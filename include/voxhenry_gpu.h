@@ -126,7 +126,8 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
  * two products each; inputs are a constant pattern, the timing does not depend on the values),
  * keeps the fastest in the geometry and returns it: y_variant (1 the register y-pass for padded y
  * lengths 256, 512, 1024; 2 the shared-memory Stockham pass), z_variant (1 the two-lane register
- * z-pass; 2 one thread per column, for padded z lengths up to 32) and max_rhs (right-hand sides per
+ * z-pass; 2 one thread per column, for padded z lengths up to 32; 3, complex64 and double-float, the
+ * direct Toeplitz convolution along z for voxel boxes up to 16 rows high) and max_rhs (right-hand sides per
  * launch sequence; 0: the whole batch), and its milliseconds per RHS-matvec.  vh_conv_set_tuning
  * sets a choice without timing (a cached one); zeros restore the defaults.  The products of every
  * choice agree within the precision's rounding.                                                     */

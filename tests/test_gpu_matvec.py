@@ -202,9 +202,10 @@ def test_matvec_df_takes_the_double_float_passes(vie, shape, zr):
 @pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL), ("df", DF_TOL)])
 def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     """Each launch choice the autotuner can make (vh_conv_set_tuning: the register or the Stockham
-    y-pass, the two-lane or the one-thread-per-column z-pass, the whole batch or chunks of 4
-    right-hand sides) gives the FP64 product of the default within the precision's tolerance;
-    vh_conv_tune picks one of them and leaves it set."""
+    y-pass, the two-lane or the one-thread-per-column z-pass or (complex64) the direct Toeplitz z
+    convolution, the whole batch or chunks of 4 right-hand sides) gives the FP64 product of the
+    default within the precision's tolerance; vh_conv_tune picks one of them and leaves it set.
+    A variant a precision does not take (z 3 in FP64) falls back to the automatic pass."""
     import ctypes as C
 
     from voxhenry_gb300 import _lib, executer, geometry, structure
@@ -220,7 +221,7 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     ref = g.matvec(X, scale=scale, prec="fp64")
     lib = g.ctx._lib
     for yv in (1, 2):
-        for zv in (1, 2):
+        for zv in (1, 2, 3):
             for mr in (0, 4):
                 _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], yv, zv, mr), g.ctx.handle)
                 got = g.matvec(X, scale=scale, prec=prec)
@@ -229,7 +230,67 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     yv, zv, mr, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
     _lib.check(lib.vh_conv_tune(g.handle, _lib.PREC[prec], B, C.byref(yv), C.byref(zv), C.byref(mr), C.byref(ms)),
                g.ctx.handle)
-    assert yv.value in (1, 2) and zv.value in (1, 2) and mr.value in (0, 4) and ms.value > 0
+    assert yv.value in (1, 2) and zv.value in ((1, 2) if prec == "fp64" else (1, 2, 3)) and mr.value in (0, 4)
+    assert ms.value > 0
     got = g.matvec(X, scale=scale, prec=prec)
     assert max(rel(got[b], ref[b]) for b in range(B)) < tol
     _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], 0, 0, 0), g.ctx.handle)
+
+
+@pytest.mark.parametrize("shape,fill", [((40, 24, 7), 0.3), ((16, 16, 16), 0.9), ((30, 20, 3), 0.5),
+                                        ((64, 32, 10), 0.4)])
+def test_toeplitz_z_pass_matches_the_fft_product(vie, shape, fill):
+    """The direct z convolution (z_variant 3, complex64) against the oracle's FP64 product, over box
+    heights 3 to 16 (odd heights run with one zero row of padding) and a padded x length (80) that is
+    not a multiple of the kernel's 32 columns.  Its product is not bitwise the
+    FFT z-pass's (a different kernel ran) but within the same complex64 tolerance."""
+    from voxhenry_gb300 import _lib, executer, geometry
+
+    w = geometry.random_blob(shape, fill=fill, seed=31)
+    S = structure.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, _ = circulant.generate_circulant_tensor(S.dx, 1.0, S.L, S.M, S.N)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)
+    rng = np.random.default_rng(5)
+    B = 3
+    X = np.stack([rand_c(rng, g.n) for _ in range(B)])
+    scale = 1j * 2 * np.pi * np.array([1e6, 1e9, 2e10]) * solver.MU0
+    lib = g.ctx._lib
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 1, 0), g.ctx.handle)
+    fft = g.matvec(X, scale=scale, prec="fp32")
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 3, 0), g.ctx.handle)
+    toep = g.matvec(X, scale=scale, prec="fp32")
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0), g.ctx.handle)
+    assert not np.array_equal(fft, toep)
+    for b in range(B):
+        ref = solver.lse_matvect_mult(X[b], scale[b] * fN, S.Ar, z_real, None, S.dx, S.idxS5)
+        assert rel(toep[b], ref) < FP32_TOL, b
+        assert rel(fft[b], ref) < FP32_TOL, b
+
+
+@pytest.mark.parametrize("shape", [(128, 128, 4), (128, 128, 8), (128, 128, 16)])
+def test_toeplitz_z_pass_double_float(vie, shape):
+    """The direct z convolution in double-float arithmetic (z_variant 3 of VH_PREC_DF) on grids the
+    double-float product takes (padded 256 x 256 x 8, 16, 32; box heights 4, 8 and 16): within the
+    double-float tolerance of the oracle's FP64 product, and not bitwise the FFT z-pass's."""
+    from voxhenry_gb300 import _lib, geometry
+
+    w = geometry.random_blob(shape, fill=0.1, seed=17)
+    S = structure.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, _ = circulant.generate_circulant_tensor(S.dx, 1.0, S.L, S.M, S.N)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)
+    rng = np.random.default_rng(8)
+    B = 3
+    X = np.stack([rand_c(rng, g.n) for _ in range(B)])
+    scale = 1j * 2 * np.pi * np.array([1e6, 1e9, 2e10]) * solver.MU0
+    lib = g.ctx._lib
+    fft = g.matvec(X, scale=scale, prec="df")
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["df"], 0, 3, 0), g.ctx.handle)
+    toep = g.matvec(X, scale=scale, prec="df")
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["df"], 0, 0, 0), g.ctx.handle)
+    assert not np.array_equal(fft, toep)
+    for b in range(B):
+        ref = solver.lse_matvect_mult(X[b], scale[b] * fN, S.Ar, z_real, None, S.dx, S.idxS5)
+        assert rel(toep[b], ref) < DF_TOL, b
+        assert rel(fft[b], ref) < DF_TOL, b

@@ -227,6 +227,7 @@ void conv_plan_destroy(ConvPlan& p) {
   cudaFree(p.tens32);
   cudaFree(p.tens32ri);
   cudaFree(p.tensdf);
+  cudaFree(p.tensz);
   cudaFree(p.twdf);
   cudaFree(p.twxdf);
   cudaFree(p.twydf);
@@ -350,6 +351,7 @@ void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, do
   if (prec == PREC_DF && conv_df_supported(p)) ensure_df_tensor(p, st);
   p.y_variant_now = t.y_variant;
   p.z_variant_now = t.z_variant;
+  if (t.z_variant == 3 && (prec == PREC_FP64 || !ztoep_build(p, st))) p.z_variant_now = 0;
   for (int b0 = 0; b0 < B; b0 += w) {
     const int nb = std::min(w, B - b0);
     const double2* xb = x + (int64_t)b0 * ldx;

@@ -23,8 +23,12 @@ bool fft_factor(int n, FftDesc& d);
 struct ConvTuning {
   int y_variant = 0;
   int max_rhs = 0;
-  int z_variant = 0;   // 0 automatic = 1 the two-lane register z-pass; 2 one thread per column (Z <= 32)
+  int z_variant = 0;   // 0 automatic = 1 the two-lane register z-pass; 2 one thread per column (Z <= 32);
+                       // 3 (complex64, double-float) the direct Toeplitz convolution along z
+                       // (nz <= kZtoepMaxRows)
 };
+
+constexpr int kZtoepMaxRows = 16;
 
 struct ConvPlan {
   int L = 0, M = 0, N = 0;   // voxel grid
@@ -48,6 +52,11 @@ struct ConvPlan {
   bool ri = false;            // the spectrum has the real/imaginary form above (checked at creation)
   void* tensdf = nullptr;     // double-float real/imaginary tensor (one pair of floats per component,
                               // layout as tens32ri), built on first PREC_DF use when ri holds
+  // z_variant 3: h_k(kx, ky, d) = sum_kz S_k e^{+2 pi i kz d / Z} for 0 <= d < nz, one float per value
+  // (real, or the imaginary part for components 1 and 2), layout [ky][k][d][kx], followed by the
+  // low floats of the same values as double-float pairs; built on first use
+  float* tensz = nullptr;
+  int ztoep_state = 0;        // 0 not built, 1 built, -1 not available (nz too large or form check failed)
   void* twdf = nullptr;       // double-float z twiddles
   void* twxdf = nullptr;      // double-float x and y twiddles
   void* twydf = nullptr;
@@ -91,6 +100,14 @@ void conv_scratch_bytes(const ConvPlan& p, Prec prec, size_t& a_per_rhs, size_t&
 void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, double2* y, int64_t ldy,
                         const double2* scale, const double2* zdiag, int64_t zstride, void* scratchA, void* scratchB,
                         cudaStream_t st);
+
+// The z-pass of z_variant 3 (complex64): builds the Toeplitz table on first call (false when the
+// geometry does not take it), and the pass itself on Bf (false when the table is not built).
+bool ztoep_build(ConvPlan& p, cudaStream_t st);
+bool zpass_toep(const ConvPlan& p, float2* Bf, int B, cudaStream_t st);
+// the same in double-float arithmetic on pair storage (PREC_DF)
+struct dcomplex;
+bool zpass_toep_df(const ConvPlan& p, dcomplex* Bf, int B, cudaStream_t st);
 
 // In-place forward 3-D FFT of `batch` column-major X x Y x Z complex arrays (device).
 void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaStream_t st);

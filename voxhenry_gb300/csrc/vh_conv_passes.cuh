@@ -882,11 +882,13 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   // pass 3 (complex64: the real/imaginary tensor when the spectrum has that form)
   bool z_done = false;
   if constexpr (std::is_same<T, float>::value) {
-    if (p.tens32ri)
+    if (p.z_variant_now == 3) z_done = zpass_toep(p, Bf, B, st);
+    if (!z_done && p.tens32ri)
       z_done = zpass_any<float>(p.z_variant_now, Z, nz, Bf, static_cast<const float*>(p.tens32ri), Y, X, B, twp[2], st);
   }
   if constexpr (std::is_same<T, dfloat>::value) {
-    z_done = zpass_df(p.z_variant_now, Z, nz, Bf, static_cast<const dfloat*>(p.tensdf), Y, X, B, twp[2], st);
+    if (p.z_variant_now == 3) z_done = zpass_toep_df(p, Bf, B, st);
+    if (!z_done) z_done = zpass_df(p.z_variant_now, Z, nz, Bf, static_cast<const dfloat*>(p.tensdf), Y, X, B, twp[2], st);
     VH_REQUIRE(z_done, ERR_UNSUPPORTED, "double-float z-pass length");
   } else if (!z_done && !zpass_any<T>(p.z_variant_now, Z, nz, Bf, tens, Y, X, B, twp[2], st)) {
     const int tx = z_lines_per_cta(Z, X);

@@ -108,6 +108,7 @@ __device__ __forceinline__ bool operator>(dfloat a, dfloat b) { return a.hi > b.
 // dependency is a single addition per term (a pair fma carries about nine dependent operations).
 struct df_dot {
   float s, c;
+  df_dot() = default;   // uninitialised (arrays of accumulators set before use)
   __device__ __forceinline__ explicit df_dot(dfloat init) : s(init.hi), c(init.lo) {}
   // += a * b
   __device__ __forceinline__ void add(dfloat a, dfloat b) {
