@@ -912,6 +912,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps, (STAGE || std::is_same<T, do
 constexpr int kWideWarps = 8;
 constexpr size_t kWarpSolveSmemMax = 160 * 1024;   // warp-per-front CTAs above this go wide
 constexpr int kWideMaxFronts = 16;   // levels with at most this many fronts take the wide kernels
+constexpr int kWideItemsPerSm = 4;   // ... and levels with at most this many (front, RHS) items per SM
 
 template <typename T>
 struct WideSmem {
@@ -1139,8 +1140,18 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
   };
   // a level of few fronts, or of fronts whose per-warp vectors do not fit four to a CTA, takes the
   // wide kernels (one CTA per front and RHS)
+  // ... or a level whose (front, RHS) items number at most kWideItemsPerSm per SM: one warp per item
+  // would leave each SM a few warps streaming long panels (measured on the ring and two-bar sweeps:
+  // 400-800 items at 152 SMs cut the apply by 7-10 %, 3200 items lost again)
+  static const int64_t wide_items = [] {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    return (int64_t)kWideItemsPerSm * sms;
+  }();
   auto wide = [&](size_t h) {
-    return (int)s.levels[h].size() <= kWideMaxFronts || warp_smem(h, false) > kWarpSolveSmemMax;
+    return (int)s.levels[h].size() <= kWideMaxFronts || warp_smem(h, false) > kWarpSolveSmemMax ||
+           (int64_t)s.levels[h].size() * B <= wide_items;
   };
   // a wide level stages its panels when the largest (max ns columns of odd leading dimension) fits
   auto wide_smem = [&](size_t h, bool staged) {
