@@ -1004,7 +1004,8 @@ __global__ void __launch_bounds__(32 * kWideWarps)
       yb[lane] = tv;
     }
     __syncthreads();
-    for (int r = j0 + w + tid; r < nf; r += NT) {
+    // the block's update of the pivot rows below it (the boundary rows follow in one pass)
+    for (int r = j0 + w + tid; r < ns; r += NT) {
       const T* Lr = F + r + (int64_t)j0 * ld;
       T lv[kBlk];
 #pragma unroll
@@ -1020,6 +1021,29 @@ __global__ void __launch_bounds__(32 * kWideWarps)
     }
     __syncthreads();
   }
+  // the boundary rows: t_r -= sum_{j < ns} L(r, j) y_j in one pass over the front's off-diagonal part
+  // (each thread a row, the columns in groups of kBlk loads in flight), instead of one slice per
+  // block step: the steps above then walk only the pivot rows
+  for (int r = ns + tid; r < nf; r += NT) {
+    Dot ax(t[r].x), ay(t[r].y);
+    for (int j0 = 0; j0 < ns; j0 += kBlk) {
+      const int w = min(kBlk, ns - j0);
+      const T* Lr = F + r + (int64_t)j0 * ld;
+      T lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * ld] : T(0);
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        if (k < w) {
+          const C y = t[j0 + k];
+          ax.add(-lv[k], y.x);
+          ay.add(-lv[k], y.y);
+        }
+    }
+    t[r].x = ax.value();
+    t[r].y = ay.value();
+  }
+  __syncthreads();
   for (int j = tid; j < ns; j += NT) xb[rw[j]] = t[j];
   for (int a = tid; a < f.nb; a += NT) {
     const C v = t[ns + a];
