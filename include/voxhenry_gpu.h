@@ -125,7 +125,8 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
  * batch of B right-hand sides with CUDA events on the context stream (one warm-up and the best of
  * two products each; inputs are a constant pattern, the timing does not depend on the values),
  * keeps the fastest in the geometry and returns it: y_variant (1 the register y-pass for padded y
- * lengths 256, 512, 1024; 2 the shared-memory Stockham pass), z_variant (1 the two-lane register
+ * lengths 256, 512, 1024; 2 the shared-memory Stockham pass; 3 the register y-pass over 64-byte row
+ * segments), z_variant (1 the two-lane register
  * z-pass; 2 one thread per column, for padded z lengths up to 32; 3, complex64 and double-float, the
  * direct Toeplitz convolution along z for voxel boxes up to 16 rows high) and max_rhs (right-hand sides per
  * launch sequence; 0: the whole batch), and its milliseconds per RHS-matvec.  vh_conv_set_tuning

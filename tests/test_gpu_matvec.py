@@ -201,8 +201,8 @@ def test_matvec_df_takes_the_double_float_passes(vie, shape, zr):
 
 @pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL), ("df", DF_TOL)])
 def test_every_tuning_choice_gives_the_product(vie, prec, tol):
-    """Each launch choice the autotuner can make (vh_conv_set_tuning: the register or the Stockham
-    y-pass, the two-lane or the one-thread-per-column z-pass or (complex64) the direct Toeplitz z
+    """Each launch choice the autotuner can make (vh_conv_set_tuning: the register y-pass over 128- or
+    64-byte row segments or the Stockham y-pass, the two-lane or the one-thread-per-column z-pass or (complex64) the direct Toeplitz z
     convolution, the whole batch or chunks of 4 right-hand sides) gives the FP64 product of the
     default within the precision's tolerance; vh_conv_tune picks one of them and leaves it set.
     A variant a precision does not take (z 3 in FP64) falls back to the automatic pass."""
@@ -220,7 +220,7 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     scale = 1j * 2 * np.pi * np.logspace(6, 10, B) * solver.MU0
     ref = g.matvec(X, scale=scale, prec="fp64")
     lib = g.ctx._lib
-    for yv in (1, 2):
+    for yv in (1, 2, 3):
         for zv in (1, 2, 3):
             for mr in (0, 4):
                 _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], yv, zv, mr), g.ctx.handle)
@@ -230,7 +230,7 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     yv, zv, mr, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
     _lib.check(lib.vh_conv_tune(g.handle, _lib.PREC[prec], B, C.byref(yv), C.byref(zv), C.byref(mr), C.byref(ms)),
                g.ctx.handle)
-    assert yv.value in (1, 2) and zv.value in ((1, 2) if prec == "fp64" else (1, 2, 3)) and mr.value in (0, 4)
+    assert yv.value in (1, 2, 3) and zv.value in ((1, 2) if prec == "fp64" else (1, 2, 3)) and mr.value in (0, 4)
     assert ms.value > 0
     got = g.matvec(X, scale=scale, prec=prec)
     assert max(rel(got[b], ref[b]) for b in range(B)) < tol

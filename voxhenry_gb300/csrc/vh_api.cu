@@ -232,12 +232,12 @@ const char* vh_last_error(const vh_ctx* ctx) { return ctx ? ctx->last_error.c_st
 vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_variant, int max_rhs) {
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
-    VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && y_variant >= 0 && y_variant <= 2 && z_variant >= 0 &&
+    VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && y_variant >= 0 && y_variant <= 3 && z_variant >= 0 &&
                    z_variant <= 3 && max_rhs >= 0,
                ERR_BAD_ARG, "bad tuning");
     VH_REQUIRE(g->has_conv, ERR_BAD_ARG, "geometry was created without a circulant tensor");
     const int Y = g->conv.Y;
-    VH_REQUIRE(y_variant != 1 || Y == 256 || Y == 512 || Y == 1024, ERR_UNSUPPORTED,
+    VH_REQUIRE((y_variant != 1 && y_variant != 3) || Y == 256 || Y == 512 || Y == 1024, ERR_UNSUPPORTED,
                "the register y-pass takes padded y lengths 256, 512 and 1024");
     g->conv.tune[prec] = ConvTuning{y_variant, max_rhs, z_variant};
   });
@@ -264,8 +264,8 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_v
     const bool reg_ok = p.Y == 256 || p.Y == 512 || p.Y == 1024;
     const bool col_ok = p.Z <= 32;   // the one-thread-per-column z-pass takes Z = 8, 16, 32
     const bool toep_ok = pr != PREC_FP64 && ztoep_build(p, st);   // the direct z convolution (nz <= 16)
-    for (int yv : {1, 2}) {
-      if (yv == 1 && !reg_ok) continue;
+    for (int yv : {1, 2, 3}) {
+      if (yv != 2 && !reg_ok) continue;
       for (int zv : {1, 2, 3}) {
         if ((zv == 2 && !col_ok) || (zv == 3 && !toep_ok)) continue;
         cands.push_back(ConvTuning{yv, 0, zv});

@@ -17,7 +17,9 @@ bool fft_factor(int n, FftDesc& d);
 
 // Launch choices of the FFT convolution at one precision, set by the autotuner (vh_conv_tune) or from
 // its cache (vh_conv_set_tuning): the y-pass (0 automatic = the register pass where Y is 256, 512 or
-// 1024; 1 the register pass; 2 the shared-memory Stockham pass), the z-pass (z_variant) and the
+// 1024, over 64-byte row segments for complex64; 1 the register pass over 128-byte row segments; 2 the
+// shared-memory Stockham pass; 3 the register pass over 64-byte row segments), the z-pass (z_variant)
+// and the
 // right-hand sides per launch sequence (0: the whole batch; else chunks of at most max_rhs, which
 // keeps the spectra of a chunk smaller at the price of reading the tensor once per chunk).
 struct ConvTuning {
