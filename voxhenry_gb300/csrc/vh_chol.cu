@@ -929,6 +929,7 @@ struct WideSmem {
 // round trips per 32-column block.  The staged panel's leading dimension is odd, so that lanes
 // walking columns (the backward updates) hit distinct banks.
 constexpr size_t kWideStageMax = 220 * 1024;   // shared memory of a staged wide CTA
+constexpr size_t kPipeSmemMax = 224 * 1024;    // ... and of a slab-pipelined one
 __host__ __device__ __forceinline__ int staged_ld(int nf) { return nf | 1; }
 
 template <typename T>
@@ -1032,6 +1033,140 @@ __global__ void __launch_bounds__(32 * kWideWarps)
       T lv[kBlk];
 #pragma unroll
       for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * ld] : T(0);
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        if (k < w) {
+          const C y = t[j0 + k];
+          ax.add(-lv[k], y.x);
+          ay.add(-lv[k], y.y);
+        }
+    }
+    t[r].x = ax.value();
+    t[r].y = ay.value();
+  }
+  __syncthreads();
+  for (int j = tid; j < ns; j += NT) xb[rw[j]] = t[j];
+  for (int a = tid; a < f.nb; a += NT) {
+    const C v = t[ns + a];
+    C nv;
+    nv.x = -v.x;
+    nv.y = -v.y;
+    Ub[f.u_off + a] = nv;
+  }
+}
+
+// The wide forward solve for fronts too large to stage whole: the pivot-block steps read 32-column
+// slabs of the panel (columns j0 .. j0 + 31, rows j0 .. ns - 1) from shared memory, and the next slab
+// is copied with cp.async while the current step computes (two slabs of `sl` rows), so that no step
+// waits on global memory; the boundary rows then take one streaming pass over the off-diagonal part.
+template <typename T>
+struct PipeSmem {
+  static __host__ __device__ size_t bytes(int max_nf, int sl) {
+    return WideSmem<T>::vec_bytes(max_nf) + ((kBlk * sizeof(cplx<T>) + 15) & ~(size_t)15) +
+           2 * (size_t)kBlk * sl * sizeof(T);
+  }
+};
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps)
+    k_chol_fsolve_wide_pipe(const int32_t* __restrict__ lev, int nlev, const FrontInfo* __restrict__ fr,
+                            const int32_t* __restrict__ rows, const int32_t* __restrict__ relmap,
+                            T* const* __restrict__ Wp, cplx<T>* __restrict__ x, int64_t ldx, int64_t xoff,
+                            cplx<T>* __restrict__ U, int64_t u_total, int max_nf, int sl) {
+  using C = cplx<T>;
+  using Dot = typename dot_of<T>::type;
+  constexpr int NT = 32 * kWideWarps;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* t = reinterpret_cast<C*>(smem_raw);
+  C* yb = reinterpret_cast<C*>(smem_raw + WideSmem<T>::vec_bytes(max_nf));
+  T* slab0 = reinterpret_cast<T*>(smem_raw + WideSmem<T>::vec_bytes(max_nf) +
+                                  ((kBlk * sizeof(C) + 15) & ~(size_t)15));
+  T* slabs[2] = {slab0, slab0 + (size_t)kBlk * sl};
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const FrontInfo f = fr[lev[blockIdx.x % nlev]];
+  const int b = (int)(blockIdx.x / nlev);
+  const T* F = Wp[b] + f.w_off;
+  C* xb = x + b * ldx + xoff;
+  C* Ub = U + b * u_total;
+  const int32_t* rw = rows + f.rows_off;
+  const int nf = f.nf, ns = f.ns;
+  auto stage = [&](int j0, T* dst) {   // slab of step j0: element (i, k) = L(j0 + i, j0 + k) at dst[k sl + i]
+    const int w = min(kBlk, ns - j0), h = ns - j0;
+    for (int q = tid; q < w * h; q += NT) {
+      const int k = q / h, i = q - k * h;
+      cp_async8(dst + k * sl + i, F + (j0 + i) + (int64_t)(j0 + k) * nf);
+    }
+    cp_async_commit();
+  };
+  stage(0, slabs[0]);
+  for (int r = tid; r < nf; r += NT) t[r] = r < ns ? xb[rw[r]] : czero<C>();
+  __syncthreads();
+  for (int c = 0; c < 2; ++c) {
+    if (f.child[c] < 0) continue;
+    const FrontInfo ch = fr[f.child[c]];
+    const int32_t* rm = relmap + ch.relmap_off;
+    for (int a = tid; a < ch.nb; a += NT) {   // distinct targets within one child
+      const C u = Ub[ch.u_off + a];
+      C& tv = t[rm[a]];
+      tv.x -= u.x;
+      tv.y -= u.y;
+    }
+    __syncthreads();
+  }
+  int buf = 0;
+  for (int j0 = 0; j0 < ns; j0 += kBlk, buf ^= 1) {
+    const int w = min(kBlk, ns - j0);
+    cp_async_wait0();
+    __syncthreads();   // slab j0 in shared memory; every thread is done with the previous step
+    if (j0 + kBlk < ns) stage(j0 + kBlk, slabs[buf ^ 1]);
+    const T* S = slabs[buf];
+    if (warp == 0) {   // y_blk = L_blk^-1 t_blk (stored inverse), lane i owns row i
+      T lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = (k < w && lane < w && lane >= k) ? S[k * sl + lane] : T(0);
+      yb[lane] = lane < w ? t[j0 + lane] : czero<C>();
+      __syncwarp();
+      Dot tx(T(0)), ty(T(0));
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k)
+        if (k < w) {
+          tx.add(lv[k], yb[k].x);
+          ty.add(lv[k], yb[k].y);
+        }
+      C tv;
+      tv.x = tx.value();
+      tv.y = ty.value();
+      __syncwarp();
+      if (lane < w) t[j0 + lane] = tv;
+      yb[lane] = tv;
+    }
+    __syncthreads();
+    for (int r = j0 + w + tid; r < ns; r += NT) {
+      T lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? S[k * sl + (r - j0)] : T(0);
+      Dot ax(t[r].x), ay(t[r].y);
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) {
+        ax.add(-lv[k], yb[k].x);
+        ay.add(-lv[k], yb[k].y);
+      }
+      t[r].x = ax.value();
+      t[r].y = ay.value();
+    }
+  }
+  __syncthreads();
+  for (int r = ns + tid; r < nf; r += NT) {   // the boundary rows in one pass (as k_chol_fsolve_wide)
+    Dot ax(t[r].x), ay(t[r].y);
+    for (int j0 = 0; j0 < ns; j0 += kBlk) {
+      const int w = min(kBlk, ns - j0);
+      const T* Lr = F + r + (int64_t)j0 * nf;
+      T lv[kBlk];
+#pragma unroll
+      for (int k = 0; k < kBlk; ++k) lv[k] = k < w ? Lr[(int64_t)k * nf] : T(0);
 #pragma unroll
       for (int k = 0; k < kBlk; ++k)
         if (k < w) {
@@ -1183,11 +1318,15 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
     return staged ? base + (size_t)s.level_max_ns[h] * staged_ld(s.level_max_nf[h]) * sizeof(T) : base;
   };
   auto wide_stage = [&](size_t h) { return wide_smem(h, true) <= kWideStageMax; };
-  size_t sm_f[2] = {0, 0}, sm_b[2] = {0, 0}, sm_w[2] = {0, 0};
+  // a wide level too large to stage whole pipelines two 32-column slabs of its panels when they fit
+  auto pipe_smem = [&](size_t h) { return PipeSmem<T>::bytes(s.level_max_nf[h], s.level_max_ns[h]); };
+  auto pipe_ok = [&](size_t h) { return pipe_smem(h) <= kPipeSmemMax; };
+  size_t sm_f[2] = {0, 0}, sm_b[2] = {0, 0}, sm_w[2] = {0, 0}, sm_p = 0;
   for (size_t h = 0; h < s.levels.size(); ++h) {
     if (wide(h)) {
       const bool ws = wide_stage(h);
       sm_w[ws] = std::max(sm_w[ws], wide_smem(h, ws));
+      if (!ws && pipe_ok(h)) sm_p = std::max(sm_p, pipe_smem(h));
     } else {
       sm_f[stage(h)] = std::max(sm_f[stage(h)], warp_smem(h, true));
       sm_b[stage(h)] = std::max(sm_b[stage(h)], warp_smem(h, false));
@@ -1206,6 +1345,7 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
     allow_dyn_smem(k_chol_fsolve_wide<T, true>, sm_w[1]);
     allow_dyn_smem(k_chol_bsolve_wide<T, true>, sm_w[1]);
   }
+  if (sm_p) allow_dyn_smem(k_chol_fsolve_wide_pipe<T>, sm_p);
   for (size_t h = 0; h < s.levels.size(); ++h) {
     const int nlev = (int)s.levels[h].size();
     const int mnf = s.level_max_nf[h];
@@ -1214,6 +1354,10 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       if (wide_stage(h))
         k_chol_fsolve_wide<T, true><<<g, 32 * kWideWarps, wide_smem(h, true), st>>>(
             s.d_levels[h], nlev, s.d_fronts, s.d_rows, s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf);
+      else if (pipe_ok(h))
+        k_chol_fsolve_wide_pipe<T><<<g, 32 * kWideWarps, pipe_smem(h), st>>>(
+            s.d_levels[h], nlev, s.d_fronts, s.d_rows, s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf,
+            s.level_max_ns[h]);
       else
         k_chol_fsolve_wide<T, false><<<g, 32 * kWideWarps, wide_smem(h, false), st>>>(
             s.d_levels[h], nlev, s.d_fronts, s.d_rows, s.d_relmap, Wp, x, ldx, xoff, U, s.u_total, mnf);
@@ -1242,6 +1386,7 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       if (wide_stage(hh))
         k_chol_bsolve_wide<T, true><<<g, 32 * kWideWarps, wide_smem(hh, true), st>>>(
             s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf, xd, ldxd);
+
       else
         k_chol_bsolve_wide<T, false><<<g, 32 * kWideWarps, wide_smem(hh, false), st>>>(
             s.d_levels[hh], nlev, s.d_fronts, s.d_rows, Wp, x, ldx, xoff, mnf, xd, ldxd);
