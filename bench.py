@@ -508,17 +508,20 @@ def run_ours(args, rank, world):
 
 def serving_run(args):
     """The serving configuration (continuous batching, voxhenry_gb300.serving.Server) on the seeded
-    2000-request stream: a calibration sample served at saturation on one slot and on the server's
-    slots (the speed-up of overlapping requests on the device), then the stream's next requests arriving
-    as a seeded Poisson process at 80 % of the measured capacity, replayed on the wall clock: p50/p99
-    latency = completion - arrival."""
+    2000-request stream: a calibration sample of the replayed requests served at saturation on one slot
+    and on the server's slots (the speed-up of overlapping requests on the device), then the stream's
+    first requests arriving as a seeded Poisson process at 80 % of the measured capacity, replayed on the
+    wall clock: p50/p99 latency = completion - arrival."""
     from voxhenry_gb300 import serving
 
     slots = args.serving_slots
     n_cal = args.serving_calibration
     n = args.serving_requests
-    reqs = serving.request_stream(n_cal + n)
-    cal, stream = reqs[:n_cal], reqs[n_cal:]
+    # the replayed requests are the stream's first n; the capacity is measured on n_cal of them taken
+    # evenly over that range (request sizes drift along the stream, so its head is not representative)
+    stream = serving.request_stream(n)
+    step = max(1, n // max(1, n_cal))
+    cal = stream[::step][:n_cal]
     out = {"slots": slots}
     srv1 = serving.Server(slots=1, tol=TOL)
     t0 = time.perf_counter()
@@ -549,9 +552,10 @@ def serving_run(args):
     out["p50_latency_s"] = summ["p50_latency_s"]
     out["p99_latency_s"] = summ["p99_latency_s"]
     out["freq_points_per_s"] = summ["freq_points_per_s"]
-    out["sample"] = (f"requests {n_cal}..{n_cal + n - 1} of the seeded 2000-request stream (bars, wires, square "
+    out["sample"] = (f"requests 0..{n - 1} of the seeded 2000-request stream (bars, wires, square "
                      f"spirals; {summ['freq_points']} frequency points) arriving as a seeded Poisson process at 80 % of "
-                     f"the capacity measured on requests 0..{n_cal - 1}, replayed on the wall clock; mixed precision at "
+                     f"the capacity measured on {len(cal)} of them (every {step}th), replayed on the wall clock; "
+                     f"mixed precision at "
                      f"GMRES tol {TOL:g}; {slots} slots (library contexts, one CUDA stream each) admitted first come first "
                      "served by device-memory footprint; latency = completion - arrival")
     return out
@@ -689,9 +693,9 @@ def run_probe(args):
     y = torch.empty_like(x)
     if args.probe in ("conv32", "conv64", "convdf"):
         prec = _lib.PREC[{"conv32": "fp32", "conv64": "fp64", "convdf": "df"}[args.probe]]
-        if args.probe_tuning:   # y-pass variant, z-pass variant, right-hand sides per launch
-            yv, zv, mr = (int(t) for t in args.probe_tuning.split(","))
-            _lib.check(lib.vh_conv_set_tuning(g.handle, prec, yv, zv, mr), g.ctx.handle)
+        if args.probe_tuning:   # y-pass variant, z-pass variant, right-hand sides per launch[, x variant]
+            t = [int(v) for v in args.probe_tuning.split(",")] + [0]
+            _lib.check(lib.vh_conv_set_tuning(g.handle, prec, t[0], t[1], t[2], t[3]), g.ctx.handle)
         for _ in range(args.probe_iters):
             _lib.check(lib.vh_matvec_device(g.handle, B, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), None,
                                             None, prec), g.ctx.handle)
@@ -746,7 +750,7 @@ def main():
     ap.add_argument("--probe-iters", type=int, default=3)
     ap.add_argument("--probe-restart", type=int, default=20)
     ap.add_argument("--probe-tuning", default=None,
-                    help="conv probes: 'y,z,max_rhs' as vh_conv_set_tuning takes them (default: untuned)")
+                    help="conv probes: 'y,z,max_rhs[,x]' as vh_conv_set_tuning takes them (default: untuned)")
     ap.add_argument("--probe-kind", default="schur_invert", choices=["schur_invert", "schur_invert_df"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)

@@ -128,13 +128,14 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
  * lengths 256, 512, 1024; 2 the shared-memory Stockham pass; 3 the register y-pass over 64-byte row
  * segments), z_variant (1 the two-lane register
  * z-pass; 2 one thread per column, for padded z lengths up to 32; 3, complex64 and double-float, the
- * direct Toeplitz convolution along z for voxel boxes up to 16 rows high) and max_rhs (right-hand sides per
- * launch sequence; 0: the whole batch), and its milliseconds per RHS-matvec.  vh_conv_set_tuning
+ * direct Toeplitz convolution along z for voxel boxes up to 16 rows high), max_rhs (right-hand sides per
+ * launch sequence; 0: the whole batch), x_variant (complex64: 0 the shared-memory x passes, 1 one warp
+ * per line for padded x lengths 256, 512, 1024), and its milliseconds per RHS-matvec.  vh_conv_set_tuning
  * sets a choice without timing (a cached one); zeros restore the defaults.  The products of every
  * choice agree within the precision's rounding.                                                     */
 vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_variant, int* max_rhs,
-                       double* ms_per_rhs);
-vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_variant, int max_rhs);
+                       int* x_variant, double* ms_per_rhs);
+vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_variant, int max_rhs, int x_variant);
 
 /* ---- allocation-free matvec (no counterpart in the reference) -----------------------------------
  * The operator of vh_matvec_device, same arguments and results for VH_PREC_FP64 and VH_PREC_FP32,

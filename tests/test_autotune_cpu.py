@@ -29,7 +29,7 @@ def test_tune_times_once_then_uses_the_cache(tmp_path):
     a = autotune.tune(g, "fp32", 12, (64, 16, 16), (16, 16), path=path, timer=timer)
     assert a["cached"] is False and calls == [("fp32", 12)]
     b = autotune.tune(g, "fp32", 16, (64, 16, 16), (16, 16), path=path, timer=timer)   # same bucket
-    assert b["cached"] is True and len(calls) == 1 and g.tuning == ("fp32", 2, 1, 8)
+    assert b["cached"] is True and len(calls) == 1 and g.tuning == ("fp32", 2, 1, 8, 0)
     autotune.tune(g, "fp32", 12, (64, 16, 16), (16, 16), path=path, timer=timer, retune=True)
     assert len(calls) == 2
     d = json.load(open(path))

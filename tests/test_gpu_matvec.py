@@ -203,7 +203,8 @@ def test_matvec_df_takes_the_double_float_passes(vie, shape, zr):
 def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     """Each launch choice the autotuner can make (vh_conv_set_tuning: the register y-pass over 128- or
     64-byte row segments or the Stockham y-pass, the two-lane or the one-thread-per-column z-pass or (complex64) the direct Toeplitz z
-    convolution, the whole batch or chunks of 4 right-hand sides) gives the FP64 product of the
+    convolution, the shared-memory or (complex64) warp-per-line x passes, the whole batch or chunks of 4
+    right-hand sides) gives the FP64 product of the
     default within the precision's tolerance; vh_conv_tune picks one of them and leaves it set.
     A variant a precision does not take (z 3 in FP64) falls back to the automatic pass."""
     import ctypes as C
@@ -223,18 +224,19 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     for yv in (1, 2, 3):
         for zv in (1, 2, 3):
             for mr in (0, 4):
-                _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], yv, zv, mr), g.ctx.handle)
-                got = g.matvec(X, scale=scale, prec=prec)
-                for b in range(B):
-                    assert rel(got[b], ref[b]) < tol, (yv, zv, mr, b)
-    yv, zv, mr, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
-    _lib.check(lib.vh_conv_tune(g.handle, _lib.PREC[prec], B, C.byref(yv), C.byref(zv), C.byref(mr), C.byref(ms)),
-               g.ctx.handle)
+                for xv in ((0, 1) if prec == "fp32" else (0,)):
+                    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], yv, zv, mr, xv), g.ctx.handle)
+                    got = g.matvec(X, scale=scale, prec=prec)
+                    for b in range(B):
+                        assert rel(got[b], ref[b]) < tol, (yv, zv, mr, xv, b)
+    yv, zv, mr, xv, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_double()
+    _lib.check(lib.vh_conv_tune(g.handle, _lib.PREC[prec], B, C.byref(yv), C.byref(zv), C.byref(mr), C.byref(xv),
+                                C.byref(ms)), g.ctx.handle)
     assert yv.value in (1, 2, 3) and zv.value in ((1, 2) if prec == "fp64" else (1, 2, 3)) and mr.value in (0, 4)
-    assert ms.value > 0
+    assert ms.value > 0 and xv.value in ((0, 1) if prec == "fp32" else (0,))
     got = g.matvec(X, scale=scale, prec=prec)
     assert max(rel(got[b], ref[b]) for b in range(B)) < tol
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], 0, 0, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], 0, 0, 0, 0), g.ctx.handle)
 
 
 @pytest.mark.parametrize("shape,fill", [((40, 24, 7), 0.3), ((16, 16, 16), 0.9), ((30, 20, 3), 0.5),
@@ -256,11 +258,11 @@ def test_toeplitz_z_pass_matches_the_fft_product(vie, shape, fill):
     X = np.stack([rand_c(rng, g.n) for _ in range(B)])
     scale = 1j * 2 * np.pi * np.array([1e6, 1e9, 2e10]) * solver.MU0
     lib = g.ctx._lib
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 1, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 1, 0, 0), g.ctx.handle)
     fft = g.matvec(X, scale=scale, prec="fp32")
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 3, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 3, 0, 0), g.ctx.handle)
     toep = g.matvec(X, scale=scale, prec="fp32")
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0, 0), g.ctx.handle)
     assert not np.array_equal(fft, toep)
     for b in range(B):
         ref = solver.lse_matvect_mult(X[b], scale[b] * fN, S.Ar, z_real, None, S.dx, S.idxS5)
@@ -286,11 +288,39 @@ def test_toeplitz_z_pass_double_float(vie, shape):
     scale = 1j * 2 * np.pi * np.array([1e6, 1e9, 2e10]) * solver.MU0
     lib = g.ctx._lib
     fft = g.matvec(X, scale=scale, prec="df")
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["df"], 0, 3, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["df"], 0, 3, 0, 0), g.ctx.handle)
     toep = g.matvec(X, scale=scale, prec="df")
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["df"], 0, 0, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["df"], 0, 0, 0, 0), g.ctx.handle)
     assert not np.array_equal(fft, toep)
     for b in range(B):
         ref = solver.lse_matvect_mult(X[b], scale[b] * fN, S.Ar, z_real, None, S.dx, S.idxS5)
         assert rel(toep[b], ref) < DF_TOL, b
         assert rel(fft[b], ref) < DF_TOL, b
+
+
+@pytest.mark.parametrize("shape", [(128, 40, 6), (256, 24, 4), (512, 12, 2)])
+def test_warp_x_passes_match_the_product(vie, shape):
+    """The warp-per-line x passes (x variant 1, complex64) on padded x lengths 256, 512 and 1024 against
+    the oracle's FP64 product, and not bitwise the shared-memory passes' product."""
+    from voxhenry_gb300 import _lib, geometry
+
+    w = geometry.random_blob(shape, fill=0.3, seed=23)
+    S = structure.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    fN, _ = circulant.generate_circulant_tensor(S.dx, 1.0, S.L, S.M, S.N)
+    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)
+    rng = np.random.default_rng(6)
+    B = 3
+    X = np.stack([rand_c(rng, g.n) for _ in range(B)])
+    scale = 1j * 2 * np.pi * np.array([1e6, 1e9, 2e10]) * solver.MU0
+    lib = g.ctx._lib
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0, 0), g.ctx.handle)
+    smem = g.matvec(X, scale=scale, prec="fp32")
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0, 1), g.ctx.handle)
+    warp = g.matvec(X, scale=scale, prec="fp32")
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0, 0), g.ctx.handle)
+    assert not np.array_equal(smem, warp)
+    for b in range(B):
+        ref = solver.lse_matvect_mult(X[b], scale[b] * fN, S.Ar, z_real, None, S.dx, S.idxS5)
+        assert rel(warp[b], ref) < FP32_TOL, b
+

@@ -42,8 +42,8 @@ SIGNATURES = {
     "vh_matvec": (C.c_int, [_p, C.c_int, _dp, _dp, _dp, _ip, C.c_int]),
     "vh_matvec_device": (C.c_int, [_p, C.c_int, _p, _p, _p, _ip, C.c_int]),
     "vh_matvec_device_noalloc": (C.c_int, [_p, C.c_int, _p, _p, _p, _ip, C.c_int]),
-    "vh_conv_tune": (C.c_int, [_p, C.c_int, C.c_int, _ip, _ip, _ip, _dp]),
-    "vh_conv_set_tuning": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "vh_conv_tune": (C.c_int, [_p, C.c_int, C.c_int, _ip, _ip, _ip, _ip, _dp]),
+    "vh_conv_set_tuning": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "vh_currents_on_grid": (C.c_int, [_p, C.c_int, C.c_int, C.c_int, C.c_int64, _i64p, C.c_int, _dp, C.c_int64, _dp]),
     "vh_sparse_matvec": (C.c_int, [_p, C.c_int64, C.c_int64, _i64p, _i64p, _dp, C.c_int, _dp, C.c_int64, _dp, C.c_int64]),
     "vh_precon_create": (C.c_int, [_p, C.c_int, _dp, C.c_int, C.POINTER(_p)]),

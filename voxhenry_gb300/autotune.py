@@ -2,9 +2,10 @@
 
 The FFT convolution of lse_matvect_mult.m:57-93 has launch choices whose best setting depends on the
 grid, the voxel box, the precision and the batch width: the y-pass (the register pass for padded y
-lengths 256, 512, 1024, or the shared-memory Stockham pass), the z-pass (two lanes per column, or one
-thread per column for padded z lengths up to 32) and how many right-hand sides share one launch
-sequence.  vh_conv_tune times the candidates on the geometry itself with CUDA events; the
+lengths 256, 512, 1024 over 128- or 64-byte rows, or the shared-memory Stockham pass), the z-pass (two
+lanes per column, one thread per column for padded z lengths up to 32, or the direct Toeplitz
+convolution for voxel boxes up to 16 rows), the x passes (complex64: one warp per line for padded x
+lengths 256, 512, 1024) and how many right-hand sides share one launch sequence.  vh_conv_tune times the candidates on the geometry itself with CUDA events; the
 choice is cached in a JSON file keyed by the GPU, the grid, the voxel box, the precision and the
 batch width, so later runs (and other geometries of the same shape) apply it without timing.
 
@@ -83,27 +84,28 @@ def box_of(prob) -> tuple:
 def tune(geom, prec: str, B: int, grid, box, path: str | None = None, retune: bool = False, timer=None) -> dict:
     """Applies the cached choice for this (grid, box, prec, B) to `geom`, or times the candidates
     (vh_conv_tune, or `timer(geom, prec, B)` in tests) and caches the winner.  Returns the choice
-    {"y_variant", "z_variant", "max_rhs", "ms_per_rhs", "cached"}."""
+    {"y_variant", "z_variant", "max_rhs", "x_variant", "ms_per_rhs", "cached"}."""
     key = tuning_key(grid, box, prec, B)
     if not retune:
         hit = load_cache(path).get(key)
         if hit is not None:
-            _set(geom, prec, hit["y_variant"], hit.get("z_variant", 0), hit["max_rhs"])
+            _set(geom, prec, hit["y_variant"], hit.get("z_variant", 0), hit["max_rhs"], hit.get("x_variant", 0))
             return dict(hit, cached=True)
     if timer is not None:
         choice = timer(geom, prec, B)
     else:
-        yv, zv, mr, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        yv, zv, mr, xv, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_double()
         _lib.check(geom.ctx._lib.vh_conv_tune(geom.handle, PREC[prec], int(B), C.byref(yv), C.byref(zv), C.byref(mr),
-                                              C.byref(ms)), geom.ctx.handle)
-        choice = {"y_variant": yv.value, "z_variant": zv.value, "max_rhs": mr.value, "ms_per_rhs": ms.value}
+                                              C.byref(xv), C.byref(ms)), geom.ctx.handle)
+        choice = {"y_variant": yv.value, "z_variant": zv.value, "max_rhs": mr.value, "x_variant": xv.value,
+                  "ms_per_rhs": ms.value}
     store(key, choice, path)
     return dict(choice, cached=False)
 
 
-def _set(geom, prec, y_variant, z_variant, max_rhs):
+def _set(geom, prec, y_variant, z_variant, max_rhs, x_variant=0):
     if hasattr(geom, "ctx"):
         _lib.check(geom.ctx._lib.vh_conv_set_tuning(geom.handle, PREC[prec], int(y_variant), int(z_variant),
-                                                    int(max_rhs)), geom.ctx.handle)
+                                                    int(max_rhs), int(x_variant)), geom.ctx.handle)
     else:   # a stand-in geometry (tests)
-        geom.tuning = (prec, y_variant, z_variant, max_rhs)
+        geom.tuning = (prec, y_variant, z_variant, max_rhs, x_variant)

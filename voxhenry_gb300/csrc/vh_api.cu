@@ -229,22 +229,22 @@ void vh_ctx_destroy(vh_ctx* ctx) { vh::ctx_release(ctx); }
 
 const char* vh_last_error(const vh_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
-vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_variant, int max_rhs) {
+vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_variant, int max_rhs, int x_variant) {
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
     VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && y_variant >= 0 && y_variant <= 3 && z_variant >= 0 &&
-                   z_variant <= 3 && max_rhs >= 0,
+                   z_variant <= 3 && max_rhs >= 0 && (x_variant == 0 || x_variant == 1),
                ERR_BAD_ARG, "bad tuning");
     VH_REQUIRE(g->has_conv, ERR_BAD_ARG, "geometry was created without a circulant tensor");
     const int Y = g->conv.Y;
     VH_REQUIRE((y_variant != 1 && y_variant != 3) || Y == 256 || Y == 512 || Y == 1024, ERR_UNSUPPORTED,
                "the register y-pass takes padded y lengths 256, 512 and 1024");
-    g->conv.tune[prec] = ConvTuning{y_variant, max_rhs, z_variant};
+    g->conv.tune[prec] = ConvTuning{y_variant, max_rhs, x_variant, z_variant};
   });
 }
 
 vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_variant, int* max_rhs,
-                       double* ms_per_rhs) {
+                       int* x_variant, double* ms_per_rhs) {
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
     VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && B >= 1, ERR_BAD_ARG, "bad tuning arguments");
@@ -268,9 +268,9 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_v
       if (yv != 2 && !reg_ok) continue;
       for (int zv : {1, 2, 3}) {
         if ((zv == 2 && !col_ok) || (zv == 3 && !toep_ok)) continue;
-        cands.push_back(ConvTuning{yv, 0, zv});
+        cands.push_back(ConvTuning{yv, 0, 0, zv});
         for (int w : {8, 4})
-          if (w < B) cands.push_back(ConvTuning{yv, w, zv});
+          if (w < B) cands.push_back(ConvTuning{yv, w, 0, zv});
       }
     }
     cudaEvent_t e0, e1;
@@ -279,8 +279,12 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_v
     ConvTuning best{};
     float best_ms = 0.0f;
     const ConvTuning saved = p.tune[pr];
+    // the warp-per-line x passes (complex64) are timed with the best y/z choice once it is known
+    const bool xw = pr == PREC_FP32 && xpass_warp_ok(p);
     try {
-      for (const ConvTuning& c : cands) {
+      for (size_t ci = 0; ci < cands.size() + (xw ? 1 : 0); ++ci) {
+        ConvTuning c = ci < cands.size() ? cands[ci] : best;
+        if (ci == cands.size()) c.x_variant = 1;
         p.tune[pr] = c;
         conv_apply(p, pr, B, x, g->n, y, g->n, g->ones, g->zslots[0], 0, st);   // warm-up, sizes the scratch
         float ms = 1e30f;
@@ -314,6 +318,7 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_v
     if (y_variant) *y_variant = best.y_variant;
     if (z_variant) *z_variant = best.z_variant;
     if (max_rhs) *max_rhs = best.max_rhs;
+    if (x_variant) *x_variant = best.x_variant;
     if (ms_per_rhs) *ms_per_rhs = best_ms / B;
   });
 }

@@ -25,6 +25,8 @@ bool fft_factor(int n, FftDesc& d);
 struct ConvTuning {
   int y_variant = 0;
   int max_rhs = 0;
+  // x passes (complex64): 0 the shared-memory passes; 1 one warp per line (X = 256, 512, 1024)
+  int x_variant = 0;
   int z_variant = 0;   // 0 automatic = 1 the two-lane register z-pass; 2 one thread per column (Z <= 32);
                        // 3 (complex64, double-float) the direct Toeplitz convolution along z
                        // (nz <= kZtoepMaxRows)
@@ -69,8 +71,9 @@ struct ConvPlan {
   void* scratchB = nullptr;
   size_t scratch_bytes_A = 0, scratch_bytes_B = 0;
   ConvTuning tune[3];          // per Prec
-  int y_variant_now = 0;       // the y- and z-passes of the launch sequence being issued (ConvTuning)
+  int y_variant_now = 0;       // the x-, y- and z-passes of the launch sequence being issued (ConvTuning)
   int z_variant_now = 0;
+  int x_variant_now = 0;
 
   int64_t points() const { return (int64_t)X * Y * Z; }
   int64_t lmn() const { return (int64_t)L * M * N; }
@@ -107,6 +110,12 @@ void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, i
 // geometry does not take it), and the pass itself on Bf (false when the table is not built).
 bool ztoep_build(ConvPlan& p, cudaStream_t st);
 bool zpass_toep(const ConvPlan& p, float2* Bf, int B, cudaStream_t st);
+// The x passes of x variant 1 (complex64): one warp per line for X = 256, 512, 1024
+// (vh_conv_xwarp.cu); false where X is another length.
+bool xpass_warp_ok(const ConvPlan& p);
+bool xpass_warp_fwd(const ConvPlan& p, int B, const double2* x, int64_t ldx, float2* A, cudaStream_t st);
+bool xpass_warp_inv(const ConvPlan& p, int B, const float2* A, const double2* x, int64_t ldx, double2* y, int64_t ldy,
+                    const double2* scale, const double2* zdiag, int64_t zstride, cudaStream_t st);
 // the same in double-float arithmetic on pair storage (PREC_DF)
 struct dcomplex;
 bool zpass_toep_df(const ConvPlan& p, dcomplex* Bf, int B, cudaStream_t st);

@@ -866,7 +866,11 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
   const int y0 = p.y0, ny = p.ny, z0 = p.z0, nz = p.nz;
   VH_REQUIRE(ny > 0 && nz > 0, ERR_BAD_ARG, "FFT convolution of a geometry without voxels");
   // pass 1
-  {
+  bool x_warp = false;
+  if constexpr (std::is_same<T, float>::value) {
+    if (p.x_variant_now == 1) x_warp = xpass_warp_fwd(p, B, x, ldx, A, st);
+  }
+  if (!x_warp) {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
     const int64_t lines = (int64_t)ny * nz * 5 * B;
     const size_t sm = (size_t)(X + 2 * xpad_len<C>(X * nl)) * sizeof(C) + nl * sizeof(XLine);
@@ -924,7 +928,9 @@ static void conv_apply_t(ConvPlan& p, int B, const double2* x, int64_t ldx, doub
     VH_CUDA_TRY(cudaGetLastError());
   }
   // pass 5
-  {
+  if (x_warp) {
+    if constexpr (std::is_same<T, float>::value) xpass_warp_inv(p, B, A, x, ldx, y, ldy, scale, zdiag, zstride, st);
+  } else {
     const int nl = x_lines_per_cta(X, TileCfg<T>::target);
     const int64_t lines = (int64_t)ny * nz * 5 * B;
     const size_t sm = (size_t)(X + 2 * xpad_len<C>(X * nl)) * sizeof(C) + nl * (sizeof(XLine) + sizeof(float2));
