@@ -129,9 +129,11 @@ vh_status vh_matvec_device(vh_geom* g, int B, const void* x_dev, void* y_dev, co
  * segments), z_variant (1 the two-lane register
  * z-pass; 2 one thread per column, for padded z lengths up to 32; 3, complex64 and double-float, the
  * direct Toeplitz convolution along z for voxel boxes up to 16 rows high), max_rhs (right-hand sides per
- * launch sequence; 0: the whole batch), x_variant (complex64: 0 the shared-memory x passes, 1 one warp
- * per line for padded x lengths 256, 512, 1024), and its milliseconds per RHS-matvec.  vh_conv_set_tuning
- * sets a choice without timing (a cached one); zeros restore the defaults.  The products of every
+ * launch sequence; 0: the whole batch), x_variant (complex64: 1 one warp per line for padded x lengths
+ * 256, 512, 1024, 2 the shared-memory x passes), and its milliseconds per RHS-matvec.
+ * vh_conv_set_tuning sets a choice without timing (a cached one); zeros restore the automatic
+ * choices (complex64: warp-per-line x passes where they apply, the Toeplitz z-pass for voxel boxes up
+ * to 16 rows, the register y-pass over 64-byte rows).  The products of every
  * choice agree within the precision's rounding.                                                     */
 vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_variant, int* max_rhs,
                        int* x_variant, double* ms_per_rhs);

@@ -224,7 +224,7 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     for yv in (1, 2, 3):
         for zv in (1, 2, 3):
             for mr in (0, 4):
-                for xv in ((0, 1) if prec == "fp32" else (0,)):
+                for xv in ((0, 1, 2) if prec == "fp32" else (0,)):
                     _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], yv, zv, mr, xv), g.ctx.handle)
                     got = g.matvec(X, scale=scale, prec=prec)
                     for b in range(B):
@@ -233,7 +233,7 @@ def test_every_tuning_choice_gives_the_product(vie, prec, tol):
     _lib.check(lib.vh_conv_tune(g.handle, _lib.PREC[prec], B, C.byref(yv), C.byref(zv), C.byref(mr), C.byref(xv),
                                 C.byref(ms)), g.ctx.handle)
     assert yv.value in (1, 2, 3) and zv.value in ((1, 2) if prec == "fp64" else (1, 2, 3)) and mr.value in (0, 4)
-    assert ms.value > 0 and xv.value in ((0, 1) if prec == "fp32" else (0,))
+    assert ms.value > 0 and xv.value in ((1, 2) if prec == "fp32" else (0,))
     got = g.matvec(X, scale=scale, prec=prec)
     assert max(rel(got[b], ref[b]) for b in range(B)) < tol
     _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC[prec], 0, 0, 0, 0), g.ctx.handle)
@@ -314,7 +314,7 @@ def test_warp_x_passes_match_the_product(vie, shape):
     X = np.stack([rand_c(rng, g.n) for _ in range(B)])
     scale = 1j * 2 * np.pi * np.array([1e6, 1e9, 2e10]) * solver.MU0
     lib = g.ctx._lib
-    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0, 0), g.ctx.handle)
+    _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0, 2), g.ctx.handle)
     smem = g.matvec(X, scale=scale, prec="fp32")
     _lib.check(lib.vh_conv_set_tuning(g.handle, _lib.PREC["fp32"], 0, 0, 0, 1), g.ctx.handle)
     warp = g.matvec(X, scale=scale, prec="fp32")

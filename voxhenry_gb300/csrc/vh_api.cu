@@ -233,7 +233,7 @@ vh_status vh_conv_set_tuning(vh_geom* g, vh_prec prec, int y_variant, int z_vari
   if (!g) return VH_ERR_BAD_ARG;
   return guarded(g->ctx, [&] {
     VH_REQUIRE(prec >= VH_PREC_FP64 && prec <= VH_PREC_DF && y_variant >= 0 && y_variant <= 3 && z_variant >= 0 &&
-                   z_variant <= 3 && max_rhs >= 0 && (x_variant == 0 || x_variant == 1),
+                   z_variant <= 3 && max_rhs >= 0 && x_variant >= 0 && x_variant <= 2,
                ERR_BAD_ARG, "bad tuning");
     VH_REQUIRE(g->has_conv, ERR_BAD_ARG, "geometry was created without a circulant tensor");
     const int Y = g->conv.Y;
@@ -264,13 +264,14 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_v
     const bool reg_ok = p.Y == 256 || p.Y == 512 || p.Y == 1024;
     const bool col_ok = p.Z <= 32;   // the one-thread-per-column z-pass takes Z = 8, 16, 32
     const bool toep_ok = pr != PREC_FP64 && ztoep_build(p, st);   // the direct z convolution (nz <= 16)
+    const bool xw = pr == PREC_FP32 && xpass_warp_ok(p);   // the candidates below use the shared-memory x passes
     for (int yv : {1, 2, 3}) {
       if (yv != 2 && !reg_ok) continue;
       for (int zv : {1, 2, 3}) {
         if ((zv == 2 && !col_ok) || (zv == 3 && !toep_ok)) continue;
-        cands.push_back(ConvTuning{yv, 0, 0, zv});
+        cands.push_back(ConvTuning{yv, 0, xw ? 2 : 0, zv});
         for (int w : {8, 4})
-          if (w < B) cands.push_back(ConvTuning{yv, w, 0, zv});
+          if (w < B) cands.push_back(ConvTuning{yv, w, xw ? 2 : 0, zv});
       }
     }
     cudaEvent_t e0, e1;
@@ -280,7 +281,6 @@ vh_status vh_conv_tune(vh_geom* g, vh_prec prec, int B, int* y_variant, int* z_v
     float best_ms = 0.0f;
     const ConvTuning saved = p.tune[pr];
     // the warp-per-line x passes (complex64) are timed with the best y/z choice once it is known
-    const bool xw = pr == PREC_FP32 && xpass_warp_ok(p);
     try {
       for (size_t ci = 0; ci < cands.size() + (xw ? 1 : 0); ++ci) {
         ConvTuning c = ci < cands.size() ? cands[ci] : best;

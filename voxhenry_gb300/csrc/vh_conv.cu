@@ -351,7 +351,10 @@ void conv_apply(ConvPlan& p, Prec prec, int B, const double2* x, int64_t ldx, do
   if (prec == PREC_DF && conv_df_supported(p)) ensure_df_tensor(p, st);
   p.y_variant_now = t.y_variant;
   p.z_variant_now = t.z_variant;
-  p.x_variant_now = prec == PREC_FP32 ? t.x_variant : 0;
+  // the automatic choices of complex64 (the faster variants on every measured grid): warp-per-line x
+  // passes where X fits, the Toeplitz z-pass where the box is short enough and the table builds
+  p.x_variant_now = prec != PREC_FP32 ? 0 : (t.x_variant == 0 ? (xpass_warp_ok(p) ? 1 : 0) : (t.x_variant == 1 ? 1 : 0));
+  if (prec == PREC_FP32 && t.z_variant == 0 && p.nz <= kZtoepMaxRows && ztoep_build(p, st)) p.z_variant_now = 3;
   if (t.z_variant == 3 && (prec == PREC_FP64 || !ztoep_build(p, st))) p.z_variant_now = 0;
   for (int b0 = 0; b0 < B; b0 += w) {
     const int nb = std::min(w, B - b0);
@@ -385,7 +388,7 @@ void conv_apply_scratch(const ConvPlan& p, Prec prec, int B, const double2* x, i
   ConvPlan q = p;   // shallow view of the plan with the caller's scratch; owns nothing
   q.y_variant_now = 0;   // the automatic pass choices
   q.z_variant_now = 0;
-  q.x_variant_now = 0;
+  q.x_variant_now = prec == PREC_FP32 && xpass_warp_ok(p) ? 1 : 0;   // allocates nothing
   q.scratchA = scratchA;
   q.scratchB = scratchB;
   q.scratch_bytes_A = a1 * B;

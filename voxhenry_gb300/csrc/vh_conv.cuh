@@ -25,11 +25,12 @@ bool fft_factor(int n, FftDesc& d);
 struct ConvTuning {
   int y_variant = 0;
   int max_rhs = 0;
-  // x passes (complex64): 0 the shared-memory passes; 1 one warp per line (X = 256, 512, 1024)
+  // x passes (complex64): 0 automatic = 1 where X is 256, 512 or 1024; 1 one warp per line; 2 the
+  // shared-memory passes
   int x_variant = 0;
-  int z_variant = 0;   // 0 automatic = 1 the two-lane register z-pass; 2 one thread per column (Z <= 32);
-                       // 3 (complex64, double-float) the direct Toeplitz convolution along z
-                       // (nz <= kZtoepMaxRows)
+  int z_variant = 0;   // 0 automatic = 3 for complex64 where nz <= kZtoepMaxRows, else 1; 1 the two-lane
+                       // register z-pass; 2 one thread per column (Z <= 32); 3 (complex64, double-float)
+                       // the direct Toeplitz convolution along z (nz <= kZtoepMaxRows)
 };
 
 constexpr int kZtoepMaxRows = 16;

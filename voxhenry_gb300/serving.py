@@ -163,9 +163,14 @@ def footprint_estimate(w: geometry.Workload, nfreq: int, restart: int = 50) -> i
 
 
 def tensor_bytes(w: geometry.Workload) -> int:
-    """Device bytes of a resident geometry's tensor spectra (complex128, complex64 and the pairs)."""
+    """Device bytes of a resident geometry's tensor spectra (complex128, complex64 and the pairs) and of
+    the Toeplitz table of the complex64 z-pass (two floats per component, row and (kx, ky) of the
+    voxel box's height, for boxes up to 16 rows)."""
     L, M, N = w.sigma_e.shape
-    return int(7 * 8 * L * M * N * (16 + 8 + 16))
+    nz_rows = np.flatnonzero(np.abs(np.asarray(w.sigma_e)).sum(axis=(0, 1)) > 0)
+    nz = int(nz_rows.max() - nz_rows.min() + 1) if nz_rows.size else 0
+    table = 2 * 7 * nz * (2 * L) * (2 * M) * 4 if nz <= 16 else 0
+    return int(7 * 8 * L * M * N * (16 + 8 + 16) + table)
 
 
 def geometry_key(w: geometry.Workload) -> str:
