@@ -610,6 +610,9 @@ constexpr int kFsolveCtasPerSm = 6;
 // the unstaged pair-precision backward solve: shared memory (vector + 32 x 33 block per warp) of the
 // leaf level's fronts allows five CTAs per SM, and the registers are held to that
 constexpr int kBsolveCtasPerSm = 5;
+// the warp-per-front backward solve reads its panels from global memory at every level (staging them
+// in shared memory, as the forward solve does, left the staged levels at one CTA per SM)
+constexpr bool kStageBackward = false;
 
 __device__ __forceinline__ void cp_async8(void* s, const void* g) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
@@ -1329,7 +1332,8 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       if (!ws && pipe_ok(h)) sm_p = std::max(sm_p, pipe_smem(h));
     } else {
       sm_f[stage(h)] = std::max(sm_f[stage(h)], warp_smem(h, true));
-      sm_b[stage(h)] = std::max(sm_b[stage(h)], warp_smem(h, false));
+      const bool sb = kStageBackward && stage(h);
+      sm_b[sb] = std::max(sm_b[sb], kSolveWarps * SolveSmem<T>::per_warp(s.level_max_nf[h], sb ? panel(h) : 0));
     }
   }
   VH_REQUIRE(sm_w[0] <= kWideStageMax, ERR_UNSUPPORTED, "front too large for the shared-memory solve");
@@ -1395,7 +1399,7 @@ void chol_solve(const CholSymbolic& s, int B, T* const* Wp, cplx<T>* x, int64_t 
       continue;
     }
     const int mp = panel(hh);
-    const bool stg = stage(hh);
+    const bool stg = kStageBackward && stage(hh);
     const size_t smh = kSolveWarps * SolveSmem<T>::per_warp(mnf, stg ? mp : 0);
     const unsigned grid = (unsigned)ceil_div((int64_t)nlev * B, kSolveWarps);
     if (stg)
