@@ -270,17 +270,26 @@ def test_toeplitz_z_pass_matches_the_fft_product(vie, shape, fill):
         assert rel(fft[b], ref) < FP32_TOL, b
 
 
-@pytest.mark.parametrize("shape", [(128, 128, 4), (128, 128, 8), (128, 128, 16)])
-def test_toeplitz_z_pass_double_float(vie, shape):
+@pytest.mark.parametrize("shape,height", [((128, 128, 4), 4), ((128, 128, 8), 8), ((128, 128, 16), 16),
+                                          ((128, 128, 16), 7), ((128, 128, 16), 10)])
+def test_toeplitz_z_pass_double_float(vie, shape, height):
     """The direct z convolution in double-float arithmetic (z_variant 3 of VH_PREC_DF) on grids the
-    double-float product takes (padded 256 x 256 x 8, 16, 32; box heights 4, 8 and 16): within the
-    double-float tolerance of the oracle's FP64 product, and not bitwise the FFT z-pass's."""
+    double-float product takes (padded 256 x 256 x 8, 16, 32) with voxel-box heights 4, 8, 16 and, on
+    the tallest grid with the upper layers empty, 7 (an odd height: one zero row of padding) and 10:
+    within the double-float tolerance of the oracle's FP64 product, and not bitwise the FFT z-pass's."""
     from voxhenry_gb300 import _lib, geometry
 
     w = geometry.random_blob(shape, fill=0.1, seed=17)
-    S = structure.build_system(w.sigma_e, None, w.dx, w.pnt_lft, w.pnt_rght)
+    sigma = np.array(w.sigma_e)
+    sigma[:, :, height:] = 0.0
+    m1 = np.zeros(shape, bool)
+    m1[0, :, :height] = True
+    m2 = np.zeros(shape, bool)
+    m2[-1, :, :height] = True
+    S = structure.build_system(np.asfortranarray(sigma), None, w.dx, [geometry.face_nodes(m1, "-x")],
+                               [geometry.face_nodes(m2, "+x")])
     fN, _ = circulant.generate_circulant_tensor(S.dx, 1.0, S.L, S.M, S.N)
-    z_real, _ = solver.z_arrays(w.sigma_e, None, 1.0)
+    z_real, _ = solver.z_arrays(np.asfortranarray(sigma), None, 1.0)
     g = vie.Geometry(fN, S.Ar, z_real, None, S.dx, S.idxS, want_fp32=True)
     rng = np.random.default_rng(8)
     B = 3

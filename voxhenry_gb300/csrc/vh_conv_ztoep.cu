@@ -69,10 +69,14 @@ constexpr int kZtCols = 32;
 // 16-byte chunks, so that the 8 lanes of a quarter-warp's 16-byte loads hit 8 different bank quads
 __host__ __device__ constexpr int zt_gstride(int nz) { return ((nz + 3) / 4) % 2 ? (nz + 3) / 4 * 4 : (nz + 3) / 4 * 4 + 4; }
 
-// One convolution term into acc: acc[m] += SIGN sum_n h[m - n] v(n), h = g (real) or i g (IMAG),
-// h[-d] = PAR h[d]; v(n) gives the input at row n (rows nz .. NZ - 1 are zero).
-template <int NZ, bool IMAG, int PAR, int SIGN, typename V>
-__device__ __forceinline__ void zt_conv(float2 (&acc)[NZ], const float* grow, V v_at) {
+// One convolution step into acc: acc[m] += sum_n h[m - n] v(n), h[d] = g[d] for d >= 0 and
+// h[-d] = (ODD ? -1 : 1) g[d]; v(n) = p1[n] or, PAIR, i (p1[n] + s2 p2[n]) (the two combined inputs
+// of the operator are both taken times an imaginary kernel); p1[n] is row n of a staged component
+// (rows nz .. NZ - 1 are zero).  A fully unrolled body: the kernel instantiates three of them and
+// every warp runs its steps through these three, so the hot code stays small.
+template <int NZ, bool ODD, bool PAIR>
+__device__ __forceinline__ void zt_conv(float2 (&acc)[NZ], const float* grow, const float2* p1, const float2* p2,
+                                        float s2) {
   float g[NZ];
 #pragma unroll
   for (int d = 0; d < NZ; d += 4) {
@@ -84,13 +88,18 @@ __device__ __forceinline__ void zt_conv(float2 (&acc)[NZ], const float* grow, V 
   }
 #pragma unroll
   for (int n = 0; n < NZ; ++n) {
-    const float2 v = v_at(n);
+    float2 v = p1[n * kZtCols];
+    if (PAIR) {
+      const float2 u = p2[n * kZtCols];
+      v.x = fmaf(s2, u.x, v.x);   // = v + s2 u with s2 = +-1, rounded once
+      v.y = fmaf(s2, u.y, v.y);
+    }
 #pragma unroll
     for (int m = 0; m < NZ; ++m) {
       const int d = m - n;
       const float w = g[d >= 0 ? d : -d];
-      const float ws = ((d >= 0 ? SIGN : SIGN * PAR) > 0) ? w : -w;
-      if (IMAG) {
+      const float ws = (d < 0 && ODD) ? -w : w;
+      if (PAIR) {
         acc[m].x = fmaf(-ws, v.y, acc[m].x);
         acc[m].y = fmaf(ws, v.x, acc[m].y);
       } else {
@@ -132,14 +141,26 @@ __device__ __forceinline__ void zt_bar_sync() { asm volatile("bar.sync 1, 160;\n
 
 // Five warps over 32 columns of one ky row (lane = column), all right-hand sides of the batch; the
 // 13 distinct convolutions of the operator (tensor_apply_ri in the spectral form) split 3/3/3/2/2:
-//   warp 0: o0 = G0 jx + G1 (j2 + j3)  and  A = G1 jx
-//   warp 1: o1 = G0 jy + G2 (j2 - j3)  and  B = G2 jy
-//   warp 2: o2 = G0 jz + G4 j3         and  P = G4 jz
+//   warp 0: A = G1 jx,  then o0 = G0 jx + G1 (j2 + j3)
+//   warp 1: B = G2 jy,  then o1 = G0 jy + G2 (j2 - j3)
+//   warp 2: P = G4 jz,  then o2 = G0 jz + G4 j3
 //   warp 3: o3 = G3 j2 + G5 j3 - A - B
 //   warp 4: o4 = G5 j2 + G6 j3 - A + B - P
-// A, B and P pass through shared memory (named barrier 1: warps 0-2 arrive, 3-4 wait).  Each RHS's
-// inputs are staged in shared memory (double-buffered: the next RHS's copies are in flight while this
-// one is computed; rows nz .. NZ - 1 stay zero), so the in-place stores never meet another warp's loads.
+// A, B and P are computed first and pass through shared memory (named barrier 1: warps 0-2 arrive,
+// 3-4 wait), so that warps 3-4 rarely wait for them.  G1 and G2 are imaginary: their combined inputs
+// run through the PAIR body; A and B run through the real body and are rotated by i when stored.
+// Each RHS's inputs are staged in shared memory (double-buffered: the next RHS's copies are in flight
+// while this one is computed; rows nz .. NZ - 1 stay zero), so the in-place stores never meet another
+// warp's loads.
+//
+// A step is coded as kind (bits 0-1: 0 even kernel, 1 combined inputs, 2 odd kernel), kernel k (bits
+// 2-4), first input (5-7), second input (8-10), second input subtracted (bit 11).
+__constant__ unsigned short kZtProgram[5][3] = {
+    {0 | 1 << 2 | 0 << 5, 0 | 0 << 2 | 0 << 5, 1 | 1 << 2 | 3 << 5 | 4 << 8},
+    {0 | 2 << 2 | 1 << 5, 0 | 0 << 2 | 1 << 5, 1 | 2 << 2 | 3 << 5 | 4 << 8 | 1 << 11},
+    {2 | 4 << 2 | 2 << 5, 0 | 0 << 2 | 2 << 5, 2 | 4 << 2 | 4 << 5},
+    {0, 0 | 3 << 2 | 3 << 5, 0 | 5 << 2 | 4 << 5},
+    {0, 0 | 5 << 2 | 3 << 5, 0 | 6 << 2 | 4 << 5}};
 
 template <int NZ>
 struct ZtSmem {
@@ -173,127 +194,94 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(float2* __restrict__ Bf, 
   }
   const float* gl = &sm.g[0][lane][0];
   constexpr int gk = kZtCols * ZtSmem<NZ>::GST;   // g[k + 1] - g[k]
+  constexpr int ck = NZ * kZtCols;                // in[c + 1] - in[c]
   for (int b = 0; b < nrhs; ++b) {
     zt_wait<0>();
     // RHS b staged by every thread; every warp is done with RHS b - 1 (its buffer and the partial sums)
     __syncthreads();
     if (b + 1 < nrhs) zt_stage<NZ>(sm.in[(b + 1) & 1], src0 + (int64_t)(b + 1) * 5 * comp, nz, plane, comp, kx0, X);
-    const float2(*s)[NZ][kZtCols] = sm.in[b & 1];
-    auto in = [&](int c, int n) { return s[c][n][lane]; };
+    const float2* s = &sm.in[b & 1][0][0][lane];
     float2 acc[NZ];
 #pragma unroll
     for (int m = 0; m < NZ; ++m) acc[m] = make_float2(0.0f, 0.0f);
-    float2* out = Bf + (int64_t)b * 5 * comp + (int64_t)warp * comp + (int64_t)ky * X + kx;
-    auto store = [&]() {   // the warp's output; acc starts over for a partial sum
-      if (ok) {
-#pragma unroll
-        for (int m = 0; m < NZ; ++m)
-          if (m < nz) out[m * plane] = acc[m];
+#pragma unroll 1
+    for (int st = warp < 3 ? 0 : 1; st < 3; ++st) {
+      const unsigned code = kZtProgram[warp][st];
+      const float* gr = gl + ((code >> 2) & 7) * gk;
+      const float2* p1 = s + ((code >> 5) & 7) * ck;
+      switch (code & 3) {
+        case 0: zt_conv<NZ, false, false>(acc, gr, p1, p1, 0.0f); break;
+        case 1: zt_conv<NZ, false, true>(acc, gr, p1, s + ((code >> 8) & 7) * ck, (code >> 11) & 1 ? -1.0f : 1.0f); break;
+        default: zt_conv<NZ, true, false>(acc, gr, p1, p1, 0.0f); break;
       }
-#pragma unroll
-      for (int m = 0; m < NZ; ++m) acc[m] = make_float2(0.0f, 0.0f);
-    };
-    auto put = [&](int j) {
-#pragma unroll
-      for (int m = 0; m < NZ; ++m) sm.part[j][m][lane] = acc[m];
-    };
-    switch (warp) {
-      case 0:
-        zt_conv<NZ, false, 1, 1>(acc, gl, [&](int n) { return in(0, n); });
-        zt_conv<NZ, true, 1, 1>(acc, gl + gk, [&](int n) {
-          const float2 a = in(3, n), c = in(4, n);
-          return make_float2(a.x + c.x, a.y + c.y);
-        });
-        store();
-        zt_conv<NZ, true, 1, 1>(acc, gl + gk, [&](int n) { return in(0, n); });
-        put(0);
-        zt_bar_arrive();
-        break;
-      case 1:
-        zt_conv<NZ, false, 1, 1>(acc, gl, [&](int n) { return in(1, n); });
-        zt_conv<NZ, true, 1, 1>(acc, gl + 2 * gk, [&](int n) {
-          const float2 a = in(3, n), c = in(4, n);
-          return make_float2(a.x - c.x, a.y - c.y);
-        });
-        store();
-        zt_conv<NZ, true, 1, 1>(acc, gl + 2 * gk, [&](int n) { return in(1, n); });
-        put(1);
-        zt_bar_arrive();
-        break;
-      case 2:
-        zt_conv<NZ, false, 1, 1>(acc, gl, [&](int n) { return in(2, n); });
-        zt_conv<NZ, false, -1, 1>(acc, gl + 4 * gk, [&](int n) { return in(4, n); });
-        store();
-        zt_conv<NZ, false, -1, 1>(acc, gl + 4 * gk, [&](int n) { return in(2, n); });
-        put(2);
-        zt_bar_arrive();
-        break;
-      case 3:
-        zt_conv<NZ, false, 1, 1>(acc, gl + 3 * gk, [&](int n) { return in(3, n); });
-        zt_conv<NZ, false, 1, 1>(acc, gl + 5 * gk, [&](int n) { return in(4, n); });
-        zt_bar_sync();
+      if (st == 0) {   // A, B (times i: G1 and G2 are imaginary) or P for warps 3-4; acc starts over
+        const bool rot = warp < 2;
 #pragma unroll
         for (int m = 0; m < NZ; ++m) {
-          const float2 a = sm.part[0][m][lane], bb = sm.part[1][m][lane];
-          acc[m].x -= a.x + bb.x;
-          acc[m].y -= a.y + bb.y;
+          sm.part[warp][m][lane] = rot ? make_float2(-acc[m].y, acc[m].x) : acc[m];
+          acc[m] = make_float2(0.0f, 0.0f);
         }
-        store();
-        break;
-      default:
-        zt_conv<NZ, false, 1, 1>(acc, gl + 5 * gk, [&](int n) { return in(3, n); });
-        zt_conv<NZ, false, 1, 1>(acc, gl + 6 * gk, [&](int n) { return in(4, n); });
-        zt_bar_sync();
+        zt_bar_arrive();
+      }
+    }
+    if (warp == 3) {
+      zt_bar_sync();
 #pragma unroll
-        for (int m = 0; m < NZ; ++m) {
-          const float2 a = sm.part[0][m][lane], bb = sm.part[1][m][lane], pp = sm.part[2][m][lane];
-          acc[m].x += (bb.x - a.x) - pp.x;
-          acc[m].y += (bb.y - a.y) - pp.y;
-        }
-        store();
-        break;
+      for (int m = 0; m < NZ; ++m) {
+        const float2 a = sm.part[0][m][lane], bb = sm.part[1][m][lane];
+        acc[m].x -= a.x + bb.x;
+        acc[m].y -= a.y + bb.y;
+      }
+    } else if (warp == 4) {
+      zt_bar_sync();
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) {
+        const float2 a = sm.part[0][m][lane], bb = sm.part[1][m][lane], pp = sm.part[2][m][lane];
+        acc[m].x += (bb.x - a.x) - pp.x;
+        acc[m].y += (bb.y - a.y) - pp.y;
+      }
+    }
+    if (ok) {   // the warp's output component
+      float2* out = Bf + (int64_t)b * 5 * comp + (int64_t)warp * comp + (int64_t)ky * X + kx;
+#pragma unroll
+      for (int m = 0; m < NZ; ++m)
+        if (m < nz) out[m * plane] = acc[m];
     }
   }
 }
 
 // ---- the same pass in double-float arithmetic (VH_PREC_DF: pair storage of Bf, pair h values, each
 // output a Dot2 accumulation over all its terms, ~48 significant bits); single-buffered staging.
+// A pair multiply-add is about twelve instructions, so a fully unrolled convolution would be several
+// kilobytes of code per step: the body loops over the input rows at run time, reads the row's NZ
+// kernel values from a two-sided table in shared memory (h2[k][j] = h_k[j - (NZ - 1)], the parity
+// already applied) and serves every step of every warp.
 template <int NZ>
 struct ZtSmemDf {
-  static constexpr int GST = zt_gstride(NZ);
-  float ghi[7][kZtCols][GST];
-  float glo[7][kZtCols][GST];
+  dfloat h2[7][2 * NZ - 1][kZtCols];
   dcomplex in[5][NZ][kZtCols];
   dcomplex part[3][NZ][kZtCols];
 };
 
-template <int NZ, bool IMAG, int PAR, int SIGN, typename V>
-__device__ __forceinline__ void zt_conv_df(df_dot (&re)[NZ], df_dot (&im)[NZ], const float* ghi, const float* glo,
-                                           V v_at) {
-  dfloat g[NZ];
-#pragma unroll
-  for (int d = 0; d < NZ; d += 4) {
-    const float4 h = *reinterpret_cast<const float4*>(ghi + d);
-    const float4 l = *reinterpret_cast<const float4*>(glo + d);
-    g[d] = dfloat(h.x, l.x);
-    if (d + 1 < NZ) g[d + 1] = dfloat(h.y, l.y);
-    if (d + 2 < NZ) g[d + 2] = dfloat(h.z, l.z);
-    if (d + 3 < NZ) g[d + 3] = dfloat(h.w, l.w);
-  }
-#pragma unroll
-  for (int n = 0; n < NZ; ++n) {
-    const dcomplex v = v_at(n);
+// (re, im)[m] += sum_n h[m - n] v(n) for n < nz; v(n) = p1[n] (+ or - p2[n] with PAIR), times i with
+// IMAG; H = &h2[k][0][lane]
+template <int NZ>
+__device__ __forceinline__ void zt_conv_df(df_dot (&re)[NZ], df_dot (&im)[NZ], const dfloat* H, const dcomplex* p1,
+                                           const dcomplex* p2, int nz, bool pair, bool neg2, bool imag) {
+#pragma unroll 1
+  for (int n = 0; n < nz; ++n) {
+    dcomplex v = p1[n * kZtCols];
+    if (pair) {
+      const dcomplex u = p2[n * kZtCols];
+      v = neg2 ? dcomplex{v.x - u.x, v.y - u.y} : dcomplex{v.x + u.x, v.y + u.y};
+    }
+    const dfloat vx = imag ? -v.y : v.x, vy = imag ? v.x : v.y;
+    const dfloat* w = H + (NZ - 1 - n) * kZtCols;   // w[m * kZtCols] = h[m - n]
 #pragma unroll
     for (int m = 0; m < NZ; ++m) {
-      const int d = m - n;
-      const dfloat w = ((d >= 0 ? SIGN : SIGN * PAR) > 0) ? g[d >= 0 ? d : -d] : -g[d >= 0 ? d : -d];
-      if (IMAG) {
-        re[m].add(-w, v.y);
-        im[m].add(w, v.x);
-      } else {
-        re[m].add(w, v.x);
-        im[m].add(w, v.y);
-      }
+      const dfloat wm = w[m * kZtCols];
+      re[m].add(wm, vx);
+      im[m].add(wm, vy);
     }
   }
 }
@@ -315,13 +303,18 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(dcomplex* __restrict__
     const int col = i % kZtCols, n = (i / kZtCols) % NZ, c = i / (kZtCols * NZ);
     if (n >= nz) sm.in[c][n][col] = dcomplex{dfloat(0.0f), dfloat(0.0f)};
   }
-  for (int i = threadIdx.x; i < 7 * NZ * kZtCols; i += blockDim.x) {
-    const int col = i % kZtCols, d = (i / kZtCols) % NZ, k = i / (kZtCols * NZ);
-    const bool in_range = kx0 + col < X && d < nz;
-    const int64_t gi = (((int64_t)ky * 7 + k) * nz + d) * X + kx0 + col;
-    sm.ghi[k][col][d] = in_range ? gz[gi] : 0.0f;
-    sm.glo[k][col][d] = in_range ? gzlo[gi] : 0.0f;
+  for (int i = threadIdx.x; i < 7 * (2 * NZ - 1) * kZtCols; i += blockDim.x) {
+    const int col = i % kZtCols, j = (i / kZtCols) % (2 * NZ - 1), k = i / (kZtCols * (2 * NZ - 1));
+    const int d = j - (NZ - 1), ad = d < 0 ? -d : d;
+    dfloat h(0.0f);
+    if (kx0 + col < X && ad < nz) {
+      const int64_t gi = (((int64_t)ky * 7 + k) * nz + ad) * X + kx0 + col;
+      h = dfloat(gz[gi], gzlo[gi]);
+      if (d < 0 && zt_parity(k) < 0) h = -h;
+    }
+    sm.h2[k][j][col] = h;
   }
+  constexpr int ck = NZ * kZtCols;   // in[c + 1] - in[c]
   for (int b = 0; b < nrhs; ++b) {
     __syncthreads();   // every warp is done with RHS b - 1 (the staged inputs and the partial sums)
     {
@@ -335,88 +328,53 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(dcomplex* __restrict__
       zt_wait<0>();
     }
     __syncthreads();
-    auto in = [&](int c, int n) { return sm.in[c][n][lane]; };   // rows nz .. NZ - 1 are zero
+    const dcomplex* s = &sm.in[0][0][lane];
     df_dot re[NZ], im[NZ];
 #pragma unroll
     for (int m = 0; m < NZ; ++m) re[m] = im[m] = df_dot(dfloat(0.0f));
-    dcomplex* out = Bf + (int64_t)b * 5 * comp + (int64_t)warp * comp + (int64_t)ky * X + kx;
-    auto store = [&]() {   // the warp's output; the accumulators start over for a partial sum
-      if (ok) {
+#pragma unroll 1
+    for (int st = warp < 3 ? 0 : 1; st < 3; ++st) {   // the warp's steps, as in k_zpass_toep
+      const unsigned code = kZtProgram[warp][st];
+      const int k = (code >> 2) & 7;
+      zt_conv_df<NZ>(re, im, &sm.h2[k][0][lane], s + ((code >> 5) & 7) * ck, s + ((code >> 8) & 7) * ck, nz,
+                     (code & 3) == 1, (code >> 11) & 1, zt_imag(k));
+      if (st == 0) {   // A, B or P for warps 3-4; the accumulators start over
 #pragma unroll
-        for (int m = 0; m < NZ; ++m)
-          if (m < nz) out[m * plane] = dcomplex{re[m].value(), im[m].value()};
+        for (int m = 0; m < NZ; ++m) {
+          sm.part[warp][m][lane] = dcomplex{re[m].value(), im[m].value()};
+          re[m] = im[m] = df_dot(dfloat(0.0f));
+        }
+        zt_bar_arrive();
       }
-#pragma unroll
-      for (int m = 0; m < NZ; ++m) re[m] = im[m] = df_dot(dfloat(0.0f));
-    };
-    auto put = [&](int j) {
+    }
+    if (warp == 3) {
+      zt_bar_sync();
 #pragma unroll
       for (int m = 0; m < NZ; ++m) {
-        sm.part[j][m][lane] = dcomplex{re[m].value(), im[m].value()};
-        re[m] = im[m] = df_dot(dfloat(0.0f));
+        const dcomplex a = sm.part[0][m][lane], bb = sm.part[1][m][lane];
+        re[m].merge(-a.x.hi, -a.x.lo);
+        re[m].merge(-bb.x.hi, -bb.x.lo);
+        im[m].merge(-a.y.hi, -a.y.lo);
+        im[m].merge(-bb.y.hi, -bb.y.lo);
       }
-    };
-    auto sum2 = [&](int c1, int c2, bool minus) {
-      return [&, c1, c2, minus](int n) {
-        const dcomplex a = in(c1, n), c = in(c2, n);
-        return minus ? dcomplex{a.x - c.x, a.y - c.y} : dcomplex{a.x + c.x, a.y + c.y};
-      };
-    };
-    switch (warp) {
-      case 0:
-        zt_conv_df<NZ, false, 1, 1>(re, im, sm.ghi[0][lane], sm.glo[0][lane], [&](int n) { return in(0, n); });
-        zt_conv_df<NZ, true, 1, 1>(re, im, sm.ghi[1][lane], sm.glo[1][lane], sum2(3, 4, false));
-        store();
-        zt_conv_df<NZ, true, 1, 1>(re, im, sm.ghi[1][lane], sm.glo[1][lane], [&](int n) { return in(0, n); });
-        put(0);
-        zt_bar_arrive();
-        break;
-      case 1:
-        zt_conv_df<NZ, false, 1, 1>(re, im, sm.ghi[0][lane], sm.glo[0][lane], [&](int n) { return in(1, n); });
-        zt_conv_df<NZ, true, 1, 1>(re, im, sm.ghi[2][lane], sm.glo[2][lane], sum2(3, 4, true));
-        store();
-        zt_conv_df<NZ, true, 1, 1>(re, im, sm.ghi[2][lane], sm.glo[2][lane], [&](int n) { return in(1, n); });
-        put(1);
-        zt_bar_arrive();
-        break;
-      case 2:
-        zt_conv_df<NZ, false, 1, 1>(re, im, sm.ghi[0][lane], sm.glo[0][lane], [&](int n) { return in(2, n); });
-        zt_conv_df<NZ, false, -1, 1>(re, im, sm.ghi[4][lane], sm.glo[4][lane], [&](int n) { return in(4, n); });
-        store();
-        zt_conv_df<NZ, false, -1, 1>(re, im, sm.ghi[4][lane], sm.glo[4][lane], [&](int n) { return in(2, n); });
-        put(2);
-        zt_bar_arrive();
-        break;
-      case 3:
-        zt_conv_df<NZ, false, 1, 1>(re, im, sm.ghi[3][lane], sm.glo[3][lane], [&](int n) { return in(3, n); });
-        zt_conv_df<NZ, false, 1, 1>(re, im, sm.ghi[5][lane], sm.glo[5][lane], [&](int n) { return in(4, n); });
-        zt_bar_sync();
+    } else if (warp == 4) {
+      zt_bar_sync();
 #pragma unroll
-        for (int m = 0; m < NZ; ++m) {
-          const dcomplex a = sm.part[0][m][lane], bb = sm.part[1][m][lane];
-          re[m].merge(-a.x.hi, -a.x.lo);
-          re[m].merge(-bb.x.hi, -bb.x.lo);
-          im[m].merge(-a.y.hi, -a.y.lo);
-          im[m].merge(-bb.y.hi, -bb.y.lo);
-        }
-        store();
-        break;
-      default:
-        zt_conv_df<NZ, false, 1, 1>(re, im, sm.ghi[5][lane], sm.glo[5][lane], [&](int n) { return in(3, n); });
-        zt_conv_df<NZ, false, 1, 1>(re, im, sm.ghi[6][lane], sm.glo[6][lane], [&](int n) { return in(4, n); });
-        zt_bar_sync();
+      for (int m = 0; m < NZ; ++m) {
+        const dcomplex a = sm.part[0][m][lane], bb = sm.part[1][m][lane], pp = sm.part[2][m][lane];
+        re[m].merge(-a.x.hi, -a.x.lo);
+        re[m].merge(bb.x.hi, bb.x.lo);
+        re[m].merge(-pp.x.hi, -pp.x.lo);
+        im[m].merge(-a.y.hi, -a.y.lo);
+        im[m].merge(bb.y.hi, bb.y.lo);
+        im[m].merge(-pp.y.hi, -pp.y.lo);
+      }
+    }
+    if (ok) {   // the warp's output component
+      dcomplex* out = Bf + (int64_t)b * 5 * comp + (int64_t)warp * comp + (int64_t)ky * X + kx;
 #pragma unroll
-        for (int m = 0; m < NZ; ++m) {
-          const dcomplex a = sm.part[0][m][lane], bb = sm.part[1][m][lane], pp = sm.part[2][m][lane];
-          re[m].merge(-a.x.hi, -a.x.lo);
-          re[m].merge(bb.x.hi, bb.x.lo);
-          re[m].merge(-pp.x.hi, -pp.x.lo);
-          im[m].merge(-a.y.hi, -a.y.lo);
-          im[m].merge(bb.y.hi, bb.y.lo);
-          im[m].merge(-pp.y.hi, -pp.y.lo);
-        }
-        store();
-        break;
+      for (int m = 0; m < NZ; ++m)
+        if (m < nz) out[m * plane] = dcomplex{re[m].value(), im[m].value()};
     }
   }
 }
