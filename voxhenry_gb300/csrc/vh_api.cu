@@ -525,6 +525,7 @@ vh_status vh_matvec(vh_geom* g, int B, const double* x, double* y, const double*
     matvec_device(g, B, g->io_x, g->io_y, sd, zslot, (Prec)prec);
     VH_CUDA_TRY(cudaMemcpyAsync(y, g->io_y, bytes, cudaMemcpyDeviceToHost, st));
     VH_CUDA_TRY(cudaStreamSynchronize(st));
+    VH_REQUIRE(!ztoep_take_stall(st), ERR_TIMEOUT, "a z-pass gave up waiting for its staging copies");
   });
 }
 

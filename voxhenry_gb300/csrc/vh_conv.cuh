@@ -120,6 +120,10 @@ bool xpass_warp_inv(const ConvPlan& p, int B, const float2* A, const double2* x,
 // the same in double-float arithmetic on pair storage (PREC_DF)
 struct dcomplex;
 bool zpass_toep_df(const ConvPlan& p, dcomplex* Bf, int B, cudaStream_t st);
+// The Toeplitz passes stage their inputs with the copy engine and wait for the copies a bounded number
+// of polls; a pass that gave up wrote NaN and raised a device flag.  Reads and clears that flag (one
+// per device process, shared by all contexts), after the work on `st` is done.
+bool ztoep_take_stall(cudaStream_t st);
 
 // In-place forward 3-D FFT of `batch` column-major X x Y x Z complex arrays (device).
 void fft3d_forward_inplace(double2* data, int X, int Y, int Z, int batch, cudaStream_t st);

@@ -12,6 +12,10 @@
 // (1, 2), even in d except for component 4 (odd): one float per (k, d >= 0).  The table is built on
 // the device from the complex128 spectrum in FP64 and checked for that form (like the spectrum's own
 // real/imaginary check); where it fails the variant is not offered.
+#include <cuda.h>   // CUtensorMap (the encoder is looked up through the runtime)
+#include <cudaTypedefs.h>
+
+#include <cstddef>
 #include <cstring>
 
 #include "vh_conv.cuh"
@@ -110,30 +114,63 @@ __device__ __forceinline__ void zt_conv(float2 (&acc)[NZ], const float* grow, co
   }
 }
 
-__device__ __forceinline__ void zt_cp16(void* dst, const void* src) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
-}
-__device__ __forceinline__ void zt_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void zt_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+// ---- staging by the tensor memory accelerator.  The right-hand sides' five components are one 3-D
+// tensor of 64-bit elements: x = kx (W elements per value: 1 for complex64, 2 for the double-float
+// pairs), y = ky, z = the row (b * 5 + c) * nz + n.  One copy moves a box of 32 columns x 1 x nz rows
+// (one component of one RHS) into in[c][0 .. nz); columns past the grid's last read as zeros.  Its
+// x coordinate is a multiple of 32 W elements (256 W bytes), the 16-byte rule of tiled copies.
+constexpr unsigned kZtWaitLimit = 1u << 20;   // polls of an mbarrier before the pass gives up
 
-// Stages RHS b's five components (nz rows x 32 columns) into in[c][n][32] with 16-byte cp.async
-// copies (two columns each), thread t taking rows t/16, t/16 + 10, ... at column pair t % 16;
-// copies past the grid's last column are skipped.
-template <int NZ>
-__device__ __forceinline__ void zt_stage(float2 (*dst)[NZ][kZtCols], const float2* src, int nz, int64_t plane,
-                                         int64_t comp, int kx0, int X) {
-  const int q = threadIdx.x % (kZtCols / 2);
-  const bool ok = kx0 + 2 * q < X;
-  int c = 0, n = threadIdx.x / (kZtCols / 2);   // row c * nz + n, advanced by 10 rows per copy
-  while (n >= nz) { n -= nz; ++c; }
-  for (; c < 5;) {
-    if (ok) zt_cp16(&dst[c][n][2 * q], src + c * comp + n * plane + 2 * q);
-    n += (5 * kZtCols) / (kZtCols / 2);
-    while (n >= nz && c < 5) { n -= nz; ++c; }
+__device__ __forceinline__ unsigned zt_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void zt_mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(zt_smem(bar)) : "memory");
+}
+// the initialised barriers visible to the copy engine and to every thread (after a __syncthreads)
+__device__ __forceinline__ void zt_mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+// the threads' earlier shared-memory accesses ordered before the copies issued next
+__device__ __forceinline__ void zt_fence_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+__device__ __forceinline__ void zt_mbar_expect(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(zt_smem(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void zt_tma_load(const CUtensorMap* map, void* dst, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];\n" ::"r"(zt_smem(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(zt_smem(bar))
+      : "memory");
+}
+
+// waits for the phase of `parity` to complete; false after kZtWaitLimit polls
+__device__ __forceinline__ bool zt_mbar_wait(uint64_t* bar, unsigned parity) {
+  for (unsigned i = 0; i < kZtWaitLimit; ++i) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(zt_smem(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
   }
-  zt_commit();
+  return false;
+}
+
+// set when a pass gave up waiting for its copies (its outputs are then NaN)
+__device__ int g_zt_stalled;
+
+// thread 0: the five components of RHS b into in[0..4] (component stride `cstride` bytes), completing
+// on `bar`
+__device__ __forceinline__ void zt_issue(const CUtensorMap* map, unsigned char* in0, size_t cstride, uint64_t* bar,
+                                         int x, int ky, int b, int nz, unsigned bytes) {
+  zt_fence_async();
+  zt_mbar_expect(bar, bytes);
+#pragma unroll 1
+  for (int c = 0; c < 5; ++c) zt_tma_load(map, in0 + c * cstride, bar, x, ky, (b * 5 + c) * nz);
 }
 
 __device__ __forceinline__ void zt_bar_arrive() { asm volatile("bar.arrive 1, 160;\n" ::: "memory"); }
@@ -166,14 +203,16 @@ template <int NZ>
 struct ZtSmem {
   static constexpr int GST = zt_gstride(NZ);
   float g[7][kZtCols][GST];               // h_k of each column, rows d >= nz zero
-  float2 in[2][5][NZ][kZtCols];           // staged RHS (double-buffered)
+  float2 in[2][5][NZ][kZtCols];           // staged RHS (double-buffered), 128-byte aligned
   float2 part[3][NZ][kZtCols];            // A, B, P for the last two warps
+  uint64_t bar[2];                        // completion of each buffer's copies
 };
 
 template <int NZ>
-__global__ void __launch_bounds__(5 * 32) k_zpass_toep(float2* __restrict__ Bf, const float* __restrict__ gz, int nz,
-                                                      int Y, int X, int nrhs) {
-  extern __shared__ __align__(16) unsigned char zt_raw[];
+__global__ void __launch_bounds__(5 * 32) k_zpass_toep(const __grid_constant__ CUtensorMap map, float2* __restrict__ Bf,
+                                                      const float* __restrict__ gz, int nz, int Y, int X, int nrhs) {
+  static_assert(offsetof(ZtSmem<NZ>, in) % 128 == 0, "copy destinations 128-byte aligned");
+  extern __shared__ __align__(128) unsigned char zt_raw[];
   ZtSmem<NZ>& sm = *reinterpret_cast<ZtSmem<NZ>*>(zt_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ky = blockIdx.y;
@@ -182,12 +221,22 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(float2* __restrict__ Bf, 
   const bool ok = kx < X;
   const int64_t plane = (int64_t)Y * X;       // one z row of one component
   const int64_t comp = (int64_t)nz * plane;   // one component of one RHS
-  const float2* src0 = Bf + (int64_t)ky * X + kx0;
+  constexpr size_t cbytes = sizeof(sm.in[0][0]);                       // one staged component
+  const unsigned bytes = 5u * (unsigned)nz * kZtCols * sizeof(float2);   // one RHS's copies
   for (int i = threadIdx.x; i < 2 * 5 * NZ * kZtCols; i += blockDim.x) {   // padding rows nz.. stay zero
     const int cc = i % kZtCols, n = (i / kZtCols) % NZ, cb = i / (kZtCols * NZ);
     if (n >= nz) sm.in[cb / 5][cb % 5][n][cc] = make_float2(0.0f, 0.0f);
   }
-  if (nrhs > 0) zt_stage<NZ>(sm.in[0], src0, nz, plane, comp, kx0, X);
+  if (threadIdx.x == 0) {
+    zt_mbar_init(&sm.bar[0]);
+    zt_mbar_init(&sm.bar[1]);
+    zt_mbar_fence_init();
+  }
+  __syncthreads();
+  // the copies want 128-byte aligned destinations (checked, not assumed: a pass that cannot copy says so)
+  const bool aligned = (zt_smem(sm.in) & 127u) == 0;
+  if (threadIdx.x == 0 && nrhs > 0 && aligned)
+    zt_issue(&map, reinterpret_cast<unsigned char*>(sm.in[0]), cbytes, &sm.bar[0], kx0, ky, 0, nz, bytes);
   for (int i = threadIdx.x; i < 7 * NZ * kZtCols; i += blockDim.x) {
     const int cc = i % kZtCols, d = (i / kZtCols) % NZ, k = i / (kZtCols * NZ);
     sm.g[k][cc][d] = (kx0 + cc < X && d < nz) ? gz[(((int64_t)ky * 7 + k) * nz + d) * X + kx0 + cc] : 0.0f;
@@ -195,11 +244,14 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(float2* __restrict__ Bf, 
   const float* gl = &sm.g[0][lane][0];
   constexpr int gk = kZtCols * ZtSmem<NZ>::GST;   // g[k + 1] - g[k]
   constexpr int ck = NZ * kZtCols;                // in[c + 1] - in[c]
+  bool stalled = !aligned;
   for (int b = 0; b < nrhs; ++b) {
-    zt_wait<0>();
-    // RHS b staged by every thread; every warp is done with RHS b - 1 (its buffer and the partial sums)
+    if (!stalled) stalled = !zt_mbar_wait(&sm.bar[b & 1], (b >> 1) & 1);   // RHS b staged
+    // every warp is done with RHS b - 1 (its buffer and the partial sums)
     __syncthreads();
-    if (b + 1 < nrhs) zt_stage<NZ>(sm.in[(b + 1) & 1], src0 + (int64_t)(b + 1) * 5 * comp, nz, plane, comp, kx0, X);
+    if (threadIdx.x == 0 && b + 1 < nrhs && !stalled)
+      zt_issue(&map, reinterpret_cast<unsigned char*>(sm.in[(b + 1) & 1]), cbytes, &sm.bar[(b + 1) & 1], kx0, ky,
+               b + 1, nz, bytes);
     const float2* s = &sm.in[b & 1][0][0][lane];
     float2 acc[NZ];
 #pragma unroll
@@ -241,6 +293,11 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(float2* __restrict__ Bf, 
         acc[m].y += (bb.y - a.y) - pp.y;
       }
     }
+    if (stalled) {   // the copies never completed: the product is NaN, and the pass says so
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) acc[m] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+      g_zt_stalled = 1;
+    }
     if (ok) {   // the warp's output component
       float2* out = Bf + (int64_t)b * 5 * comp + (int64_t)warp * comp + (int64_t)ky * X + kx;
 #pragma unroll
@@ -259,8 +316,9 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(float2* __restrict__ Bf, 
 template <int NZ>
 struct ZtSmemDf {
   dfloat h2[7][2 * NZ - 1][kZtCols];
-  dcomplex in[5][NZ][kZtCols];
+  dcomplex in[5][NZ][kZtCols];   // 128-byte aligned
   dcomplex part[3][NZ][kZtCols];
+  uint64_t bar;
 };
 
 // (re, im)[m] += sum_n h[m - n] v(n) for n < nz; v(n) = p1[n] (+ or - p2[n] with PAIR), times i with
@@ -287,10 +345,12 @@ __device__ __forceinline__ void zt_conv_df(df_dot (&re)[NZ], df_dot (&im)[NZ], c
 }
 
 template <int NZ>
-__global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(dcomplex* __restrict__ Bf, const float* __restrict__ gz,
+__global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(const __grid_constant__ CUtensorMap map,
+                                                         dcomplex* __restrict__ Bf, const float* __restrict__ gz,
                                                          const float* __restrict__ gzlo, int nz, int Y, int X,
                                                          int nrhs) {
-  extern __shared__ __align__(16) unsigned char zt_raw[];
+  static_assert(offsetof(ZtSmemDf<NZ>, in) % 128 == 0, "copy destinations 128-byte aligned");
+  extern __shared__ __align__(128) unsigned char zt_raw[];
   ZtSmemDf<NZ>& sm = *reinterpret_cast<ZtSmemDf<NZ>*>(zt_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ky = blockIdx.y;
@@ -302,6 +362,10 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(dcomplex* __restrict__
   for (int i = threadIdx.x; i < 5 * NZ * kZtCols; i += blockDim.x) {   // padding rows nz.. stay zero
     const int col = i % kZtCols, n = (i / kZtCols) % NZ, c = i / (kZtCols * NZ);
     if (n >= nz) sm.in[c][n][col] = dcomplex{dfloat(0.0f), dfloat(0.0f)};
+  }
+  if (threadIdx.x == 0) {
+    zt_mbar_init(&sm.bar);
+    zt_mbar_fence_init();
   }
   for (int i = threadIdx.x; i < 7 * (2 * NZ - 1) * kZtCols; i += blockDim.x) {
     const int col = i % kZtCols, j = (i / kZtCols) % (2 * NZ - 1), k = i / (kZtCols * (2 * NZ - 1));
@@ -315,19 +379,15 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(dcomplex* __restrict__
     sm.h2[k][j][col] = h;
   }
   constexpr int ck = NZ * kZtCols;   // in[c + 1] - in[c]
+  const unsigned bytes = 5u * (unsigned)nz * kZtCols * sizeof(dcomplex);
+  bool stalled = (zt_smem(sm.in) & 127u) != 0;   // the copies want 128-byte aligned destinations
   for (int b = 0; b < nrhs; ++b) {
-    __syncthreads();   // every warp is done with RHS b - 1 (the staged inputs and the partial sums)
-    {
-      const dcomplex* src = Bf + (int64_t)b * 5 * comp + (int64_t)ky * X + kx0;
-      for (int i = threadIdx.x; i < 5 * nz * kZtCols; i += blockDim.x) {   // one 16-byte value per copy
-        const int col = i % kZtCols, cn = i / kZtCols;
-        const int c = cn / nz, n = cn - c * nz;
-        if (kx0 + col < X) zt_cp16(&sm.in[c][n][col], src + c * comp + n * plane + col);
-      }
-      zt_commit();
-      zt_wait<0>();
-    }
+    // every warp is done with RHS b - 1 (the staged inputs and the partial sums); the barrier is
+    // initialised and the table written (first pass)
     __syncthreads();
+    if (threadIdx.x == 0 && !stalled)
+      zt_issue(&map, reinterpret_cast<unsigned char*>(sm.in), sizeof(sm.in[0]), &sm.bar, 2 * kx0, ky, b, nz, bytes);
+    if (!stalled) stalled = !zt_mbar_wait(&sm.bar, b & 1);
     const dcomplex* s = &sm.in[0][0][lane];
     df_dot re[NZ], im[NZ];
 #pragma unroll
@@ -370,6 +430,12 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(dcomplex* __restrict__
         im[m].merge(-pp.y.hi, -pp.y.lo);
       }
     }
+    if (stalled) {   // the copies never completed: the product is NaN, and the pass says so
+      const float qnan = __int_as_float(0x7fc00000);
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) re[m] = im[m] = df_dot(dfloat(qnan));
+      g_zt_stalled = 1;
+    }
     if (ok) {   // the warp's output component
       dcomplex* out = Bf + (int64_t)b * 5 * comp + (int64_t)warp * comp + (int64_t)ky * X + kx;
 #pragma unroll
@@ -379,25 +445,61 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(dcomplex* __restrict__
   }
 }
 
-template <int NZ>
-void launch_zpass_toep_df(dcomplex* Bf, const float* gz, const float* gzlo, int nz, int Y, int X, int B,
-                          cudaStream_t st) {
-  constexpr size_t sm = sizeof(ZtSmemDf<NZ>);
-  allow_dyn_smem(k_zpass_toep_df<NZ>, sm);
-  dim3 grid((unsigned)ceil_div(X, kZtCols), (unsigned)Y);
-  k_zpass_toep_df<NZ><<<grid, 5 * 32, sm, st>>>(Bf, gz, gzlo, nz, Y, X, B);
-  count_launch();
-  VH_CUDA_TRY(cudaGetLastError());
+// the driver's tensor-map encoder, looked up once through the runtime
+PFN_cuTensorMapEncodeTiled_v12000 zt_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// The staging tensor of the B right-hand sides in Bf (W 64-bit elements per value); false where the
+// layout does not meet the copy engine's rules (16-byte base and row strides), and the pass is then not
+// run (the FFT z-pass runs instead).
+bool zt_tensor_map(CUtensorMap* map, const void* Bf, int W, int X, int Y, int B, int nz) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = zt_encoder();
+  const uint64_t row = (uint64_t)X * W * 8;
+  if (!enc || reinterpret_cast<uintptr_t>(Bf) % 16 != 0 || row % 16 != 0) return false;
+  const cuuint64_t dim[3] = {(cuuint64_t)X * W, (cuuint64_t)Y, (cuuint64_t)B * 5 * nz};
+  const cuuint64_t stride[2] = {row, row * (uint64_t)Y};
+  const cuuint32_t box[3] = {(cuuint32_t)(kZtCols * W), 1u, (cuuint32_t)nz};
+  const cuuint32_t step[3] = {1u, 1u, 1u};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void*>(Bf), dim, stride, box, step,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <int NZ>
-void launch_zpass_toep(float2* Bf, const float* gz, int nz, int Y, int X, int B, cudaStream_t st) {
+bool launch_zpass_toep_df(dcomplex* Bf, const float* gz, const float* gzlo, int nz, int Y, int X, int B,
+                          cudaStream_t st) {
+  CUtensorMap map;
+  if (!zt_tensor_map(&map, Bf, 2, X, Y, B, nz)) return false;
+  constexpr size_t sm = sizeof(ZtSmemDf<NZ>);
+  allow_dyn_smem(k_zpass_toep_df<NZ>, sm);
+  dim3 grid((unsigned)ceil_div(X, kZtCols), (unsigned)Y);
+  k_zpass_toep_df<NZ><<<grid, 5 * 32, sm, st>>>(map, Bf, gz, gzlo, nz, Y, X, B);
+  count_launch();
+  VH_CUDA_TRY(cudaGetLastError());
+  return true;
+}
+
+template <int NZ>
+bool launch_zpass_toep(float2* Bf, const float* gz, int nz, int Y, int X, int B, cudaStream_t st) {
+  CUtensorMap map;
+  if (!zt_tensor_map(&map, Bf, 1, X, Y, B, nz)) return false;
   constexpr size_t sm = sizeof(ZtSmem<NZ>);
   allow_dyn_smem(k_zpass_toep<NZ>, sm);
   dim3 grid((unsigned)ceil_div(X, kZtCols), (unsigned)Y);
-  k_zpass_toep<NZ><<<grid, 5 * 32, sm, st>>>(Bf, gz, nz, Y, X, B);
+  k_zpass_toep<NZ><<<grid, 5 * 32, sm, st>>>(map, Bf, gz, nz, Y, X, B);
   count_launch();
   VH_CUDA_TRY(cudaGetLastError());
+  return true;
 }
 
 }  // namespace
@@ -441,39 +543,49 @@ bool ztoep_build(ConvPlan& p, cudaStream_t st) {
   return true;
 }
 
+bool ztoep_take_stall(cudaStream_t st) {
+  int v = 0;
+  VH_CUDA_TRY(cudaMemcpyFromSymbolAsync(&v, g_zt_stalled, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  VH_CUDA_TRY(cudaStreamSynchronize(st));
+  if (v != 0) {
+    const int zero = 0;
+    VH_CUDA_TRY(cudaMemcpyToSymbolAsync(g_zt_stalled, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+    VH_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return v != 0;
+}
+
 bool zpass_toep_df(const ConvPlan& p, dcomplex* Bf, int B, cudaStream_t st) {
   if (p.ztoep_state <= 0 || !p.tensz) return false;
   const int nz = p.nz;
   const float* lo = p.tensz + (int64_t)7 * nz * p.Y * p.X;
   switch ((nz + 1) / 2) {
-    case 1: launch_zpass_toep_df<2>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
-    case 2: launch_zpass_toep_df<4>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
-    case 3: launch_zpass_toep_df<6>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
-    case 4: launch_zpass_toep_df<8>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
-    case 5: launch_zpass_toep_df<10>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
-    case 6: launch_zpass_toep_df<12>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
-    case 7: launch_zpass_toep_df<14>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
-    case 8: launch_zpass_toep_df<16>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st); break;
+    case 1: return launch_zpass_toep_df<2>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
+    case 2: return launch_zpass_toep_df<4>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
+    case 3: return launch_zpass_toep_df<6>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
+    case 4: return launch_zpass_toep_df<8>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
+    case 5: return launch_zpass_toep_df<10>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
+    case 6: return launch_zpass_toep_df<12>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
+    case 7: return launch_zpass_toep_df<14>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
+    case 8: return launch_zpass_toep_df<16>(Bf, p.tensz, lo, nz, p.Y, p.X, B, st);
     default: return false;
   }
-  return true;
 }
 
 bool zpass_toep(const ConvPlan& p, float2* Bf, int B, cudaStream_t st) {
   if (p.ztoep_state <= 0 || !p.tensz) return false;
   const int nz = p.nz;
   switch ((nz + 1) / 2) {
-    case 1: launch_zpass_toep<2>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
-    case 2: launch_zpass_toep<4>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
-    case 3: launch_zpass_toep<6>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
-    case 4: launch_zpass_toep<8>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
-    case 5: launch_zpass_toep<10>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
-    case 6: launch_zpass_toep<12>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
-    case 7: launch_zpass_toep<14>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
-    case 8: launch_zpass_toep<16>(Bf, p.tensz, nz, p.Y, p.X, B, st); break;
+    case 1: return launch_zpass_toep<2>(Bf, p.tensz, nz, p.Y, p.X, B, st);
+    case 2: return launch_zpass_toep<4>(Bf, p.tensz, nz, p.Y, p.X, B, st);
+    case 3: return launch_zpass_toep<6>(Bf, p.tensz, nz, p.Y, p.X, B, st);
+    case 4: return launch_zpass_toep<8>(Bf, p.tensz, nz, p.Y, p.X, B, st);
+    case 5: return launch_zpass_toep<10>(Bf, p.tensz, nz, p.Y, p.X, B, st);
+    case 6: return launch_zpass_toep<12>(Bf, p.tensz, nz, p.Y, p.X, B, st);
+    case 7: return launch_zpass_toep<14>(Bf, p.tensz, nz, p.Y, p.X, B, st);
+    case 8: return launch_zpass_toep<16>(Bf, p.tensz, nz, p.Y, p.X, B, st);
     default: return false;
   }
-  return true;
 }
 
 }  // namespace vh

@@ -1059,6 +1059,7 @@ vh_status vh_gmres_device_x0(vh_geom* g, int B, vh_precon* const* pcs, const voi
     VH_CUDA_TRY(cudaSetDevice(g->ctx->device));
     gmres_dispatch(g, B, pcs, (const double2*)b_dev, scale, zslot, restart, tol, maxit, flexible, prec,
                    (const double2*)x0_dev, (double2*)x_dev, flag, relres, iter, resvec, resvec_len, nres);
+    VH_REQUIRE(!ztoep_take_stall(g->ctx->stream), ERR_TIMEOUT, "a z-pass gave up waiting for its staging copies");
   });
 }
 
@@ -1088,6 +1089,7 @@ vh_status vh_gmres_x0(vh_geom* g, int B, vh_precon* const* pcs, const double* b,
                    relres, iter, resvec, resvec_len, nres);
     VH_CUDA_TRY(cudaMemcpyAsync(x, dx.p, (size_t)B * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VH_CUDA_TRY(cudaStreamSynchronize(st));
+    VH_REQUIRE(!ztoep_take_stall(st), ERR_TIMEOUT, "a z-pass gave up waiting for its staging copies");
   });
 }
 
