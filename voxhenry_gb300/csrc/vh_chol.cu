@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps, (STAGE || std::is_same<T, do
       Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * nf] : T(0);
     __syncwarp();
     Dot xx(T(0)), xy(T(0));
-#pragma unroll
+#pragma unroll 4   // a serial Dot2 chain: unrolling further adds code, not overlap
     for (int k = 0; k < kBlk; ++k) {
       if (k < w) {
         const T l = Lb[k][lane];
