@@ -1250,7 +1250,7 @@ __global__ void __launch_bounds__(32 * kWideWarps)
         Lb[lane][k] = (k < w && lane < w && lane >= k) ? F[(j0 + lane) + (int64_t)(j0 + k) * ld] : T(0);
       __syncwarp();
       Dot xx(T(0)), xy(T(0));
-#pragma unroll
+#pragma unroll 4   // one serial Dot2 chain, as in k_chol_bsolve
       for (int k = 0; k < kBlk; ++k)
         if (k < w) {
           const T l = Lb[k][lane];
