@@ -31,7 +31,7 @@ typedef enum vh_status {
   VH_ERR_BAD_ARG = 1,
   VH_ERR_OOM = 2,
   VH_ERR_UNSUPPORTED = 3,
-  VH_ERR_TIMEOUT = 4,
+  VH_ERR_TIMEOUT = 4,   /* a device wait gave up (the Toeplitz z-pass's tensor copies); products NaN */
   VH_ERR_NOT_CONVERGED = 5,
   VH_ERR_CUDA = 6,
   VH_ERR_NO_DEVICE = 7
