@@ -1,12 +1,13 @@
-// Pass 3 of the complex64 FFT convolution as a direct convolution along z (the autotuner's
-// z_variant 3).  After the x- and y-transforms every (kx, ky) column holds nz voxel rows of the five
+// Pass 3 of the complex64 and double-float FFT convolutions as a direct convolution along z (the
+// autotuner's z_variant 3).  After the x- and y-transforms every (kx, ky) column holds nz voxel rows of the five
 // current components, and the circulant's z-part acts on them as a Toeplitz operator: with the tensor
 // spectrum S_k(kx, ky, kz) (already divided by X Y Z),
 //   out[m] = sum_n h_k[m - n] in[n],   h_k[d] = sum_kz S_k[kz] e^{+2 pi i kz d / Z},   0 <= m, n < nz,
 // which is exactly what the z-FFT, the product with S_k and the inverse z-FFT compute (the operator of
-// lse_matvect_mult.m:57-93 along z).  For nz rows the direct form costs 15 nz^2 complex-by-real
-// multiply-adds per column against ten pruned Z-point transforms and 13 Z products, and needs no
-// exchange between threads: at nz <= 16 it is the cheaper form.
+// lse_matvect_mult.m:57-93 along z).  For nz rows the direct form costs 13 nz^2 complex-by-real
+// multiply-adds per column (13 distinct convolutions) against ten pruned Z-point transforms and 13 Z
+// products, and needs no exchange between threads: at nz <= 16 it is the cheaper form.  The inputs
+// of each right-hand side reach shared memory by tensor-memory-accelerator copies.
 //
 // The kernel is even or odd along each axis, so h_k is real (components 0, 3, 4, 5, 6) or imaginary
 // (1, 2), even in d except for component 4 (odd): one float per (k, d >= 0).  The table is built on
