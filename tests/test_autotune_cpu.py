@@ -15,6 +15,10 @@ def test_keys_group_batch_widths_and_separate_shapes():
     assert k != autotune.tuning_key((512, 512, 16), (311, 10), "fp32", 17, device="GB300")
     assert k != autotune.tuning_key((512, 512, 16), (311, 10), "df", 16, device="GB300")
     assert k != autotune.tuning_key((256, 256, 8), (311, 10), "fp32", 16, device="GB300")
+    # a rebuilt library (other kernel sources) does not reuse the choices timed on the old one
+    assert autotune.tuning_key((512, 512, 16), (311, 10), "fp32", 16, device="GB300", lib="0123456789ab") != \
+        autotune.tuning_key((512, 512, 16), (311, 10), "fp32", 16, device="GB300", lib="ba9876543210")
+    assert "|lib=" in k
 
 
 def test_tune_times_once_then_uses_the_cache(tmp_path):

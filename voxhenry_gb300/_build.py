@@ -41,6 +41,16 @@ def _digest(srcs, hdrs) -> str:
     return h.hexdigest()
 
 
+def build_id() -> str:
+    """The first 12 hex digits of the source digest the library was last built from ("unbuilt"
+    without a stamp): it names the kernels a cached launch choice was timed on."""
+    try:
+        with open(os.path.join(BUILD, "stamp")) as f:
+            return f.read().strip()[:12] or "unbuilt"
+    except OSError:
+        return "unbuilt"
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile every source under csrc/ and link libvhgpu.so; returns its path."""
     srcs, hdrs = _sources()

@@ -6,8 +6,10 @@ lengths 256, 512, 1024 over 128- or 64-byte rows, or the shared-memory Stockham 
 lanes per column, one thread per column for padded z lengths up to 32, or the direct Toeplitz
 convolution for voxel boxes up to 16 rows), the x passes (complex64: one warp per line for padded x
 lengths 256, 512, 1024) and how many right-hand sides share one launch sequence.  vh_conv_tune times the candidates on the geometry itself with CUDA events; the
-choice is cached in a JSON file keyed by the GPU, the grid, the voxel box, the precision and the
-batch width, so later runs (and other geometries of the same shape) apply it without timing.
+choice is cached in a JSON file keyed by the GPU, the library build (the digest of the sources its
+kernels were compiled from: a rebuilt library times its choices again), the grid, the voxel box, the
+precision and the batch width, so later runs (and other geometries of the same shape) apply it
+without timing.
 
 Cache file: $VOXHENRY_TUNE_CACHE, else ~/.cache/voxhenry_gb300/conv_tuning.json.
 """
@@ -18,7 +20,7 @@ import json
 import os
 import threading
 
-from . import _lib
+from . import _build, _lib
 
 PREC = _lib.PREC
 _lock = threading.Lock()
@@ -40,13 +42,15 @@ def device_name() -> str:
     return "unknown"
 
 
-def tuning_key(grid, box, prec: str, B: int, device: str | None = None) -> str:
+def tuning_key(grid, box, prec: str, B: int, device: str | None = None, lib: str | None = None) -> str:
     """grid: (L, M, N); box: (ny, nz) voxel box of the FFT passes; B: right-hand sides per call
-    (rounded up to a power of two: nearby batch widths share a choice)."""
+    (rounded up to a power of two: nearby batch widths share a choice); lib: the library build
+    (default: the one in the package)."""
     b = 1
     while b < B:
         b *= 2
-    return f"{device or device_name()}|grid={grid[0]}x{grid[1]}x{grid[2]}|box={box[0]}x{box[1]}|{prec}|B<={b}"
+    return (f"{device or device_name()}|lib={lib or _build.build_id()}|grid={grid[0]}x{grid[1]}x{grid[2]}"
+            f"|box={box[0]}x{box[1]}|{prec}|B<={b}")
 
 
 def load_cache(path: str | None = None) -> dict:
