@@ -236,8 +236,11 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(const __grid_constant__ C
   __syncthreads();
   // the copies want 128-byte aligned destinations (checked, not assumed: a pass that cannot copy says so)
   const bool aligned = (zt_smem(sm.in) & 127u) == 0;
-  if (threadIdx.x == 0 && nrhs > 0 && aligned)
+  int last = -1;   // thread 0: the last RHS whose copies it issued
+  if (threadIdx.x == 0 && nrhs > 0 && aligned) {
     zt_issue(&map, reinterpret_cast<unsigned char*>(sm.in[0]), cbytes, &sm.bar[0], kx0, ky, 0, nz, bytes);
+    last = 0;
+  }
   for (int i = threadIdx.x; i < 7 * NZ * kZtCols; i += blockDim.x) {
     const int cc = i % kZtCols, d = (i / kZtCols) % NZ, k = i / (kZtCols * NZ);
     sm.g[k][cc][d] = (kx0 + cc < X && d < nz) ? gz[(((int64_t)ky * 7 + k) * nz + d) * X + kx0 + cc] : 0.0f;
@@ -250,9 +253,11 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(const __grid_constant__ C
     if (!stalled) stalled = !zt_mbar_wait(&sm.bar[b & 1], (b >> 1) & 1);   // RHS b staged
     // every warp is done with RHS b - 1 (its buffer and the partial sums)
     __syncthreads();
-    if (threadIdx.x == 0 && b + 1 < nrhs && !stalled)
+    if (threadIdx.x == 0 && b + 1 < nrhs && !stalled) {
       zt_issue(&map, reinterpret_cast<unsigned char*>(sm.in[(b + 1) & 1]), cbytes, &sm.bar[(b + 1) & 1], kx0, ky,
                b + 1, nz, bytes);
+      last = b + 1;
+    }
     const float2* s = &sm.in[b & 1][0][0][lane];
     float2 acc[NZ];
 #pragma unroll
@@ -306,6 +311,10 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep(const __grid_constant__ C
         if (m < nz) out[m * plane] = acc[m];
     }
   }
+  // thread 0 issues only after its own wait succeeded, so when it gave up, the copies it waited for
+  // (its last issue) may still be in flight: one more bounded wait before the block's shared memory
+  // is released
+  if (threadIdx.x == 0 && stalled && last >= 0) zt_mbar_wait(&sm.bar[last & 1], (last >> 1) & 1);
 }
 
 // ---- the same pass in double-float arithmetic (VH_PREC_DF: pair storage of Bf, pair h values, each
@@ -382,12 +391,15 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(const __grid_constant_
   constexpr int ck = NZ * kZtCols;   // in[c + 1] - in[c]
   const unsigned bytes = 5u * (unsigned)nz * kZtCols * sizeof(dcomplex);
   bool stalled = (zt_smem(sm.in) & 127u) != 0;   // the copies want 128-byte aligned destinations
+  int last = -1;                                  // thread 0: the last RHS whose copies it issued
   for (int b = 0; b < nrhs; ++b) {
     // every warp is done with RHS b - 1 (the staged inputs and the partial sums); the barrier is
     // initialised and the table written (first pass)
     __syncthreads();
-    if (threadIdx.x == 0 && !stalled)
+    if (threadIdx.x == 0 && !stalled) {
       zt_issue(&map, reinterpret_cast<unsigned char*>(sm.in), sizeof(sm.in[0]), &sm.bar, 2 * kx0, ky, b, nz, bytes);
+      last = b;
+    }
     if (!stalled) stalled = !zt_mbar_wait(&sm.bar, b & 1);
     const dcomplex* s = &sm.in[0][0][lane];
     df_dot re[NZ], im[NZ];
@@ -444,6 +456,8 @@ __global__ void __launch_bounds__(5 * 32) k_zpass_toep_df(const __grid_constant_
         if (m < nz) out[m * plane] = dcomplex{re[m].value(), im[m].value()};
     }
   }
+  // a copy thread 0 gave up on may still be in flight: one more bounded wait before exit
+  if (threadIdx.x == 0 && stalled && last >= 0) zt_mbar_wait(&sm.bar, last & 1);
 }
 
 // the driver's tensor-map encoder, looked up once through the runtime
